@@ -1,0 +1,115 @@
+"""ctypes binding of libhodlrnd_gb300.so (the C ABI in include/hodlrnd.h).
+
+There is no fallback: if the library is missing this raises, naming the
+build command.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhodlrnd_gb300.so")
+
+HODLR_OK = 0
+HODLR_ERR_INVALID = 1
+HODLR_ERR_CUDA = 2
+HODLR_ERR_OOM = 3
+HODLR_ERR_BUDGET = 4
+HODLR_ERR_NOT_CONVERGED = 5
+HODLR_ERR_TREE = 6
+HODLR_ERR_STATE = 7
+HODLR_ERR_DEVICE = 8
+
+HODLR_KERNEL_INV_R = 1
+HODLR_KERNEL_INV_R2 = 2
+HODLR_KERNEL_LOG_R = 3
+HODLR_KERNEL_EXP_NEG_R = 4
+
+HODLR_PREC_FP64 = 0
+HODLR_PREC_MIXED = 1
+
+
+class HodlrParams(ctypes.Structure):
+    _fields_ = [("ndim", ctypes.c_int32), ("nmax", ctypes.c_int32), ("dprime", ctypes.c_int32),
+                ("restart", ctypes.c_int32), ("eps_aca", ctypes.c_double), ("tol", ctypes.c_double),
+                ("max_iter", ctypes.c_int64), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("device_budget_bytes", ctypes.c_uint64), ("rank_cap", ctypes.c_int32),
+                ("max_outer", ctypes.c_int32), ("inner_tol", ctypes.c_double)]
+
+
+class HodlrKernelDesc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("reserved", ctypes.c_int32), ("scale", ctypes.c_double),
+                ("diag", ctypes.c_double)]
+
+
+class HodlrSolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int64), ("outer_iterations", ctypes.c_int64),
+                ("rel_residual", ctypes.c_double), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("seconds", ctypes.c_double)]
+
+
+class HodlrStats(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int64) for k in ("n", "depth", "n_leaves", "n_far_blocks", "n_dense_far_blocks",
+                                              "n_near_blocks", "max_rank")] + \
+               [(k, ctypes.c_double) for k in ("n_flop", "memory_gb", "compression_ratio")] + \
+               [(k, ctypes.c_uint64) for k in ("near_bytes", "far_bytes", "device_bytes")] + \
+               [(k, ctypes.c_double) for k in ("t_tree_s", "t_aca_s", "t_near_s", "t_build_s", "t_matvec_s",
+                                               "far_entries", "dense_far_entries", "near_entries")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HodlrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[hodlr error {code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m hodlrnd_gb300.build` "
+                          "(there is no CPU fallback)")
+    L = ctypes.CDLL(LIB_PATH)
+    P, D, I64, I32 = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64), \
+        ctypes.POINTER(ctypes.c_int32)
+    L.hodlr_params_default.argtypes = [ctypes.POINTER(HodlrParams)]
+    L.hodlr_params_default.restype = None
+    L.hodlr_ctx_create.argtypes = [ctypes.POINTER(HodlrParams), ctypes.POINTER(P)]
+    L.hodlr_ctx_destroy.argtypes = [P]
+    L.hodlr_last_error.argtypes = [P]
+    L.hodlr_last_error.restype = ctypes.c_char_p
+    L.hodlr_build.argtypes = [P, D, ctypes.c_int64, D, D, ctypes.POINTER(HodlrKernelDesc), ctypes.POINTER(P)]
+    L.hodlr_op_destroy.argtypes = [P]
+    L.hodlr_matvec.argtypes = [P, D, D, ctypes.c_int64]
+    L.hodlr_matvec_device.argtypes = [P, P, P, ctypes.c_int64, P]
+    L.hodlr_solve.argtypes = [P, D, D, ctypes.c_int64, ctypes.POINTER(HodlrSolveInfo)]
+    L.hodlr_solve_device.argtypes = [P, P, P, ctypes.c_int64, P, ctypes.POINTER(HodlrSolveInfo)]
+    L.hodlr_stats_get.argtypes = [P, ctypes.POINTER(HodlrStats)]
+    L.hodlr_get_permutation.argtypes = [P, I64]
+    L.hodlr_get_blocks.argtypes = [P, I32, I64, I64, I32]
+    L.hodlr_tree_build.argtypes = [ctypes.POINTER(HodlrParams), D, ctypes.c_int64, D, D, ctypes.POINTER(P)]
+    L.hodlr_tree_sizes.argtypes = [P, I64]
+    L.hodlr_tree_get.argtypes = [P, I64, I64, I64, I64, I64, I64, I64]
+    L.hodlr_tree_destroy.argtypes = [P]
+    for f in ("hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
+              "hodlr_matvec_device", "hodlr_solve", "hodlr_solve_device", "hodlr_stats_get",
+              "hodlr_get_permutation", "hodlr_get_blocks", "hodlr_tree_build", "hodlr_tree_sizes",
+              "hodlr_tree_get", "hodlr_tree_destroy"):
+        getattr(L, f).restype = ctypes.c_int
+    _lib = L
+    return L
+
+
+def last_error(ctx=None):
+    return lib().hodlr_last_error(ctx).decode(errors="replace")
+
+
+def check(code, ctx=None):
+    if code != HODLR_OK:
+        raise HodlrError(code, last_error(ctx))

@@ -1,0 +1,156 @@
+// Device-side helpers shared by the HODLRnD GB300 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hodlr {
+
+// Kernel kinds (include/hodlrnd.h).
+enum : int { kInvR = 1, kInvR2 = 2, kLogR = 3, kExpNegR = 4 };
+
+struct KernelDev {
+  int kind;
+  double scale, diag;
+};
+
+// Points in tree order, structure of arrays: coordinate k of point i is
+// x[k * ld + i].
+struct PointsDev {
+  const double* x;
+  int64_t ld;
+};
+
+// One matrix entry A(i, j) for tree positions i, j (kernel_function::getRow /
+// getCol / getMatrix + the user getMatrixEntry, include/kernel_function.hpp:20-53).
+// d2 is accumulated in dimension order with one rounding per operation (the
+// explicit _rn intrinsics keep the compiler from contracting into FMAs), so
+// the entry is bit-identical to the scalar host code; sqrt and division are
+// IEEE round-to-nearest on both sides.
+template <int D>
+__device__ __forceinline__ double kernel_entry(const PointsDev& P, const KernelDev& K, int64_t i, int64_t j,
+                                               const double* xi) {
+  if (i == j) return K.diag;
+  double d2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    const double t = __dsub_rn(xi[k], P.x[k * P.ld + j]);
+    d2 = __dadd_rn(d2, __dmul_rn(t, t));
+  }
+  switch (K.kind) {
+    case kInvR: return __ddiv_rn(K.scale, __dsqrt_rn(d2));
+    case kInvR2: return __ddiv_rn(K.scale, d2);
+    case kLogR: return __dmul_rn(K.scale, log(__dsqrt_rn(d2)));
+    default: return __dmul_rn(K.scale, exp(-__dsqrt_rn(d2)));
+  }
+}
+
+template <int D>
+__device__ __forceinline__ void load_point(const PointsDev& P, int64_t i, double* xi) {
+#pragma unroll
+  for (int k = 0; k < D; k++) xi[k] = P.x[k * P.ld + i];
+}
+
+// ---------------------------------------------------------------- teams
+// A "team" is the group of threads that compresses one block: a warp, or a
+// whole CTA.  All members call every team function (uniform control flow).
+
+struct WarpTeam {
+  static constexpr int kSize = 32;
+  __device__ __forceinline__ int tid() const { return threadIdx.x & 31; }
+  __device__ __forceinline__ void sync() const { __syncwarp(); }
+  __device__ __forceinline__ double sum(double v) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+  }
+  // Largest |v|, lowest index on ties (kernel_function::maxAbsVector keeps the
+  // first maximum, include/kernel_function.hpp:55-68).
+  __device__ __forceinline__ void argmax(double& a, int& i, double& v) const {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double a2 = __shfl_xor_sync(0xffffffffu, a, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+      const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      if (a2 > a || (a2 == a && i2 < i)) {
+        a = a2;
+        i = i2;
+        v = v2;
+      }
+    }
+  }
+  __device__ __forceinline__ int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
+  __device__ __forceinline__ double bcast(double v) const { return __shfl_sync(0xffffffffu, v, 0); }
+};
+
+template <int NT>
+struct CtaTeam {
+  static constexpr int kSize = NT;
+  static constexpr int kWarps = NT / 32;
+  double* red;  // shared, kWarps + 1
+  int* redi;    // shared, kWarps + 1
+  __device__ __forceinline__ int tid() const { return threadIdx.x; }
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+  __device__ __forceinline__ double sum(double v) const {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      v = lane < kWarps ? red[lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[kWarps] = v;
+    }
+    __syncthreads();
+    v = red[kWarps];
+    __syncthreads();
+    return v;
+  }
+  __device__ __forceinline__ void argmax(double& a, int& i, double& v) const {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    WarpTeam().argmax(a, i, v);
+    __shared__ double sa[kWarps + 1], sv[kWarps + 1];
+    if (lane == 0) {
+      sa[w] = a;
+      sv[w] = v;
+      redi[w] = i;
+    }
+    __syncthreads();
+    if (w == 0) {
+      a = lane < kWarps ? sa[lane] : -1.0;
+      i = lane < kWarps ? redi[lane] : 0x7fffffff;
+      v = lane < kWarps ? sv[lane] : 0.0;
+      WarpTeam().argmax(a, i, v);
+      if (lane == 0) {
+        sa[kWarps] = a;
+        sv[kWarps] = v;
+        redi[kWarps] = i;
+      }
+    }
+    __syncthreads();
+    a = sa[kWarps];
+    v = sv[kWarps];
+    i = redi[kWarps];
+    __syncthreads();
+  }
+  __device__ __forceinline__ int bcast(int v) const {
+    if (threadIdx.x == 0) redi[kWarps] = v;
+    __syncthreads();
+    v = redi[kWarps];
+    __syncthreads();
+    return v;
+  }
+  __device__ __forceinline__ double bcast(double v) const {
+    if (threadIdx.x == 0) red[kWarps] = v;
+    __syncthreads();
+    v = red[kWarps];
+    __syncthreads();
+    return v;
+  }
+};
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace hodlr

@@ -1,0 +1,999 @@
+// C ABI of the GB300 HODLRnD engine (include/hodlrnd.h): build pipeline,
+// operator application and solves.  One process, one GPU; all device memory
+// of an operator is owned by its hodlr_op.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/hodlrnd.h"
+#include "aca.h"
+#include "gmres.h"
+#include "matvec.h"
+#include "tree.hpp"
+
+using namespace hodlr;
+
+namespace {
+
+thread_local std::string g_thread_err;
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Failure {
+  int code;
+  std::string msg;
+};
+
+void check_cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  const int code = (e == cudaErrorMemoryAllocation) ? HODLR_ERR_OOM : HODLR_ERR_CUDA;
+  throw Failure{code, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+#define CK(x) check_cuda((x), #x)
+
+// Device allocation tracked against the context's budget.
+struct DevMem {
+  uint64_t used = 0, budget = 0;
+  std::vector<std::pair<void*, size_t>> blocks;
+  void* alloc(size_t bytes, const char* what) {
+    if (bytes == 0) bytes = 16;
+    if (budget && used + bytes > budget)
+      throw Failure{HODLR_ERR_BUDGET, std::string(what) + ": device budget of " + std::to_string(budget) +
+                                          " bytes exceeded (" + std::to_string(used + bytes) + " needed)"};
+    void* p = nullptr;
+    check_cuda(cudaMalloc(&p, bytes), what);
+    used += bytes;
+    blocks.push_back({p, bytes});
+    return p;
+  }
+  template <typename T>
+  T* alloc_n(size_t n, const char* what) {
+    return static_cast<T*>(alloc(n * sizeof(T), what));
+  }
+  void release(void* p) {
+    for (size_t i = 0; i < blocks.size(); i++)
+      if (blocks[i].first == p) {
+        cudaFree(p);
+        used -= blocks[i].second;
+        blocks.erase(blocks.begin() + long(i));
+        return;
+      }
+  }
+  void release_all() {
+    for (auto& b : blocks) cudaFree(b.first);
+    blocks.clear();
+    used = 0;
+  }
+};
+
+template <typename T>
+T* upload(DevMem& mem, const std::vector<T>& v, cudaStream_t st, const char* what) {
+  T* d = mem.alloc_n<T>(std::max<size_t>(v.size(), 1), what);
+  if (!v.empty()) CK(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  return d;
+}
+
+uint64_t block_seed(int64_t level, int64_t t, int64_t s) {
+  // the same mixing as the CPU oracle's per-block mode
+  uint64_t h = 0x243F6A8885A308D3ull;
+  const uint64_t v[3] = {uint64_t(level), uint64_t(t), uint64_t(s)};
+  for (int i = 0; i < 3; i++) {
+    h ^= v[i] + 0x9E3779B97F4A7C15ull + (h << 6) + (h >> 2);
+    h *= 0xD6E8FEB86659FD93ull;
+    h ^= h >> 32;
+  }
+  return h;
+}
+
+// Device side of one way of applying the operator (a plan).
+struct Plan {
+  Prec a_near = Prec::kD, a_far = Prec::kD;
+  Panel* panels_near = nullptr;
+  Seg* segs_near = nullptr;
+  Item* items_near = nullptr;
+  int nitems_near = 0;
+  Panel* panels_far = nullptr;
+  Seg* segs_far = nullptr;
+  Item* items_far = nullptr;
+  int nitems_far = 0;
+  ZBlock* zb = nullptr;
+  int nzb = 0;
+};
+
+}  // namespace
+
+struct hodlr_ctx {
+  hodlr_params p;
+  std::string err;
+  cudaStream_t stream = nullptr;
+};
+
+struct hodlr_op {
+  hodlr_ctx* ctx = nullptr;
+  hodlr_params p;
+  hodlr_kernel_desc kd;
+  Tree tree;
+  std::vector<FarBlock> far;
+  NearList near;
+  std::vector<int32_t> rank, dense;
+  int64_t n = 0, zlen = 0;
+  int nslots = 0;
+  DevMem mem;
+  double* d_pts = nullptr;  // ndim x n, tree order
+  int64_t* d_perm = nullptr;
+  Plan plan64;        // FP64 operator, or the FP64-vector operator of MIXED (FP32 far factors)
+  Plan plan32;        // MIXED inner operator (all FP32)
+  // work vectors
+  double* d_in64 = nullptr;  // [x | z], n + zlen
+  double* d_y64 = nullptr;   // nslots x n
+  float* d_in32 = nullptr;
+  float* d_y32 = nullptr;
+  double* d_b64 = nullptr;   // tree-order right-hand side / solution / residual
+  double* d_x64 = nullptr;
+  double* d_r64 = nullptr;
+  float* d_r32 = nullptr;
+  float* d_d32 = nullptr;
+  double* d_io = nullptr;    // caller-order staging, n
+  double* d_io2 = nullptr;
+  double* d_part = nullptr;  // kVecCtas partials
+  double* d_scal = nullptr;  // scalars
+  double* h_scal = nullptr;  // pinned
+  GmresWork<double> g64;
+  GmresWork<float> g32;
+  hodlr_stats st;
+  ~hodlr_op() {
+    gmres_free(g64);
+    gmres_free(g32);
+    if (h_scal) cudaFreeHost(h_scal);
+    mem.release_all();
+  }
+};
+
+namespace {
+
+int fail(hodlr_ctx* ctx, int code, const std::string& msg) {
+  g_thread_err = msg;
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+// ---------------------------------------------------------------- build steps
+
+struct NearTiles {
+  std::vector<TileDesc> tiles;
+  int64_t total = 0;
+};
+
+NearTiles near_tiles(const Tree& t, const NearList& nl) {
+  NearTiles out;
+  const int L = t.levels - 1;
+  for (int64_t k = 0; k + 1 < int64_t(nl.leaf_ptr.size()); k++)
+    for (int64_t q = nl.leaf_ptr[size_t(k)]; q < nl.leaf_ptr[size_t(k + 1)]; q++) {
+      const int64_t s = nl.src[size_t(q)];
+      const int64_t gt = t.gid(L, k), gs = t.gid(L, s);
+      TileDesc d;
+      d.t_begin = t.begin[size_t(gt)];
+      d.s_begin = t.begin[size_t(gs)];
+      d.m = int32_t(t.count[size_t(gt)]);
+      d.n = int32_t(t.count[size_t(gs)]);
+      d.off = out.total;
+      out.total += int64_t(d.m) * d.n;
+      out.tiles.push_back(d);
+    }
+  return out;
+}
+
+void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a, Plan& plan, cudaStream_t st) {
+  const Tree& t = op->tree;
+  const int L = t.levels - 1;
+  std::vector<Panel> panels;
+  std::vector<Seg> segs;
+  std::vector<Item> items;
+  const size_t esz = a == Prec::kD ? 8 : 4;
+  size_t q = 0;
+  for (int64_t k = 0; k + 1 < int64_t(op->near.leaf_ptr.size()); k++) {
+    const int64_t b = op->near.leaf_ptr[size_t(k)], e = op->near.leaf_ptr[size_t(k + 1)];
+    if (b == e) continue;
+    Panel p;
+    p.row_begin = t.begin[size_t(t.gid(L, k))];
+    p.m = int32_t(t.count[size_t(t.gid(L, k))]);
+    p.slot = 0;
+    p.seg_begin = int64_t(segs.size());
+    for (int64_t z = b; z < e; z++, q++) {
+      const TileDesc& d = nt.tiles[q];
+      Seg s;
+      s.A = static_cast<const char*>(base) + size_t(d.off) * esz;
+      s.in_off = d.s_begin;
+      s.K = d.n;
+      s.pad = 0;
+      segs.push_back(s);
+    }
+    p.seg_end = int64_t(segs.size());
+    const int np = int(panels.size());
+    panels.push_back(p);
+    const int chunks = p.m <= 32 ? 1 : int((p.m + 31) / 32);
+    for (int c = 0; c < chunks; c++) items.push_back({np, c});
+  }
+  plan.a_near = a;
+  plan.panels_near = upload(op->mem, panels, st, "near panels");
+  plan.segs_near = upload(op->mem, segs, st, "near segments");
+  plan.items_near = upload(op->mem, items, st, "near items");
+  plan.nitems_near = int(items.size());
+}
+
+// Far-field plan from the per-block storage pointers.
+void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const std::vector<const void*>& vptr, Prec a,
+                    Plan& plan, cudaStream_t st) {
+  const Tree& t = op->tree;
+  std::vector<Panel> panels;
+  std::vector<Seg> segs;
+  std::vector<Item> items;
+  std::vector<ZBlock> zb;
+  int64_t zoff = op->n;
+  size_t b = 0;
+  while (b < op->far.size()) {
+    const int l = op->far[b].level;
+    const int64_t tk = op->far[b].t;
+    size_t e = b;
+    while (e < op->far.size() && op->far[e].level == l && op->far[e].t == tk) e++;
+    const int64_t gt = t.gid(l, tk);
+    Panel p;
+    p.row_begin = t.begin[size_t(gt)];
+    p.m = int32_t(t.count[size_t(gt)]);
+    p.slot = l;
+    p.seg_begin = int64_t(segs.size());
+    for (size_t q = b; q < e; q++) {
+      const int64_t gs = t.gid(l, op->far[q].s);
+      const int32_t ns = int32_t(t.count[size_t(gs)]);
+      Seg s;
+      s.pad = 0;
+      if (op->dense[q]) {
+        s.A = uptr[q];
+        s.in_off = t.begin[size_t(gs)];
+        s.K = ns;
+        segs.push_back(s);
+      } else if (op->rank[q] > 0) {
+        ZBlock z;
+        z.V = vptr[q];
+        z.x_off = t.begin[size_t(gs)];
+        z.z_off = zoff;
+        z.n = ns;
+        z.r = op->rank[q];
+        zb.push_back(z);
+        s.A = uptr[q];
+        s.in_off = zoff;
+        s.K = op->rank[q];
+        segs.push_back(s);
+        zoff += op->rank[q];
+      }
+    }
+    p.seg_end = int64_t(segs.size());
+    if (p.seg_end > p.seg_begin) {
+      const int np = int(panels.size());
+      panels.push_back(p);
+      const int chunks = p.m <= 32 ? 1 : int((p.m + 31) / 32);
+      for (int c = 0; c < chunks; c++) items.push_back({np, c});
+    }
+    b = e;
+  }
+  op->zlen = zoff - op->n;
+  plan.a_far = a;
+  plan.panels_far = upload(op->mem, panels, st, "far panels");
+  plan.segs_far = upload(op->mem, segs, st, "far segments");
+  plan.items_far = upload(op->mem, items, st, "far items");
+  plan.nitems_far = int(items.size());
+  plan.zb = upload(op->mem, zb, st, "far z blocks");
+  plan.nzb = int(zb.size());
+}
+
+// ACA of every far block, in workspace-bounded batches; compacted factors go
+// to per-batch chunks (FP64 or FP32) and uptr/vptr record where.
+void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std::vector<const void*>& vptr) {
+  const Tree& t = op->tree;
+  const size_t nb = op->far.size();
+  op->rank.assign(nb, 0);
+  op->dense.assign(nb, 0);
+  uptr.assign(nb, nullptr);
+  vptr.assign(nb, nullptr);
+  if (nb == 0) return;
+  const Prec fp = op->p.precision == HODLR_PREC_MIXED ? Prec::kF : Prec::kD;
+  const size_t esz = fp == Prec::kD ? 8 : 4;
+  const int cap0 = op->p.rank_cap > 0 ? op->p.rank_cap : 64;
+  std::vector<int32_t> cap(nb);
+  std::vector<int32_t> mm(nb), nn(nb);
+  std::vector<int64_t> tb(nb), sb(nb);
+  for (size_t b = 0; b < nb; b++) {
+    const int64_t gt = t.gid(op->far[b].level, op->far[b].t), gs = t.gid(op->far[b].level, op->far[b].s);
+    mm[b] = int32_t(t.count[size_t(gt)]);
+    nn[b] = int32_t(t.count[size_t(gs)]);
+    tb[b] = t.begin[size_t(gt)];
+    sb[b] = t.begin[size_t(gs)];
+    cap[b] = std::min({mm[b], nn[b], cap0});
+  }
+  auto ws_need = [&](size_t b) { return uint64_t(cap[b]) * uint64_t(mm[b] + nn[b]); };
+  // Scratch of one batch: the FP64 workspace is bounded (4 GiB by default);
+  // a single block that needs more grows it.  Not counted against the
+  // operator's memory: it is freed when the build returns.
+  const size_t max_batch = 1 << 20;
+  struct Scratch {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~Scratch() {
+      if (p) cudaFree(p);
+    }
+    void ensure(size_t need, cudaStream_t st, const char* what) {
+      if (need <= bytes) return;
+      check_cuda(cudaStreamSynchronize(st), what);
+      if (p) cudaFree(p);
+      p = nullptr;
+      bytes = 0;
+      check_cuda(cudaMalloc(&p, need), what);
+      bytes = need;
+    }
+  };
+  Scratch s_ws, s_bits, s_lists, s_desc, s_out, s_idx, s_cd;
+  const uint64_t ws_doubles = uint64_t(1) << 29;
+  const uint64_t bits_room = uint64_t(1) << 26, list_room = uint64_t(1) << 26;
+  s_desc.ensure(max_batch * sizeof(AcaBlockDesc), st, "ACA descriptors");
+  s_out.ensure(max_batch * sizeof(AcaOut), st, "ACA results");
+  s_idx.ensure(max_batch * sizeof(int32_t), st, "ACA team lists");
+  s_cd.ensure(max_batch * sizeof(CompactDesc), st, "compaction descriptors");
+  AcaBlockDesc* d_desc = static_cast<AcaBlockDesc*>(s_desc.p);
+  AcaOut* d_out = static_cast<AcaOut*>(s_out.p);
+  int32_t* d_lists_idx = static_cast<int32_t*>(s_idx.p);
+  CompactDesc* d_cd = static_cast<CompactDesc*>(s_cd.p);
+  std::vector<size_t> todo(nb);
+  for (size_t b = 0; b < nb; b++) todo[b] = b;
+  // large blocks first keeps the CTA-team launch ahead of the warp teams
+  std::stable_sort(todo.begin(), todo.end(), [&](size_t a, size_t b) {
+    return std::max(mm[a], nn[a]) > std::max(mm[b], nn[b]);
+  });
+
+  PointsDev P{op->d_pts, op->n};
+  KernelDev K{op->kd.kind, op->kd.scale, op->kd.diag};
+  size_t pos = 0;
+  std::vector<size_t> retry;
+  std::vector<AcaBlockDesc> desc;
+  std::vector<AcaOut> out;
+  std::vector<int32_t> warp_list, cta_list;
+  std::vector<CompactDesc> cds;
+  while (pos < todo.size() || !retry.empty()) {
+    // next batch
+    std::vector<size_t> batch;
+    uint64_t acc_w = 0, acc_b = 0, acc_l = 0;
+    auto take = [&](size_t b) {
+      const uint64_t w = ws_need(b), bw = uint64_t((mm[b] + 31) / 32 + (nn[b] + 31) / 32),
+                     lw = uint64_t(2 * (cap[b] + 2));
+      if (!batch.empty() && (acc_w + w > ws_doubles || acc_b + bw > bits_room || acc_l + lw > list_room ||
+                             batch.size() >= max_batch))
+        return false;
+      batch.push_back(b);
+      acc_w += w;
+      acc_b += bw;
+      acc_l += lw;
+      return true;
+    };
+    if (!retry.empty()) {
+      std::vector<size_t> rest;
+      for (size_t b : retry)
+        if (!take(b)) rest.push_back(b);
+      retry.swap(rest);
+    } else {
+      while (pos < todo.size() && take(todo[pos])) pos++;
+    }
+    desc.resize(batch.size());
+    warp_list.clear();
+    cta_list.clear();
+    uint64_t ow = 0, ob = 0, ol = 0;
+    for (size_t q = 0; q < batch.size(); q++) {
+      const size_t b = batch[q];
+      AcaBlockDesc& d = desc[q];
+      d.t_begin = tb[b];
+      d.s_begin = sb[b];
+      d.m = mm[b];
+      d.n = nn[b];
+      d.cap = cap[b];
+      d.pad = 0;
+      d.ws = int64_t(ow);
+      d.bits = int64_t(ob);
+      d.lists = int64_t(ol);
+      d.seed = block_seed(op->far[b].level, op->far[b].t, op->far[b].s);
+      ow += ws_need(b);
+      ob += uint64_t((mm[b] + 31) / 32 + (nn[b] + 31) / 32);
+      ol += uint64_t(2 * (cap[b] + 2));
+      (std::max(mm[b], nn[b]) <= 256 ? warp_list : cta_list).push_back(int32_t(q));
+    }
+    std::vector<int32_t> lst(cta_list);
+    lst.insert(lst.end(), warp_list.begin(), warp_list.end());
+    s_ws.ensure(std::max<uint64_t>(ow, 1) * 8, st, "ACA workspace");
+    s_bits.ensure(std::max<uint64_t>(ob, 1) * 4, st, "ACA bitmaps");
+    s_lists.ensure(std::max<uint64_t>(ol, 1) * 4, st, "ACA index lists");
+    double* ws = static_cast<double*>(s_ws.p);
+    CK(cudaMemcpyAsync(d_desc, desc.data(), desc.size() * sizeof(AcaBlockDesc), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d_lists_idx, lst.data(), lst.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    AcaArgs a;
+    a.P = P;
+    a.K = K;
+    a.tol = op->p.eps_aca;
+    a.blocks = d_desc;
+    a.ws = ws;
+    a.bits = static_cast<uint32_t*>(s_bits.p);
+    a.lists = static_cast<int32_t*>(s_lists.p);
+    a.out = d_out;
+    CK(launch_aca(op->p.ndim, a, d_lists_idx + cta_list.size(), int(warp_list.size()), d_lists_idx,
+                  int(cta_list.size()), st));
+    out.resize(batch.size());
+    CK(cudaMemcpyAsync(out.data(), d_out, out.size() * sizeof(AcaOut), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // compaction of the finished blocks into one chunk
+    cds.clear();
+    uint64_t bytes = 0;
+    std::vector<uint64_t> off(batch.size());
+    for (size_t q = 0; q < batch.size(); q++) {
+      const size_t b = batch[q];
+      if (out[q].flags & kAcaOverflow) {
+        cap[b] = std::min(std::min(mm[b], nn[b]), cap[b] * 4);
+        retry.push_back(b);
+        continue;
+      }
+      op->rank[b] = out[q].rank;
+      op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
+      off[q] = bytes;
+      const uint64_t e = op->dense[b] ? uint64_t(mm[b]) * nn[b] : uint64_t(mm[b] + nn[b]) * uint64_t(op->rank[b]);
+      bytes += (e * esz + 255) / 256 * 256;
+    }
+    if (bytes > 0) {
+      char* chunk = static_cast<char*>(op->mem.alloc(bytes, "far-field factors"));
+      for (size_t q = 0; q < batch.size(); q++) {
+        const size_t b = batch[q];
+        if (out[q].flags & kAcaOverflow) continue;
+        CompactDesc c;
+        c.t_begin = tb[b];
+        c.s_begin = sb[b];
+        c.ws = desc[q].ws;
+        c.u_dst = chunk + off[q];
+        c.v_dst = chunk + off[q] + uint64_t(mm[b]) * uint64_t(std::max(op->rank[b], 0)) * esz;
+        c.m = mm[b];
+        c.n = nn[b];
+        c.rank = op->rank[b];
+        c.dense = op->dense[b];
+        c.cap = desc[q].cap;
+        c.pad = 0;
+        uptr[b] = c.u_dst;
+        vptr[b] = c.v_dst;
+        if (op->dense[b] || op->rank[b] > 0) cds.push_back(c);
+      }
+      CK(cudaMemcpyAsync(d_cd, cds.data(), cds.size() * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
+      CK(launch_compact(op->p.ndim, P, K, ws, d_cd, int(cds.size()), fp, st));
+      CK(cudaStreamSynchronize(st));
+    }
+  }
+}
+
+void compute_stats(hodlr_op* op) {
+  hodlr_stats& s = op->st;
+  const Tree& t = op->tree;
+  s.n = op->n;
+  s.depth = t.levels - 1;
+  s.n_leaves = t.level_size.back();
+  s.n_far_blocks = int64_t(op->far.size());
+  s.n_near_blocks = int64_t(op->near.src.size());
+  s.n_dense_far_blocks = 0;
+  s.max_rank = 0;
+  s.far_entries = s.dense_far_entries = s.near_entries = 0;
+  double flop = 0.0;
+  const int L = t.levels - 1;
+  for (int64_t k = 0; k < t.level_size[size_t(L)]; k++) {
+    const int64_t g = t.gid(L, k);
+    if (t.count[size_t(g)] == 0) continue;
+    double f = 0.0;
+    for (int64_t q = op->near.leaf_ptr[size_t(k)]; q < op->near.leaf_ptr[size_t(k + 1)]; q++)
+      f += double(t.count[size_t(t.gid(L, op->near.src[size_t(q)]))]);
+    flop += f * double(t.count[size_t(g)]);
+    s.near_entries += f * double(t.count[size_t(g)]);
+  }
+  for (size_t b = 0; b < op->far.size(); b++) {
+    const double m = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].t))]);
+    const double n = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].s))]);
+    flop += double(op->rank[b]) * (m + n);
+    s.max_rank = std::max<int64_t>(s.max_rank, op->rank[b]);
+    if (op->dense[b]) {
+      s.n_dense_far_blocks++;
+      s.dense_far_entries += m * n;
+    } else {
+      s.far_entries += double(op->rank[b]) * (m + n);
+    }
+  }
+  s.n_flop = flop;
+  s.memory_gb = 8e-9 * flop;
+  s.compression_ratio = flop / (double(op->n) * double(op->n));
+  const double fesz = op->p.precision == HODLR_PREC_MIXED ? 4.0 : 8.0;
+  s.near_bytes = uint64_t(s.near_entries * 8.0 * (op->p.precision == HODLR_PREC_MIXED ? 1.5 : 1.0));
+  s.far_bytes = uint64_t((s.far_entries + s.dense_far_entries) * fesz);
+  s.device_bytes = op->mem.used;
+}
+
+// ---------------------------------------------------------------- apply
+
+template <typename T>
+struct PrecOf;
+template <>
+struct PrecOf<double> {
+  static constexpr Prec v = Prec::kD;
+};
+template <>
+struct PrecOf<float> {
+  static constexpr Prec v = Prec::kF;
+};
+
+// y = A x, tree order, nrhs = 1; x may alias nothing in the op's buffers.
+template <typename T>
+cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, T* yslots, cudaStream_t st) {
+  const int64_t n = op->n, ldin = n + op->zlen;
+  cudaError_t e = cudaMemcpyAsync(in, x, sizeof(T) * size_t(n), cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  if (op->nslots > 1) {
+    e = cudaMemsetAsync(yslots + n, 0, sizeof(T) * size_t(n) * size_t(op->nslots - 1), st);
+    if (e != cudaSuccess) return e;
+  }
+  const Prec px = PrecOf<T>::v;
+  if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.nzb, in, ldin, 1, st)) != cudaSuccess) return e;
+  if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.items_near, plan.nitems_near, in, ldin,
+                         yslots, n, op->nslots, 1, st)) != cudaSuccess)
+    return e;
+  if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.items_far, plan.nitems_far, in, ldin,
+                         yslots, n, op->nslots, 1, st)) != cudaSuccess)
+    return e;
+  return launch_combine(px, yslots, n, op->nslots, n, 1, nullptr, y, px, n, st);
+}
+
+__global__ void axpy_f2d_kernel(double* x, const float* d, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    x[i] = x[i] + double(d[i]);
+}
+
+// Solve in tree order on device buffers b, x (one right-hand side).
+void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr_solve_info* info) {
+  const hodlr_params& p = op->p;
+  const double tol = p.tol > 0 ? p.tol : p.eps_aca;
+  const int64_t max_iter = p.max_iter > 0 ? p.max_iter : op->n;
+  const int restart = p.restart > 0 ? p.restart : 100;
+  const double t0 = now_s();
+  if (p.precision != HODLR_PREC_MIXED) {
+    // HODLRdD_matrix::solve: x0 = b, iterSolver(100, N, eps_ACA) (HDD_matrix.hpp:51-62)
+    CK(cudaMemcpyAsync(x, b, sizeof(double) * size_t(op->n), cudaMemcpyDeviceToDevice, st));
+    TreeMatvec<double> A = [op, st](const double* xi, double* yo) {
+      return apply_tree<double>(op, op->plan64, xi, yo, op->d_in64, op->d_y64, st);
+    };
+    GmresResult r;
+    CK(gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter, tol, st, &r));
+    CK(cudaStreamSynchronize(st));
+    info->iterations = r.iterations;
+    info->outer_iterations = 1;
+    info->rel_residual = r.resid;
+    info->converged = r.converged ? 1 : 0;
+  } else {
+    // FP64 iterative refinement around FP32 GMRES on the FP32 operator
+    const int max_outer = p.max_outer > 0 ? p.max_outer : 10;
+    const double inner_tol = p.inner_tol > 0 ? p.inner_tol : 1e-4;
+    TreeMatvec<float> A32 = [op, st](const float* xi, float* yo) {
+      return apply_tree<float>(op, op->plan32, xi, yo, op->d_in32, op->d_y32, st);
+    };
+    const int64_t n = op->n;
+    CK(cudaMemsetAsync(x, 0, sizeof(double) * size_t(n), st));
+    CK(cudaMemcpyAsync(op->d_r64, b, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, st));
+    CK(vec_norm2<double>(b, n, op->d_part, op->d_scal + 2, st));
+    CK(vec_norm2<double>(op->d_r64, n, op->d_part, op->d_scal + 1, st));
+    CK(cudaMemcpyAsync(op->h_scal, op->d_scal, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double normb = op->h_scal[2] == 0.0 ? 1.0 : op->h_scal[2];
+    double rel = op->h_scal[1] / normb;
+    int64_t inner_total = 0;
+    int outer = 0;
+    while (rel > tol && outer < max_outer && inner_total < max_iter) {
+      CK(launch_gather(op->d_r64, Prec::kD, n, nullptr, n, 1, op->d_r32, Prec::kF, n, st));
+      GmresResult r;
+      CK(gmres_solve<float>(op->g32, A32, op->d_r32, op->d_d32, true, restart, max_iter - inner_total,
+                            std::max(inner_tol, tol), st, &r));
+      inner_total += r.iterations;
+      axpy_f2d_kernel<<<kVecCtas, 256, 0, st>>>(x, op->d_d32, n);
+      CK(cudaGetLastError());
+      // true residual with the FP64-vector operator (FP64 near field, FP32-stored far factors)
+      CK(apply_tree<double>(op, op->plan64, x, op->d_io2, op->d_in64, op->d_y64, st));
+      CK(vec_sub_norm2<double>(b, op->d_io2, op->d_r64, n, op->d_part, op->d_scal + 1, st));
+      CK(cudaMemcpyAsync(op->h_scal, op->d_scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+      CK(cudaStreamSynchronize(st));
+      rel = op->h_scal[1] / normb;
+      outer++;
+    }
+    info->iterations = inner_total;
+    info->outer_iterations = outer;
+    info->rel_residual = rel;
+    info->converged = rel <= tol ? 1 : 0;
+  }
+  info->seconds = now_s() - t0;
+}
+
+int guarded(hodlr_ctx* ctx, const std::function<int()>& f) {
+  try {
+    return f();
+  } catch (const Failure& e) {
+    return fail(ctx, e.code, e.msg);
+  } catch (const std::bad_alloc&) {
+    return fail(ctx, HODLR_ERR_OOM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return fail(ctx, HODLR_ERR_INVALID, e.what());
+  }
+}
+
+}  // namespace
+
+// ================================================================= C ABI
+
+extern "C" {
+
+void hodlr_params_default(hodlr_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->ndim = 2;
+  p->nmax = 64;
+  p->dprime = 0;
+  p->restart = 100;
+  p->eps_aca = 1e-10;
+  p->tol = 0.0;
+  p->max_iter = 0;
+  p->precision = HODLR_PREC_FP64;
+  p->device = 0;
+}
+
+const char* hodlr_last_error(const hodlr_ctx* ctx) {
+  if (ctx) return ctx->err.c_str();
+  return g_thread_err.c_str();
+}
+
+int hodlr_ctx_create(const hodlr_params* params, hodlr_ctx** out) {
+  if (!params || !out) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_ctx_create: null argument");
+  *out = nullptr;
+  const hodlr_params& p = *params;
+  if (p.ndim < 1 || p.ndim > kMaxDim) return fail(nullptr, HODLR_ERR_INVALID, "ndim must be in 1..8");
+  if (p.nmax < 1) return fail(nullptr, HODLR_ERR_INVALID, "nmax must be positive");
+  if (p.dprime < -1 || p.dprime > p.ndim - 1) return fail(nullptr, HODLR_ERR_INVALID, "dprime must be in -1..ndim-1");
+  if (!(p.eps_aca > 0.0) || !(p.eps_aca < 1.0))
+    return fail(nullptr, HODLR_ERR_INVALID, "eps_aca must be in (0, 1) (values >= 1 select a fixed rank in the "
+                                            "reference, which this engine does not support)");
+  if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED)
+    return fail(nullptr, HODLR_ERR_INVALID, "unknown precision");
+  if (p.restart < 0 || p.restart > 1000) return fail(nullptr, HODLR_ERR_INVALID, "restart must be in 0..1000");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, HODLR_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  if (p.device < 0 || p.device >= ndev) return fail(nullptr, HODLR_ERR_INVALID, "device ordinal out of range");
+  if ((e = cudaSetDevice(p.device)) != cudaSuccess)
+    return fail(nullptr, HODLR_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  hodlr_ctx* c = new hodlr_ctx();
+  c->p = p;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    delete c;
+    return fail(nullptr, HODLR_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+  }
+  *out = c;
+  return HODLR_OK;
+}
+
+int hodlr_ctx_destroy(hodlr_ctx* ctx) {
+  if (!ctx) return HODLR_OK;
+  cudaSetDevice(ctx->p.device);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return HODLR_OK;
+}
+
+int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* box_lo, const double* box_hi,
+                const hodlr_kernel_desc* kernel, hodlr_op** out) {
+  if (!ctx || !points || !box_lo || !box_hi || !kernel || !out)
+    return fail(ctx, HODLR_ERR_INVALID, "hodlr_build: null argument");
+  *out = nullptr;
+  if (n < 1) return fail(ctx, HODLR_ERR_INVALID, "hodlr_build: need at least one point");
+  if (n > (int64_t(1) << 31) - 1) return fail(ctx, HODLR_ERR_INVALID, "hodlr_build: at most 2^31-1 points");
+  if (kernel->kind < HODLR_KERNEL_INV_R || kernel->kind > HODLR_KERNEL_EXP_NEG_R)
+    return fail(ctx, HODLR_ERR_INVALID, "hodlr_build: unknown kernel kind");
+  std::unique_ptr<hodlr_op> op(new hodlr_op());
+  op->ctx = ctx;
+  op->p = ctx->p;
+  op->kd = *kernel;
+  op->n = n;
+  op->mem.budget = ctx->p.device_budget_bytes;
+  std::memset(&op->st, 0, sizeof(op->st));
+  return guarded(ctx, [&]() -> int {
+    CK(cudaSetDevice(ctx->p.device));
+    cudaStream_t st = ctx->stream;
+    const double t0 = now_s();
+    TreeParams tp;
+    tp.ndim = op->p.ndim;
+    tp.nmax = op->p.nmax;
+    tp.dprime = op->p.dprime;
+    const std::string terr = build_tree(tp, points, n, box_lo, box_hi, op->tree);
+    if (!terr.empty()) return fail(ctx, terr.find("exceeds") != std::string::npos ? HODLR_ERR_TREE : HODLR_ERR_INVALID,
+                                   "hodlr_build: " + terr);
+    op->far = far_blocks(op->tree);
+    op->near = near_blocks(op->tree);
+    op->nslots = op->tree.levels;
+    const double t1 = now_s();
+    op->st.t_tree_s = t1 - t0;
+    // points in tree order, structure of arrays
+    const int d = op->p.ndim;
+    std::vector<double> soa(size_t(n) * size_t(d));
+    for (int64_t i = 0; i < n; i++)
+      for (int k = 0; k < d; k++) soa[size_t(k) * size_t(n) + size_t(i)] = points[size_t(op->tree.perm[size_t(i)]) * d + k];
+    op->d_pts = upload(op->mem, soa, st, "points");
+    op->d_perm = upload(op->mem, op->tree.perm, st, "permutation");
+    // near field
+    const NearTiles nt = near_tiles(op->tree, op->near);
+    PointsDev P{op->d_pts, n};
+    KernelDev K{kernel->kind, kernel->scale, kernel->diag};
+    TileDesc* d_tiles = upload(op->mem, nt.tiles, st, "near tile descriptors");
+    double* near64 = op->mem.alloc_n<double>(size_t(std::max<int64_t>(nt.total, 1)), "near field (FP64)");
+    CK(launch_assemble(d, P, K, d_tiles, int(nt.tiles.size()), near64, Prec::kD, st));
+    float* near32 = nullptr;
+    if (op->p.precision == HODLR_PREC_MIXED) {
+      near32 = op->mem.alloc_n<float>(size_t(std::max<int64_t>(nt.total, 1)), "near field (FP32)");
+      CK(launch_assemble(d, P, K, d_tiles, int(nt.tiles.size()), near32, Prec::kF, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    op->mem.release(d_tiles);
+    const double t2 = now_s();
+    op->st.t_near_s = t2 - t1;
+    // far field
+    std::vector<const void*> uptr, vptr;
+    run_aca(op.get(), st, uptr, vptr);
+    const double t3 = now_s();
+    op->st.t_aca_s = t3 - t2;
+    // plans
+    const Prec fp = op->p.precision == HODLR_PREC_MIXED ? Prec::kF : Prec::kD;
+    build_near_plan(op.get(), nt, near64, Prec::kD, op->plan64, st);
+    build_far_plan(op.get(), uptr, vptr, fp, op->plan64, st);
+    if (op->p.precision == HODLR_PREC_MIXED) {
+      build_near_plan(op.get(), nt, near32, Prec::kF, op->plan32, st);
+      op->plan32.a_far = Prec::kF;
+      op->plan32.panels_far = op->plan64.panels_far;
+      op->plan32.segs_far = op->plan64.segs_far;
+      op->plan32.items_far = op->plan64.items_far;
+      op->plan32.nitems_far = op->plan64.nitems_far;
+      op->plan32.zb = op->plan64.zb;
+      op->plan32.nzb = op->plan64.nzb;
+    }
+    // work vectors
+    const int64_t ldin = n + op->zlen;
+    op->d_in64 = op->mem.alloc_n<double>(size_t(ldin), "matvec input");
+    op->d_y64 = op->mem.alloc_n<double>(size_t(n) * size_t(op->nslots), "matvec slots");
+    op->d_b64 = op->mem.alloc_n<double>(size_t(n), "rhs");
+    op->d_x64 = op->mem.alloc_n<double>(size_t(n), "solution");
+    op->d_r64 = op->mem.alloc_n<double>(size_t(n), "residual");
+    op->d_io = op->mem.alloc_n<double>(size_t(n), "staging");
+    op->d_io2 = op->mem.alloc_n<double>(size_t(n), "staging");
+    op->d_part = op->mem.alloc_n<double>(size_t(kVecCtas), "partials");
+    op->d_scal = op->mem.alloc_n<double>(8, "scalars");
+    CK(cudaMallocHost(&op->h_scal, sizeof(double) * 8));
+    const int restart = op->p.restart > 0 ? op->p.restart : 100;
+    if (op->p.precision == HODLR_PREC_MIXED) {
+      op->d_in32 = op->mem.alloc_n<float>(size_t(ldin), "matvec input (FP32)");
+      op->d_y32 = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots), "matvec slots (FP32)");
+      op->d_r32 = op->mem.alloc_n<float>(size_t(n), "residual (FP32)");
+      op->d_d32 = op->mem.alloc_n<float>(size_t(n), "correction (FP32)");
+      CK(gmres_alloc<float>(op->g32, n, restart));
+    } else {
+      CK(gmres_alloc<double>(op->g64, n, restart));
+    }
+    CK(cudaStreamSynchronize(st));
+    op->st.t_build_s = now_s() - t0;
+    compute_stats(op.get());
+    *out = op.release();
+    return HODLR_OK;
+  });
+}
+
+int hodlr_op_destroy(hodlr_op* op) {
+  if (!op) return HODLR_OK;
+  cudaSetDevice(op->p.device);
+  cudaStreamSynchronize(op->ctx->stream);
+  delete op;
+  return HODLR_OK;
+}
+
+int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nrhs, void* stream) {
+  if (!op || !d_x || !d_y) return fail(op ? op->ctx : nullptr, HODLR_ERR_INVALID, "hodlr_matvec_device: null argument");
+  if (nrhs < 1) return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_matvec_device: nrhs must be positive");
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t n = op->n;
+    for (int64_t c = 0; c < nrhs; c++) {
+      CK(launch_gather(d_x + c * n, Prec::kD, n, op->d_perm, n, 1, op->d_io, Prec::kD, n, st));
+      // the combine step scatters back to the caller's order
+      const int64_t ldin = n + op->zlen;
+      CK(cudaMemcpyAsync(op->d_in64, op->d_io, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, st));
+      if (op->nslots > 1) CK(cudaMemsetAsync(op->d_y64 + n, 0, sizeof(double) * size_t(n) * (op->nslots - 1), st));
+      const Plan& pl = op->plan64;
+      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.nzb, op->d_in64, ldin, 1, st));
+      CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.items_near, pl.nitems_near, op->d_in64,
+                       ldin, op->d_y64, n, op->nslots, 1, st));
+      CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.items_far, pl.nitems_far, op->d_in64, ldin,
+                       op->d_y64, n, op->nslots, 1, st));
+      CK(launch_combine(Prec::kD, op->d_y64, n, op->nslots, n, 1, op->d_perm, d_y + c * n, Prec::kD, n, st));
+    }
+    return HODLR_OK;
+  });
+}
+
+int hodlr_matvec(hodlr_op* op, const double* x, double* y, int64_t nrhs) {
+  if (!op || !x || !y) return fail(op ? op->ctx : nullptr, HODLR_ERR_INVALID, "hodlr_matvec: null argument");
+  if (nrhs < 1) return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_matvec: nrhs must be positive");
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    cudaStream_t st = op->ctx->stream;
+    const int64_t n = op->n;
+    const double t0 = now_s();
+    for (int64_t c = 0; c < nrhs; c++) {
+      CK(cudaMemcpyAsync(op->d_b64, x + c * n, sizeof(double) * size_t(n), cudaMemcpyHostToDevice, st));
+      const int rc = hodlr_matvec_device(op, op->d_b64, op->d_x64, 1, st);
+      if (rc != HODLR_OK) return rc;
+      CK(cudaMemcpyAsync(y + c * n, op->d_x64, sizeof(double) * size_t(n), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    op->st.t_matvec_s = (now_s() - t0) / double(nrhs);
+    return HODLR_OK;
+  });
+}
+
+int hodlr_solve_device(hodlr_op* op, const double* d_b, double* d_x, int64_t nrhs, void* stream,
+                       hodlr_solve_info* info) {
+  if (!op || !d_b || !d_x) return fail(op ? op->ctx : nullptr, HODLR_ERR_INVALID, "hodlr_solve_device: null argument");
+  if (nrhs < 1) return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_solve_device: nrhs must be positive");
+  hodlr_solve_info local;
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof(*info));
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t n = op->n;
+    bool all_conv = true;
+    double worst = 0.0;
+    hodlr_solve_info one;
+    for (int64_t c = 0; c < nrhs; c++) {
+      CK(launch_gather(d_b + c * n, Prec::kD, n, op->d_perm, n, 1, op->d_b64, Prec::kD, n, st));
+      std::memset(&one, 0, sizeof(one));
+      solve_tree(op, op->d_b64, op->d_x64, st, &one);
+      CK(launch_gather(op->d_x64, Prec::kD, n, nullptr, n, 1, op->d_io, Prec::kD, n, st));
+      // scatter: x_caller[perm[i]] = x_tree[i]
+      CK(launch_combine(Prec::kD, op->d_io, n, 1, n, 1, op->d_perm, d_x + c * n, Prec::kD, n, st));
+      info->iterations += one.iterations;
+      info->outer_iterations += one.outer_iterations;
+      info->seconds += one.seconds;
+      worst = std::max(worst, one.rel_residual);
+      all_conv = all_conv && one.converged;
+    }
+    CK(cudaStreamSynchronize(st));
+    info->rel_residual = worst;
+    info->converged = all_conv ? 1 : 0;
+    return all_conv ? HODLR_OK : fail(op->ctx, HODLR_ERR_NOT_CONVERGED, "GMRES did not reach the tolerance");
+  });
+}
+
+int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_solve_info* info) {
+  if (!op || !b || !x) return fail(op ? op->ctx : nullptr, HODLR_ERR_INVALID, "hodlr_solve: null argument");
+  if (nrhs < 1) return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_solve: nrhs must be positive");
+  hodlr_solve_info local;
+  if (!info) info = &local;
+  std::memset(info, 0, sizeof(*info));
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    cudaStream_t st = op->ctx->stream;
+    const int64_t n = op->n;
+    double* db = op->mem.alloc_n<double>(size_t(n * nrhs), "solve rhs");
+    double* dx = op->mem.alloc_n<double>(size_t(n * nrhs), "solve solution");
+    CK(cudaMemcpyAsync(db, b, sizeof(double) * size_t(n * nrhs), cudaMemcpyHostToDevice, st));
+    const int rc = hodlr_solve_device(op, db, dx, nrhs, st, info);
+    cudaMemcpyAsync(x, dx, sizeof(double) * size_t(n * nrhs), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    op->mem.release(db);
+    op->mem.release(dx);
+    return rc;
+  });
+}
+
+int hodlr_stats_get(const hodlr_op* op, hodlr_stats* out) {
+  if (!op || !out) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_stats_get: null argument");
+  *out = op->st;
+  return HODLR_OK;
+}
+
+int hodlr_get_permutation(const hodlr_op* op, int64_t* perm) {
+  if (!op || !perm) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_get_permutation: null argument");
+  std::memcpy(perm, op->tree.perm.data(), sizeof(int64_t) * size_t(op->n));
+  return HODLR_OK;
+}
+
+int hodlr_get_blocks(const hodlr_op* op, int32_t* level, int64_t* target, int64_t* source, int32_t* rank) {
+  if (!op) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_get_blocks: null argument");
+  for (size_t b = 0; b < op->far.size(); b++) {
+    if (level) level[b] = op->far[b].level;
+    if (target) target[b] = op->far[b].t;
+    if (source) source[b] = op->far[b].s;
+    if (rank) rank[b] = op->rank[b];
+  }
+  return HODLR_OK;
+}
+
+// ---------------------------------------------------------------- host-only tree
+
+struct hodlr_tree {
+  Tree t;
+  std::vector<FarBlock> far;
+  NearList near;
+};
+
+int hodlr_tree_build(const hodlr_params* params, const double* points, int64_t n, const double* box_lo,
+                     const double* box_hi, hodlr_tree** out) {
+  if (!params || !points || !box_lo || !box_hi || !out)
+    return fail(nullptr, HODLR_ERR_INVALID, "hodlr_tree_build: null argument");
+  *out = nullptr;
+  try {
+    std::unique_ptr<hodlr_tree> tr(new hodlr_tree());
+    TreeParams tp;
+    tp.ndim = params->ndim;
+    tp.nmax = params->nmax;
+    tp.dprime = params->dprime;
+    const std::string err = build_tree(tp, points, n, box_lo, box_hi, tr->t);
+    if (!err.empty())
+      return fail(nullptr, err.find("exceeds") != std::string::npos ? HODLR_ERR_TREE : HODLR_ERR_INVALID,
+                  "hodlr_tree_build: " + err);
+    tr->far = far_blocks(tr->t);
+    tr->near = near_blocks(tr->t);
+    *out = tr.release();
+    return HODLR_OK;
+  } catch (const std::exception& e) {
+    return fail(nullptr, HODLR_ERR_INVALID, e.what());
+  }
+}
+
+int hodlr_tree_sizes(const hodlr_tree* tr, int64_t* sizes) {
+  if (!tr || !sizes) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_tree_sizes: null argument");
+  sizes[0] = tr->t.levels;
+  sizes[1] = tr->t.level_off.back();
+  sizes[2] = int64_t(tr->t.nbr.size());
+  sizes[3] = int64_t(tr->t.intr.size());
+  sizes[4] = int64_t(tr->far.size());
+  sizes[5] = int64_t(tr->near.src.size());
+  return HODLR_OK;
+}
+
+int hodlr_tree_get(const hodlr_tree* tr, int64_t* level_sizes, int64_t* node_counts, int64_t* nbr_ptr, int64_t* nbr,
+                   int64_t* intr_ptr, int64_t* intr, int64_t* leaf_perm) {
+  if (!tr) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_tree_get: null argument");
+  const Tree& t = tr->t;
+  if (level_sizes) std::copy(t.level_size.begin(), t.level_size.end(), level_sizes);
+  if (node_counts) std::copy(t.count.begin(), t.count.end(), node_counts);
+  if (nbr_ptr) std::copy(t.nbr_ptr.begin(), t.nbr_ptr.end(), nbr_ptr);
+  if (nbr) std::copy(t.nbr.begin(), t.nbr.end(), nbr);
+  if (intr_ptr) std::copy(t.intr_ptr.begin(), t.intr_ptr.end(), intr_ptr);
+  if (intr) std::copy(t.intr.begin(), t.intr.end(), intr);
+  if (leaf_perm) std::copy(t.perm.begin(), t.perm.end(), leaf_perm);
+  return HODLR_OK;
+}
+
+int hodlr_tree_destroy(hodlr_tree* tr) {
+  delete tr;
+  return HODLR_OK;
+}
+
+}  // extern "C"

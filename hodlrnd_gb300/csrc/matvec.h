@@ -1,0 +1,93 @@
+// HODLR matvec launch interface (matvec.cu).
+//
+// The operator is applied in tree order in two phases:
+//   phase 1: z_b = V_b^T x_s for every low-rank far block b (warp per block);
+//   phase 2: for every "panel" -- the rows of one node at one level, or of one
+//            leaf for the near field -- y_slot[rows] = sum over its segments of
+//            M_seg * in[seg], where a segment is a dense leaf block (input x_s),
+//            a far block kept dense (input x_s) or a factor U_b (input z_b).
+// Each level's far panels write their own output slot and the near field
+// writes slot 0, so no two warps update the same output; the slots are then
+// summed in a fixed order (deterministic, no atomics).  This replaces the
+// reference's serial gather / per-node GEMV / scatter-add (HODLRnD
+// include/HDD_tree.hpp:86-107, include/HDD_node.hpp:82-99,223-254,
+// include/LowRank_matrix.hpp:40-63).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device.cuh"
+
+namespace hodlr {
+
+struct Panel {
+  int64_t row_begin;  // tree position of the first row
+  int64_t seg_begin, seg_end;
+  int32_t m;          // rows
+  int32_t slot;       // output slot
+};
+
+struct Seg {
+  const void* A;   // m x K column major (element type of the launch)
+  int64_t in_off;  // offset of the K inputs in the input buffer
+  int32_t K;
+  int32_t pad;
+};
+
+struct Item {
+  int32_t panel;
+  int32_t chunk;  // 32-row chunk of the panel (panels with m <= 32 have one item)
+};
+
+struct ZBlock {
+  const void* V;   // n x r column major
+  int64_t x_off;   // tree position of the source node
+  int64_t z_off;   // offset of z_b in the input buffer
+  int32_t n, r;
+};
+
+// Element types: A = stored matrix, X = vectors, ACC = accumulation.
+enum class Prec { kD, kF };  // double, float
+
+// in:   input buffer [x (ld_in rows of x) | z], nrhs columns with leading dimension ld_in
+// y:    output slots, slot s of column c at y + (c * nslots + s) * ld_y
+cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, int nzb, void* in, int64_t ld_in, int nrhs,
+                         cudaStream_t st);
+cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* items, int nitems,
+                          const void* in, int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs,
+                          cudaStream_t st);
+// out[perm[i] + c*ld_out] (or out[i + c*ld_out] when perm == NULL) =
+//   sum_s y[(c*nslots + s)*ld_y + i], i < n
+cudaError_t launch_combine(Prec x, const void* y, int64_t ld_y, int nslots, int64_t n, int nrhs, const int64_t* perm,
+                           void* out, Prec out_prec, int64_t ld_out, cudaStream_t st);
+// dst[i + c*ld_dst] = src[perm[i] + c*ld_src] (perm == NULL: identity), converting precision
+cudaError_t launch_gather(const void* src, Prec sp, int64_t ld_src, const int64_t* perm, int64_t n, int nrhs, void* dst,
+                          Prec dp, int64_t ld_dst, cudaStream_t st);
+
+// Dense blocks from the kernel: tile t is out + off[t], m x n column major,
+// A(t_begin + i, s_begin + j).
+struct TileDesc {
+  int64_t t_begin, s_begin;
+  int64_t off;  // element offset in the output array
+  int32_t m, n;
+};
+cudaError_t launch_assemble(int ndim, const PointsDev& P, const KernelDev& K, const TileDesc* tiles, int ntiles,
+                            void* out, Prec op, cudaStream_t st);
+
+// Far-block compaction after ACA: for each listed block copy U (m x rank) and
+// V (n x rank) out of its ACA workspace (FP64) into u_dst/v_dst in the stored
+// precision, or, for a block kept dense, evaluate its m x n tile into u_dst.
+struct CompactDesc {
+  int64_t t_begin, s_begin;
+  int64_t ws;         // ACA workspace offset (doubles)
+  void* u_dst;        // U or the dense tile
+  void* v_dst;        // V (unused for dense blocks)
+  int32_t m, n, rank, dense;
+  int32_t cap;        // workspace columns (V starts after m * cap doubles)
+  int32_t pad;
+};
+cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws,
+                           const CompactDesc* blocks, int nblocks, Prec op, cudaStream_t st);
+
+}  // namespace hodlr

@@ -1,0 +1,182 @@
+/*
+ * hodlrnd.h -- C ABI of the GB300 HODLRnD engine (libhodlrnd_gb300.so).
+ *
+ * The reference (HODLRnD) is a header-only C++ template library whose hot
+ * path is: 2^d-tree clustering -> ACA compression of every admissible block
+ * -> HODLR matvec -> restarted GMRES.  It has no binary interface; its users
+ * call the class HODLRdD_matrix<Kernel>.  This header is the drop-in
+ * boundary for that path: plain C types, host or device pointers and sizes,
+ * status codes.  Each entry point names the reference interface it replaces
+ * (paths relative to the HODLRnD project root).
+ *
+ * Conventions
+ *  - Every function returns HODLR_OK (0) or a HODLR_ERR_* code; the message
+ *    of the last failure is returned by hodlr_last_error().
+ *  - Points are passed as n x ndim row-major doubles (the x[] field of the
+ *    reference's ptsnD, include/points_dt.hpp:9-13).  Vectors are in the
+ *    caller's point order; several right-hand sides are n x nrhs column-major.
+ *  - The engine copies what it needs to the device and owns that memory until
+ *    the matching *_destroy call.  Host buffers stay owned by the caller.
+ *  - A context and the operators built from it must be used from one host
+ *    thread at a time (the reference is single-threaded too).
+ */
+#ifndef HODLRND_H
+#define HODLRND_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define HODLR_OK 0
+#define HODLR_ERR_INVALID 1       /* bad argument */
+#define HODLR_ERR_CUDA 2          /* a CUDA runtime call failed */
+#define HODLR_ERR_OOM 3           /* device allocation failed */
+#define HODLR_ERR_BUDGET 4        /* device_budget_bytes would be exceeded */
+#define HODLR_ERR_NOT_CONVERGED 5 /* GMRES stopped at max_iter (result still written) */
+#define HODLR_ERR_TREE 6          /* tree would exceed the node limit (degenerate input) */
+#define HODLR_ERR_STATE 7         /* call out of order (e.g. matvec before build) */
+#define HODLR_ERR_DEVICE 8        /* a device-side check failed (index or size out of range) */
+
+/* ---- kernels --------------------------------------------------------- */
+/* Entry A_ij for i != j with r = |x_i - x_j| (Euclidean, include/points_dt.hpp:31-39);
+ * A_ii = diag.  These cover the reference's test kernels
+ * (include/user_kernel.hpp:46-49,101-104,167-170) and the benchmark kernels. */
+#define HODLR_KERNEL_INV_R 1     /* scale / r          */
+#define HODLR_KERNEL_INV_R2 2    /* scale / r^2        */
+#define HODLR_KERNEL_LOG_R 3     /* scale * log(r)     */
+#define HODLR_KERNEL_EXP_NEG_R 4 /* scale * exp(-r)    */
+
+typedef struct hodlr_kernel_desc {
+  int32_t kind; /* HODLR_KERNEL_* */
+  int32_t reserved;
+  double scale;
+  double diag;
+} hodlr_kernel_desc;
+
+/* ---- precision of the stored far-field factors ------------------------ */
+#define HODLR_PREC_FP64 0  /* everything FP64 (the reference's arithmetic, include/myHeaders.hpp:66-72) */
+#define HODLR_PREC_MIXED 1 /* far-field U, V in FP32; FP64 near field; solve = FP64 iterative
+                              refinement around an FP32 inner GMRES */
+
+/* ---- parameters -------------------------------------------------------- */
+typedef struct hodlr_params {
+  int32_t ndim;      /* NDIM (include/myHeaders.hpp:35), 1..8 */
+  int32_t nmax;      /* Nmax (include/myHeaders.hpp:36): split while a node holds more points */
+  int32_t dprime;    /* INTERACTION_TYPE_ALLOWED = d' (include/myHeaders.hpp:39), -1..ndim-1 */
+  int32_t restart;   /* GMRES restart length; the reference uses 100 (include/HDD_matrix.hpp:54) */
+  double eps_aca;    /* eps_ACA (include/myHeaders.hpp:47) */
+  double tol;        /* GMRES relative-residual tolerance; <= 0 selects eps_aca (HDD_matrix.hpp:54) */
+  int64_t max_iter;  /* GMRES iteration limit; <= 0 selects N (HDD_matrix.hpp:54) */
+  int32_t precision; /* HODLR_PREC_* */
+  int32_t device;    /* CUDA device ordinal */
+  uint64_t device_budget_bytes; /* refuse a build whose device footprint would exceed this; 0 = no limit */
+  int32_t rank_cap;  /* initial ACA workspace columns per block (0 = default); grown on demand */
+  int32_t max_outer; /* MIXED: iterative-refinement sweeps (0 = default 10) */
+  double inner_tol;  /* MIXED: relative-residual target of each FP32 inner GMRES (<= 0: default 1e-4) */
+} hodlr_params;
+
+/* Fill p with the reference's defaults: ndim 2, Nmax 64, d' 0, eps 1e-10,
+ * restart 100, tol = eps, max_iter = N, FP64.  No counterpart in the
+ * reference (its defaults are the constants in include/myHeaders.hpp:35-49). */
+void hodlr_params_default(hodlr_params* p);
+
+typedef struct hodlr_ctx hodlr_ctx;
+typedef struct hodlr_op hodlr_op;
+
+/* Create a context on params->device.  Replaces editing the compile-time
+ * constants of include/myHeaders.hpp:32-49. */
+int hodlr_ctx_create(const hodlr_params* params, hodlr_ctx** out);
+int hodlr_ctx_destroy(hodlr_ctx* ctx);
+
+/* Message of the last failure on this context (or, with ctx == NULL, of the
+ * last failure on the calling thread).  Never NULL. */
+const char* hodlr_last_error(const hodlr_ctx* ctx);
+
+/* Build the operator: tree and interaction lists (HODLRdD_matrix ctor,
+ * include/HDD_matrix.hpp:20-33 -> Tree::Tree, include/HDD_tree.hpp:23-74)
+ * followed by Assemble_matrix_operators (include/HDD_matrix.hpp:39-41 ->
+ * Tree::Initialise_tree / Node::Initialize_node, include/HDD_node.hpp:118-148):
+ * ACA of every admissible block and the dense leaf blocks.
+ * points: host, n x ndim row-major; box_lo/box_hi: host, ndim each (the
+ * bounding box the reference takes as x1, x2). */
+int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* box_lo, const double* box_hi,
+                const hodlr_kernel_desc* kernel, hodlr_op** out);
+int hodlr_op_destroy(hodlr_op* op);
+
+/* y = A x (HODLRdD_matrix::operator*, include/HDD_matrix.hpp:43-47).  Host
+ * pointers, n x nrhs column-major, caller's point order. */
+int hodlr_matvec(hodlr_op* op, const double* x, double* y, int64_t nrhs);
+
+/* Same with device pointers on the given cudaStream_t (NULL = the legacy
+ * default stream).  Asynchronous: returns once the work is queued. */
+int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nrhs, void* stream);
+
+typedef struct hodlr_solve_info {
+  int64_t iterations;       /* total inner GMRES iterations (the reference's return value, GMRES.hpp:267,294,302) */
+  int64_t outer_iterations; /* iterative-refinement sweeps (1 for FP64) */
+  double rel_residual;      /* |b - A x| / |b| with A the stored operator, FP64 */
+  int32_t converged;
+  int32_t reserved;
+  double seconds;
+} hodlr_solve_info;
+
+/* Solve A x = b (HODLRdD_matrix::solve, include/HDD_matrix.hpp:51-62 ->
+ * iterSolver::GMRES, include/GMRES.hpp:160-305).  FP64: restarted GMRES with
+ * x0 = b, as the reference.  MIXED: FP64 iterative refinement whose inner
+ * solves are FP32 GMRES on the FP32-factor operator.  Host pointers. */
+int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_solve_info* info);
+
+/* Same with device pointers; synchronous with respect to the given stream. */
+int hodlr_solve_device(hodlr_op* op, const double* d_b, double* d_x, int64_t nrhs, void* stream,
+                       hodlr_solve_info* info);
+
+typedef struct hodlr_stats {
+  int64_t n, depth, n_leaves, n_far_blocks, n_dense_far_blocks, n_near_blocks, max_rank;
+  double n_flop;            /* Node::compute_flop_count summed (include/HDD_node.hpp:182-202) */
+  double memory_gb;         /* 8e-9 * n_flop, as print_matrix_statistics (include/HDD_matrix.hpp:69-85) */
+  double compression_ratio; /* n_flop / N^2 */
+  uint64_t near_bytes;      /* stored dense leaf blocks */
+  uint64_t far_bytes;       /* stored far-field factors and dense far blocks */
+  uint64_t device_bytes;    /* everything the operator holds on the device */
+  double t_tree_s, t_aca_s, t_near_s, t_build_s, t_matvec_s;
+  double far_entries;       /* sum over low-rank blocks of r (m + n) */
+  double dense_far_entries; /* sum over dense far blocks of m n */
+  double near_entries;      /* sum over near blocks of m n */
+} hodlr_stats;
+
+/* print_matrix_statistics figures (include/HDD_matrix.hpp:69-85) plus byte counts. */
+int hodlr_stats_get(const hodlr_op* op, hodlr_stats* out);
+
+/* Leaf-order permutation: perm[k] = caller index of the k-th point in tree
+ * order (the concatenated index_of_points of the leaves, HDD_clusters.hpp:26). */
+int hodlr_get_permutation(const hodlr_op* op, int64_t* perm);
+
+/* Far blocks in the reference's assembly order (level, target node, partner
+ * in interaction-list order; include/HDD_tree.hpp:76-83, HDD_node.hpp:126-130).
+ * Arrays of length n_far_blocks; rank is the reference's rank() (min(m,n)
+ * for a block kept dense, LowRank_matrix.hpp:348-363). */
+int hodlr_get_blocks(const hodlr_op* op, int32_t* level, int64_t* target, int64_t* source, int32_t* rank);
+
+/* ---- host-only tree planning (no device needed) ------------------------ */
+typedef struct hodlr_tree hodlr_tree;
+
+/* Tree and lists only (include/HDD_tree.hpp:23-74, include/HDD_node.hpp:150-180). */
+int hodlr_tree_build(const hodlr_params* params, const double* points, int64_t n, const double* box_lo,
+                     const double* box_hi, hodlr_tree** out);
+/* sizes[0..5] = levels, nodes (all levels), neighbour entries, interaction entries,
+ * far blocks (both nodes non-empty), near blocks (self + non-empty neighbours of non-empty leaves) */
+int hodlr_tree_sizes(const hodlr_tree* tree, int64_t* sizes);
+/* Node arrays run over all levels, level by level, nodes in reference order
+ * (child c of node k is node k*2^ndim + c of the next level). */
+int hodlr_tree_get(const hodlr_tree* tree, int64_t* level_sizes, int64_t* node_counts, int64_t* nbr_ptr,
+                   int64_t* nbr, int64_t* intr_ptr, int64_t* intr, int64_t* leaf_perm);
+int hodlr_tree_destroy(hodlr_tree* tree);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HODLRND_H */

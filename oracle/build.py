@@ -11,6 +11,7 @@
   absent (it only exists where the fixtures are generated) this returns None.
 """
 import os
+import platform
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -22,11 +23,16 @@ OUT_REF = os.path.join(HERE, "_ref")
 def build_oracle(force=False):
     src = os.path.join(HERE, "hodlr_oracle.cpp")
     out = os.path.join(HERE, "liboracle.so")
+    stamp = os.path.join(HERE, "liboracle.machine")
+    if not os.path.exists(stamp) or open(stamp).read() != platform.machine():
+        force = True
     if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
         return out
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
            "-Wall", src, "-o", out]
     subprocess.run(cmd, check=True)
+    with open(stamp, "w") as f:
+        f.write(platform.machine())
     return out
 
 

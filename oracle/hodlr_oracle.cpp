@@ -168,6 +168,7 @@ void build_tree(Oracle& o, const double* lo, const double* hi) {
   int64_t maxc = o.n;
   while (maxc > o.p.nmax) {
     const std::vector<TNode>& par = o.lv.back();
+    if (par.size() * size_t(fan) > (size_t(1) << 22)) throw std::runtime_error("tree too wide");
     std::vector<TNode> ch(par.size() * size_t(fan));
     for (size_t pk = 0; pk < par.size(); pk++) {
       const TNode& P = par[pk];
@@ -695,7 +696,12 @@ void* orc_build(const orc_params* prm, const double* pts, int64_t n, const doubl
   o->pts.assign(pts, pts + size_t(n) * size_t(prm->ndim));
   if (o->p.rng_mode == 0) std::srand(1);
   double t0 = now_s();
-  build_tree(*o, lo, hi);
+  try {
+    build_tree(*o, lo, hi);
+  } catch (const std::exception&) {
+    delete o;
+    return nullptr;
+  }
   o->t_tree = now_s() - t0;
   if (with_operators) {
     t0 = now_s();
