@@ -59,6 +59,16 @@ class HodlrStats(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+TRACE_KINDS = 16
+TRACE_NAMES = {0: "zgemv_fp64", 1: "near_fp64", 2: "far_fp64", 3: "combine_fp64", 4: "zgemv_fp32", 5: "near_fp32",
+               6: "far_fp32", 7: "combine_fp32"}
+
+
+class HodlrTrace(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_uint64 * TRACE_KINDS), ("total_ms", ctypes.c_double * TRACE_KINDS),
+                ("bytes_per_launch", ctypes.c_double * TRACE_KINDS)]
+
+
 class HodlrError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"[hodlr error {code}] {msg}")
@@ -93,6 +103,11 @@ def lib():
     L.hodlr_stats_get.argtypes = [P, ctypes.POINTER(HodlrStats)]
     L.hodlr_get_permutation.argtypes = [P, I64]
     L.hodlr_get_blocks.argtypes = [P, I32, I64, I64, I32]
+    L.hodlr_get_block.argtypes = [P, ctypes.c_int64, I32, I32, I32, I32, D, D]
+    L.hodlr_trace_enable.argtypes = [P, ctypes.c_int]
+    L.hodlr_trace_get.argtypes = [P, ctypes.POINTER(HodlrTrace)]
+    L.hodlr_kernel_launches.argtypes = []
+    L.hodlr_kernel_launches.restype = ctypes.c_uint64
     L.hodlr_tree_build.argtypes = [ctypes.POINTER(HodlrParams), D, ctypes.c_int64, D, D, ctypes.POINTER(P)]
     L.hodlr_tree_sizes.argtypes = [P, I64]
     L.hodlr_tree_get.argtypes = [P, I64, I64, I64, I64, I64, I64, I64]
@@ -100,7 +115,7 @@ def lib():
     for f in ("hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
               "hodlr_matvec_device", "hodlr_solve", "hodlr_solve_device", "hodlr_stats_get",
               "hodlr_get_permutation", "hodlr_get_blocks", "hodlr_tree_build", "hodlr_tree_sizes",
-              "hodlr_tree_get", "hodlr_tree_destroy"):
+              "hodlr_tree_get", "hodlr_tree_destroy", "hodlr_get_block", "hodlr_trace_enable", "hodlr_trace_get"):
         getattr(L, f).restype = ctypes.c_int
     _lib = L
     return L

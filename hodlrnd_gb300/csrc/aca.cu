@@ -27,6 +27,11 @@
 // match the oracle bit for bit; only the norm reductions are summed in a
 // different order.
 //
+// Rows and columns are indexed in the reference's order of the node's points
+// (by caller index; a non-leaf node's tree-order range is grouped by leaf
+// instead), so the pivots, the restarts and hence the factors follow the
+// reference; the compaction step scatters the factors into tree order.
+//
 // Workspace per block: U (m x cap) and V (n x cap) FP64 column major, a
 // bitmap of remaining rows and one of remaining columns, the lists of used
 // row and column indices.  A block whose rank would exceed cap reports
@@ -157,11 +162,12 @@ struct AcaTeam {
   // Residual row i0 into V[:, r]; argmax over the remaining columns.
   __device__ void gen_row(int i0, int r, int nc, double& mx, int& piv, double& sq) {
     double xi[D];
-    load_point<D>(a.P, B.t_begin + i0, xi);
+    const int64_t pi = a.lmap[B.t_map + i0];
+    load_point<D>(a.P, pi, xi);
     double ba = -1.0, bv = 0.0, v0 = 0.0, s = 0.0;
     int bi = 0x7fffffff;
     for (int j = tm.tid(); j < n; j += Team::kSize) {
-      double val = kernel_entry<D>(a.P, a.K, B.t_begin + i0, B.s_begin + j, xi);
+      double val = kernel_entry<D>(a.P, a.K, pi, a.lmap[B.s_map + j], xi);
       for (int k = 0; k < r; k++) val = __dsub_rn(val, __dmul_rn(U[i0 + int64_t(k) * m], V[j + int64_t(k) * n]));
       V[j + int64_t(r) * n] = val;
       s += val * val;
@@ -191,13 +197,14 @@ struct AcaTeam {
   __device__ void gen_col(int j0, int r, int nr, double& mx, int& piv, double& sq) {
     double ba = -1.0, bv = 0.0, v0 = 0.0, s = 0.0;
     int bi = 0x7fffffff;
+    const int64_t pj = a.lmap[B.s_map + j0];
     for (int i = tm.tid(); i < m; i += Team::kSize) {
-      // A(i, j0): the kernel is evaluated with the target point first, as
-      // getCol does (getMatrixEntry(sources[j], k), kernel_function.hpp:32-40);
-      // r is symmetric in the two points, so the entry is the same.
+      // A(i, j0) with the target point first, as getCol evaluates it
+      // (getMatrixEntry(sources[j], k), kernel_function.hpp:32-40).
       double xi[D];
-      load_point<D>(a.P, B.t_begin + i, xi);
-      double val = kernel_entry<D>(a.P, a.K, B.t_begin + i, B.s_begin + j0, xi);
+      const int64_t pi = a.lmap[B.t_map + i];
+      load_point<D>(a.P, pi, xi);
+      double val = kernel_entry<D>(a.P, a.K, pi, pj, xi);
       for (int k = 0; k < r; k++) val = __dsub_rn(val, __dmul_rn(V[j0 + int64_t(k) * n], U[i + int64_t(k) * m]));
       U[i + int64_t(r) * m] = val;
       s += val * val;
@@ -361,6 +368,7 @@ void launch_d(const AcaArgs& a, const int32_t* warp_list, int nwarp, const int32
 
 cudaError_t launch_aca(int ndim, const AcaArgs& a, const int32_t* warp_list, int nwarp, const int32_t* cta_list,
                        int ncta, cudaStream_t st) {
+  count_launches(uint64_t(nwarp > 0) + uint64_t(ncta > 0));
   switch (ndim) {
     case 1: launch_d<1>(a, warp_list, nwarp, cta_list, ncta, st); break;
     case 2: launch_d<2>(a, warp_list, nwarp, cta_list, ncta, st); break;

@@ -12,7 +12,7 @@ enum : int32_t { kAcaDense = 1, kAcaOverflow = 2 };
 
 // One admissible block in an ACA launch.
 struct AcaBlockDesc {
-  int64_t t_begin, s_begin;  // tree positions of the target (rows) and source (columns) nodes
+  int64_t t_map, s_map;      // offsets into AcaArgs::lmap of the target (rows) and source (columns) node
   int32_t m, n;              // rows, columns
   int32_t cap;               // workspace columns
   int32_t pad;
@@ -28,6 +28,10 @@ struct AcaOut {
 };
 
 struct AcaArgs {
+  // lmap[l * n + begin + k] = tree position of the k-th point of the level-l
+  // node starting at tree position `begin`, in the reference's order (points
+  // of a node by increasing caller index, HDD_clusters.hpp:124-127).
+  const int32_t* lmap;
   PointsDev P;
   KernelDev K;
   double tol;

@@ -4,7 +4,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace hodlr {
+
+// Process-wide count of this engine's kernel launches (hodlr_kernel_launches).
+inline std::atomic<uint64_t> g_kernel_launches{0};
+inline void count_launches(uint64_t k) { g_kernel_launches.fetch_add(k, std::memory_order_relaxed); }
 
 // Kernel kinds (include/hodlrnd.h).
 enum : int { kInvR = 1, kInvR2 = 2, kLogR = 3, kExpNegR = 4 };

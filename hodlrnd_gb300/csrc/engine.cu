@@ -94,6 +94,54 @@ uint64_t block_seed(int64_t level, int64_t t, int64_t s) {
   return h;
 }
 
+// CUDA events around operator launches (hodlr_trace_*).
+struct Tracer {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  std::vector<std::pair<int, size_t>> pending;  // kind, index of the start event (stop = +1)
+  size_t used = 0;
+  uint64_t launches[HODLR_TRACE_KINDS] = {};
+  double ms[HODLR_TRACE_KINDS] = {};
+  double bytes[HODLR_TRACE_KINDS] = {};
+  void start(int kind, cudaStream_t st) {
+    if (!on) return;
+    while (pool.size() < used + 2) {
+      cudaEvent_t e;
+      check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+      pool.push_back(e);
+    }
+    check_cuda(cudaEventRecord(pool[used], st), "cudaEventRecord");
+    pending.push_back({kind, used});
+    used += 2;
+  }
+  void stop(cudaStream_t st) {
+    if (!on || pending.empty()) return;
+    check_cuda(cudaEventRecord(pool[pending.back().second + 1], st), "cudaEventRecord");
+  }
+  void harvest() {
+    for (auto& p : pending) {
+      check_cuda(cudaEventSynchronize(pool[p.second + 1]), "cudaEventSynchronize");
+      float t = 0.f;
+      check_cuda(cudaEventElapsedTime(&t, pool[p.second], pool[p.second + 1]), "cudaEventElapsedTime");
+      launches[p.first]++;
+      ms[p.first] += double(t);
+    }
+    pending.clear();
+    used = 0;
+  }
+  void reset() {
+    pending.clear();
+    used = 0;
+    for (int k = 0; k < HODLR_TRACE_KINDS; k++) {
+      launches[k] = 0;
+      ms[k] = 0.0;
+    }
+  }
+  ~Tracer() {
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+  }
+};
+
 // Device side of one way of applying the operator (a plan).
 struct Plan {
   Prec a_near = Prec::kD, a_far = Prec::kD;
@@ -125,11 +173,13 @@ struct hodlr_op {
   std::vector<FarBlock> far;
   NearList near;
   std::vector<int32_t> rank, dense;
+  std::vector<const void*> uptr, vptr;  // stored factors (or dense tile) of each far block
   int64_t n = 0, zlen = 0;
   int nslots = 0;
   DevMem mem;
   double* d_pts = nullptr;  // ndim x n, tree order
   int64_t* d_perm = nullptr;
+  int32_t* d_lmap = nullptr;  // levels x n: reference order of each node's points (tree positions)
   Plan plan64;        // FP64 operator, or the FP64-vector operator of MIXED (FP32 far factors)
   Plan plan32;        // MIXED inner operator (all FP32)
   // work vectors
@@ -150,6 +200,7 @@ struct hodlr_op {
   GmresWork<double> g64;
   GmresWork<float> g32;
   hodlr_stats st;
+  Tracer tr;
   ~hodlr_op() {
     gmres_free(g64);
     gmres_free(g32);
@@ -167,6 +218,34 @@ int fail(hodlr_ctx* ctx, int code, const std::string& msg) {
 }
 
 // ---------------------------------------------------------------- build steps
+
+// For every level, the tree positions of each node's points listed in the
+// reference's order (increasing caller index; cluster::binary_clustering keeps
+// the parent's order, HDD_clusters.hpp:124-127).  Within a leaf that is the
+// tree order itself; a non-leaf node's tree range is grouped by leaf instead.
+std::vector<int32_t> reference_order_map(const Tree& t) {
+  const int64_t n = t.n;
+  const int L = t.levels - 1, d = t.p.ndim;
+  std::vector<int32_t> map(size_t(n) * size_t(t.levels));
+  std::vector<int64_t> inv(static_cast<size_t>(n)), leaf_of(static_cast<size_t>(n));
+  for (int64_t q = 0; q < n; q++) inv[size_t(t.perm[size_t(q)])] = q;
+  for (int64_t k = 0; k < t.level_size[size_t(L)]; k++) {
+    const int64_t g = t.gid(L, k);
+    for (int64_t q = t.begin[size_t(g)]; q < t.begin[size_t(g)] + t.count[size_t(g)]; q++) leaf_of[size_t(q)] = k;
+  }
+  for (int l = 0; l <= L; l++) {
+    std::vector<int64_t> cur(static_cast<size_t>(t.level_size[size_t(l)]));
+    for (int64_t k = 0; k < t.level_size[size_t(l)]; k++) cur[size_t(k)] = t.begin[size_t(t.gid(l, k))];
+    int32_t* out = map.data() + size_t(l) * size_t(n);
+    const int shift = d * (L - l);
+    for (int64_t i = 0; i < n; i++) {  // caller order
+      const int64_t q = inv[size_t(i)];
+      const int64_t node = leaf_of[size_t(q)] >> shift;
+      out[cur[size_t(node)]++] = int32_t(q);
+    }
+  }
+  return map;
+}
 
 struct NearTiles {
   std::vector<TileDesc> tiles;
@@ -397,8 +476,8 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
     for (size_t q = 0; q < batch.size(); q++) {
       const size_t b = batch[q];
       AcaBlockDesc& d = desc[q];
-      d.t_begin = tb[b];
-      d.s_begin = sb[b];
+      d.t_map = int64_t(op->far[b].level) * op->n + tb[b];
+      d.s_map = int64_t(op->far[b].level) * op->n + sb[b];
       d.m = mm[b];
       d.n = nn[b];
       d.cap = cap[b];
@@ -421,6 +500,7 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
     CK(cudaMemcpyAsync(d_desc, desc.data(), desc.size() * sizeof(AcaBlockDesc), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(d_lists_idx, lst.data(), lst.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     AcaArgs a;
+    a.lmap = op->d_lmap;
     a.P = P;
     a.K = K;
     a.tol = op->p.eps_aca;
@@ -459,6 +539,8 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
         CompactDesc c;
         c.t_begin = tb[b];
         c.s_begin = sb[b];
+        c.t_map = desc[q].t_map;
+        c.s_map = desc[q].s_map;
         c.ws = desc[q].ws;
         c.u_dst = chunk + off[q];
         c.v_dst = chunk + off[q] + uint64_t(mm[b]) * uint64_t(std::max(op->rank[b], 0)) * esz;
@@ -473,7 +555,7 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
         if (op->dense[b] || op->rank[b] > 0) cds.push_back(c);
       }
       CK(cudaMemcpyAsync(d_cd, cds.data(), cds.size() * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
-      CK(launch_compact(op->p.ndim, P, K, ws, d_cd, int(cds.size()), fp, st));
+      CK(launch_compact(op->p.ndim, P, K, ws, op->d_lmap, d_cd, int(cds.size()), fp, st));
       CK(cudaStreamSynchronize(st));
     }
   }
@@ -520,6 +602,26 @@ void compute_stats(hodlr_op* op) {
   s.near_bytes = uint64_t(s.near_entries * 8.0 * (op->p.precision == HODLR_PREC_MIXED ? 1.5 : 1.0));
   s.far_bytes = uint64_t((s.far_entries + s.dense_far_entries) * fesz);
   s.device_bytes = op->mem.used;
+  // Algorithmic bytes per launch of each operator kernel: stored matrix
+  // entries once, plus each vector once (re-reads of x are not counted).
+  double lr_rows = 0.0, lr_cols = 0.0, zsum = 0.0;
+  for (size_t b = 0; b < op->far.size(); b++) {
+    if (op->dense[b] || op->rank[b] == 0) continue;
+    const double m = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].t))]);
+    const double n = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].s))]);
+    lr_rows += double(op->rank[b]) * m;
+    lr_cols += double(op->rank[b]) * n;
+    zsum += double(op->rank[b]);
+  }
+  const double N = double(op->n), slots = double(op->nslots);
+  for (int v = 0; v < 2; v++) {  // v = 0: FP64 vectors, 1: FP32 vectors
+    const double sx = v == 0 ? 8.0 : 4.0, snear = v == 0 ? 8.0 : 4.0;
+    const int kb = v == 0 ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
+    op->tr.bytes[kb + 0] = lr_cols * fesz + zsum * sx + N * sx;
+    op->tr.bytes[kb + 1] = s.near_entries * snear + 2.0 * N * sx;
+    op->tr.bytes[kb + 2] = (lr_rows + s.dense_far_entries) * fesz + zsum * sx + N * sx + N * (slots - 1.0) * sx;
+    op->tr.bytes[kb + 3] = N * slots * sx + N * sx;
+  }
 }
 
 // ---------------------------------------------------------------- apply
@@ -546,14 +648,26 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
     if (e != cudaSuccess) return e;
   }
   const Prec px = PrecOf<T>::v;
+  const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
+  Tracer& tr = op->tr;
+  if (plan.nzb > 0) tr.start(kb + 0, st);
   if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.nzb, in, ldin, 1, st)) != cudaSuccess) return e;
+  if (plan.nzb > 0) tr.stop(st);
+  tr.start(kb + 1, st);
   if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.items_near, plan.nitems_near, in, ldin,
                          yslots, n, op->nslots, 1, st)) != cudaSuccess)
     return e;
+  tr.stop(st);
+  if (plan.nitems_far > 0) tr.start(kb + 2, st);
   if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.items_far, plan.nitems_far, in, ldin,
                          yslots, n, op->nslots, 1, st)) != cudaSuccess)
     return e;
-  return launch_combine(px, yslots, n, op->nslots, n, 1, nullptr, y, px, n, st);
+  if (plan.nitems_far > 0) tr.stop(st);
+  tr.start(kb + 3, st);
+  e = launch_combine(px, yslots, n, op->nslots, n, 1, nullptr, y, px, n, st);
+  tr.stop(st);
+  if (tr.used > 8192) tr.harvest();
+  return e;
 }
 
 __global__ void axpy_f2d_kernel(double* x, const float* d, int64_t n) {
@@ -737,6 +851,7 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
       for (int k = 0; k < d; k++) soa[size_t(k) * size_t(n) + size_t(i)] = points[size_t(op->tree.perm[size_t(i)]) * d + k];
     op->d_pts = upload(op->mem, soa, st, "points");
     op->d_perm = upload(op->mem, op->tree.perm, st, "permutation");
+    op->d_lmap = upload(op->mem, reference_order_map(op->tree), st, "reference-order map");
     // near field
     const NearTiles nt = near_tiles(op->tree, op->near);
     PointsDev P{op->d_pts, n};
@@ -754,7 +869,8 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
     const double t2 = now_s();
     op->st.t_near_s = t2 - t1;
     // far field
-    std::vector<const void*> uptr, vptr;
+    std::vector<const void*>& uptr = op->uptr;
+    std::vector<const void*>& vptr = op->vptr;
     run_aca(op.get(), st, uptr, vptr);
     const double t3 = now_s();
     op->st.t_aca_s = t3 - t2;
@@ -933,6 +1049,67 @@ int hodlr_get_blocks(const hodlr_op* op, int32_t* level, int64_t* target, int64_
   }
   return HODLR_OK;
 }
+
+int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32_t* rank, int32_t* dense, double* U,
+                    double* V) {
+  if (!op) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_get_block: null argument");
+  if (b < 0 || b >= int64_t(op->far.size())) return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_get_block: no such block");
+  return guarded(op->ctx, [&]() -> int {
+    const Tree& t = op->tree;
+    const int32_t mm = int32_t(t.count[size_t(t.gid(op->far[b].level, op->far[b].t))]);
+    const int32_t nn = int32_t(t.count[size_t(t.gid(op->far[b].level, op->far[b].s))]);
+    if (m) *m = mm;
+    if (n) *n = nn;
+    if (rank) *rank = op->rank[size_t(b)];
+    if (dense) *dense = op->dense[size_t(b)];
+    const bool f32 = op->p.precision == HODLR_PREC_MIXED;
+    auto fetch = [&](const void* src, size_t count, double* dst) {
+      if (!dst || !src || count == 0) return;
+      if (f32) {
+        std::vector<float> tmp(count);
+        CK(cudaMemcpy(tmp.data(), src, count * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < count; i++) dst[i] = double(tmp[i]);
+      } else {
+        CK(cudaMemcpy(dst, src, count * 8, cudaMemcpyDeviceToHost));
+      }
+    };
+    CK(cudaSetDevice(op->p.device));
+    CK(cudaStreamSynchronize(op->ctx->stream));
+    if (op->dense[size_t(b)]) {
+      fetch(op->uptr[size_t(b)], size_t(mm) * size_t(nn), U);
+    } else {
+      const size_t r = size_t(std::max(op->rank[size_t(b)], 0));
+      fetch(op->uptr[size_t(b)], size_t(mm) * r, U);
+      fetch(op->vptr[size_t(b)], size_t(nn) * r, V);
+    }
+    return HODLR_OK;
+  });
+}
+
+int hodlr_trace_enable(hodlr_op* op, int on) {
+  if (!op) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_trace_enable: null argument");
+  return guarded(op->ctx, [&]() -> int {
+    if (on) op->tr.reset();
+    op->tr.on = on != 0;
+    return HODLR_OK;
+  });
+}
+
+int hodlr_trace_get(hodlr_op* op, hodlr_trace* out) {
+  if (!op || !out) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_trace_get: null argument");
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    op->tr.harvest();
+    for (int k = 0; k < HODLR_TRACE_KINDS; k++) {
+      out->launches[k] = op->tr.launches[k];
+      out->total_ms[k] = op->tr.ms[k];
+      out->bytes_per_launch[k] = op->tr.bytes[k];
+    }
+    return HODLR_OK;
+  });
+}
+
+uint64_t hodlr_kernel_launches(void) { return g_kernel_launches.load(); }
 
 // ---------------------------------------------------------------- host-only tree
 

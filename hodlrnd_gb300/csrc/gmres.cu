@@ -1,4 +1,5 @@
 // Restarted GMRES on the device (see gmres.h).
+#include "device.cuh"
 #include "gmres.h"
 
 #include <cmath>
@@ -213,14 +214,18 @@ void gmres_free(GmresWork<T>& W) {
 
 template <typename T>
 cudaError_t vec_sub_norm2(const T* a, const T* b, T* c, int64_t n, double* part, double* dst, cudaStream_t st) {
+  count_launches(1);
   sub_norm_kernel<T><<<kVecCtas, kThreads, 0, st>>>(a, b, c, n, part);
+  count_launches(1);
   finish_norm_kernel<<<1, kThreads, 0, st>>>(part, dst);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t vec_norm2(const T* a, int64_t n, double* part, double* dst, cudaStream_t st) {
+  count_launches(1);
   dot_partial_kernel<T><<<kVecCtas, kThreads, 0, st>>>(a, a, n, part);
+  count_launches(1);
   finish_norm_kernel<<<1, kThreads, 0, st>>>(part, dst);
   return cudaGetLastError();
 }
@@ -240,6 +245,7 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
   // normb = |b|; r = b - A x; beta = |r| (GMRES.hpp:186-197)
   HODLR_TRY(vec_norm2<T>(b, n, part0, W.scal + 2, st));
   if (x0_zero) {
+    count_launches(1);
     fill_zero_kernel<T><<<kVecCtas, kThreads, 0, st>>>(x, n);
     HODLR_TRY(vec_sub_norm2<T>(b, x, W.r, n, part0, W.scal + 1, st));
   } else {
@@ -261,27 +267,34 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
   }
   int64_t j = 1;
   while (j <= max_iter) {
+    count_launches(1);
     start_cycle_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.r, W.V, n, W.scal, W.rot + 2 * (W.restart + 1), W.restart);
     for (int i = 0; i < m && j <= max_iter; i++, j++) {
       T* vi = W.V + int64_t(i) * n;
       HODLR_TRY(A(vi, W.w));
+      count_launches(1);
       dot_partial_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, part0);
       for (int k = 0; k <= i; k++) {
         const T* next = k < i ? W.V + int64_t(k + 1) * n : nullptr;
         double* pin = (k & 1) ? part1 : part0;
         double* pout = (k & 1) ? part0 : part1;
+        count_launches(1);
         mgs_step_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V + int64_t(k) * n, next, n, pin, pout,
                                                            W.H + k + int64_t(i) * ldh);
       }
       double* plast = (i & 1) ? part0 : part1;
+      count_launches(1);
       normalize_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V + int64_t(i + 1) * n, n, plast,
                                                           W.H + (i + 1) + int64_t(i) * ldh);
+      count_launches(1);
       givens_kernel<<<1, 1, 0, st>>>(W.H, ldh, W.rot, W.restart, i, W.scal);
       HODLR_TRY(cudaGetLastError());
       HODLR_TRY(host_scal(1));
       resid = W.hscal[0];
       if (resid < tol) {
+        count_launches(1);
         backsolve_kernel<<<1, 1, 0, st>>>(W.H, ldh, W.rot, W.restart, i);
+        count_launches(1);
         update_x_kernel<T><<<kVecCtas, kThreads, 0, st>>>(x, W.V, n, W.rot, W.restart, i, n);
         HODLR_TRY(cudaGetLastError());
         res->iterations = j;
@@ -290,7 +303,9 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
         return cudaStreamSynchronize(st);
       }
     }
+    count_launches(1);
     backsolve_kernel<<<1, 1, 0, st>>>(W.H, ldh, W.rot, W.restart, m - 1);
+    count_launches(1);
     update_x_kernel<T><<<kVecCtas, kThreads, 0, st>>>(x, W.V, n, W.rot, W.restart, m - 1, n);
     HODLR_TRY(A(x, W.tmp));
     HODLR_TRY(vec_sub_norm2<T>(b, W.tmp, W.r, n, part0, W.scal + 1, st));

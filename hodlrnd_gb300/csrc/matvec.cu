@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(256) assemble_kernel(PointsDev P, KernelDev K,
 
 template <int D, typename TO>
 __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, const double* __restrict__ ws,
+                                                      const int32_t* __restrict__ lmap,
                                                       const CompactDesc* __restrict__ blocks, int nblocks) {
   const CompactDesc B = blocks[blockIdx.x];
   TO* u = static_cast<TO*>(B.u_dst);
@@ -166,12 +167,18 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
   } else {
     const double* U = ws + B.ws;
     const int64_t nu = int64_t(B.m) * B.rank;
-    for (int64_t e = threadIdx.x; e < nu; e += blockDim.x) u[e] = TO(U[e]);
+    for (int64_t e = threadIdx.x; e < nu; e += blockDim.x) {
+      const int i = int(e % B.m), k = int(e / B.m);
+      u[(lmap[B.t_map + i] - B.t_begin) + int64_t(k) * B.m] = TO(U[e]);
+    }
     // V follows U's full workspace (m x cap); its first rank columns are contiguous
     const double* Vw = ws + B.ws + int64_t(B.m) * B.cap;
     TO* v = static_cast<TO*>(B.v_dst);
     const int64_t nv = int64_t(B.n) * B.rank;
-    for (int64_t e = threadIdx.x; e < nv; e += blockDim.x) v[e] = TO(Vw[e]);
+    for (int64_t e = threadIdx.x; e < nv; e += blockDim.x) {
+      const int j = int(e % B.n), k = int(e / B.n);
+      v[(lmap[B.s_map + j] - B.s_begin) + int64_t(k) * B.n] = TO(Vw[e]);
+    }
   }
 }
 
@@ -189,6 +196,7 @@ unsigned vec_grid(int64_t n) {
 cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, int nzb, void* in, int64_t ld_in, int nrhs,
                          cudaStream_t st) {
   if (nzb <= 0) return cudaSuccess;
+  count_launches(1);
   dim3 g(warps_grid(nzb), unsigned(nrhs));
   if (a == Prec::kD && x == Prec::kD)
     zgemv_kernel<double, double, double><<<g, 256, 0, st>>>(zb, nzb, static_cast<double*>(in), ld_in);
@@ -205,6 +213,7 @@ cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, 
                           const void* in, int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs,
                           cudaStream_t st) {
   if (nitems <= 0) return cudaSuccess;
+  count_launches(1);
   dim3 g(warps_grid(nitems), unsigned(nrhs));
   if (a == Prec::kD && x == Prec::kD)
     panel_kernel<double, double, double><<<g, 256, 0, st>>>(panels, segs, items, nitems,
@@ -225,6 +234,7 @@ cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, 
 
 cudaError_t launch_combine(Prec x, const void* y, int64_t ld_y, int nslots, int64_t n, int nrhs, const int64_t* perm,
                            void* out, Prec out_prec, int64_t ld_out, cudaStream_t st) {
+  count_launches(1);
   dim3 g(vec_grid(n), unsigned(nrhs));
   if (x == Prec::kD && out_prec == Prec::kD)
     combine_kernel<double, double><<<g, 256, 0, st>>>(static_cast<const double*>(y), ld_y, nslots, n, perm,
@@ -242,6 +252,7 @@ cudaError_t launch_combine(Prec x, const void* y, int64_t ld_y, int nslots, int6
 
 cudaError_t launch_gather(const void* src, Prec sp, int64_t ld_src, const int64_t* perm, int64_t n, int nrhs, void* dst,
                           Prec dp, int64_t ld_dst, cudaStream_t st) {
+  count_launches(1);
   dim3 g(vec_grid(n), unsigned(nrhs));
   if (sp == Prec::kD && dp == Prec::kD)
     gather_kernel<double, double><<<g, 256, 0, st>>>(static_cast<const double*>(src), ld_src, perm, n,
@@ -270,6 +281,7 @@ static void assemble_d(const PointsDev& P, const KernelDev& K, const TileDesc* t
 cudaError_t launch_assemble(int ndim, const PointsDev& P, const KernelDev& K, const TileDesc* tiles, int ntiles,
                             void* out, Prec op, cudaStream_t st) {
   if (ntiles <= 0) return cudaSuccess;
+  count_launches(1);
   switch (ndim) {
     case 1: assemble_d<1>(P, K, tiles, ntiles, out, op, st); break;
     case 2: assemble_d<2>(P, K, tiles, ntiles, out, op, st); break;
@@ -285,26 +297,27 @@ cudaError_t launch_assemble(int ndim, const PointsDev& P, const KernelDev& K, co
 }
 
 template <int D>
-static void compact_d(const PointsDev& P, const KernelDev& K, const double* ws, const CompactDesc* blocks, int nblocks,
-                      Prec op, cudaStream_t st) {
+static void compact_d(const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,
+                      const CompactDesc* blocks, int nblocks, Prec op, cudaStream_t st) {
   if (op == Prec::kD)
-    compact_kernel<D, double><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, blocks, nblocks);
+    compact_kernel<D, double><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, lmap, blocks, nblocks);
   else
-    compact_kernel<D, float><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, blocks, nblocks);
+    compact_kernel<D, float><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, lmap, blocks, nblocks);
 }
 
-cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws,
+cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,
                            const CompactDesc* blocks, int nblocks, Prec op, cudaStream_t st) {
   if (nblocks <= 0) return cudaSuccess;
+  count_launches(1);
   switch (ndim) {
-    case 1: compact_d<1>(P, K, ws, blocks, nblocks, op, st); break;
-    case 2: compact_d<2>(P, K, ws, blocks, nblocks, op, st); break;
-    case 3: compact_d<3>(P, K, ws, blocks, nblocks, op, st); break;
-    case 4: compact_d<4>(P, K, ws, blocks, nblocks, op, st); break;
-    case 5: compact_d<5>(P, K, ws, blocks, nblocks, op, st); break;
-    case 6: compact_d<6>(P, K, ws, blocks, nblocks, op, st); break;
-    case 7: compact_d<7>(P, K, ws, blocks, nblocks, op, st); break;
-    case 8: compact_d<8>(P, K, ws, blocks, nblocks, op, st); break;
+    case 1: compact_d<1>(P, K, ws, lmap, blocks, nblocks, op, st); break;
+    case 2: compact_d<2>(P, K, ws, lmap, blocks, nblocks, op, st); break;
+    case 3: compact_d<3>(P, K, ws, lmap, blocks, nblocks, op, st); break;
+    case 4: compact_d<4>(P, K, ws, lmap, blocks, nblocks, op, st); break;
+    case 5: compact_d<5>(P, K, ws, lmap, blocks, nblocks, op, st); break;
+    case 6: compact_d<6>(P, K, ws, lmap, blocks, nblocks, op, st); break;
+    case 7: compact_d<7>(P, K, ws, lmap, blocks, nblocks, op, st); break;
+    case 8: compact_d<8>(P, K, ws, lmap, blocks, nblocks, op, st); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

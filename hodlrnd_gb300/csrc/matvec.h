@@ -80,6 +80,7 @@ cudaError_t launch_assemble(int ndim, const PointsDev& P, const KernelDev& K, co
 // precision, or, for a block kept dense, evaluate its m x n tile into u_dst.
 struct CompactDesc {
   int64_t t_begin, s_begin;
+  int64_t t_map, s_map;  // offsets of the nodes' reference-order maps (low-rank blocks)
   int64_t ws;         // ACA workspace offset (doubles)
   void* u_dst;        // U or the dense tile
   void* v_dst;        // V (unused for dense blocks)
@@ -87,7 +88,8 @@ struct CompactDesc {
   int32_t cap;        // workspace columns (V starts after m * cap doubles)
   int32_t pad;
 };
-cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws,
+// U row i (reference order) lands on tree row lmap[t_map + i] - t_begin; V likewise.
+cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,
                            const CompactDesc* blocks, int nblocks, Prec op, cudaStream_t st);
 
 }  // namespace hodlr

@@ -206,6 +206,39 @@ class HODLRdD_matrix:
                                                s.ctypes.data_as(_I64), r.ctypes.data_as(_I32)))
         return dict(level=lv, t=t, s=s, rank=r)
 
+    def block(self, b):
+        """(U, V, dense) of far block b: U V^T approximates the block (the L, R of
+        LowRankMat, include/LowRank_matrix.hpp:10); a dense block comes back as U."""
+        self._need_op()
+        m, n, r, d = (ctypes.c_int32() for _ in range(4))
+        L = _lib.lib()
+        _lib.check(L.hodlr_get_block(self._op, int(b), ctypes.byref(m), ctypes.byref(n), ctypes.byref(r),
+                                     ctypes.byref(d), None, None))
+        if d.value:
+            U = np.zeros((n.value, m.value))
+            _lib.check(L.hodlr_get_block(self._op, int(b), None, None, None, None, _dp(U), None))
+            return U.T.copy(), None, True
+        U = np.zeros((r.value, m.value))
+        V = np.zeros((r.value, n.value))
+        _lib.check(L.hodlr_get_block(self._op, int(b), None, None, None, None, _dp(U), _dp(V)))
+        return U.T.copy(), V.T.copy(), False
+
+    def trace(self, on=None):
+        """Enable/disable tracing (on=True/False) or read the accumulated figures."""
+        self._need_op()
+        L = _lib.lib()
+        if on is not None:
+            _lib.check(L.hodlr_trace_enable(self._op, 1 if on else 0), self._ctx)
+            return None
+        t = _lib.HodlrTrace()
+        _lib.check(L.hodlr_trace_get(self._op, ctypes.byref(t)), self._ctx)
+        out = {}
+        for k, name in _lib.TRACE_NAMES.items():
+            if t.launches[k]:
+                out[name] = dict(launches=int(t.launches[k]), total_ms=float(t.total_ms[k]),
+                                 bytes_per_launch=float(t.bytes_per_launch[k]))
+        return out
+
     def permutation(self):
         self._need_op()
         p = np.zeros(self.N, np.int64)

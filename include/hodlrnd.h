@@ -161,6 +161,42 @@ int hodlr_get_permutation(const hodlr_op* op, int64_t* perm);
  * for a block kept dense, LowRank_matrix.hpp:348-363). */
 int hodlr_get_blocks(const hodlr_op* op, int32_t* level, int64_t* target, int64_t* source, int32_t* rank);
 
+/* Factors of far block b (order of hodlr_get_blocks), converted to FP64:
+ * U (m x rank) and V (n x rank) column major with A_b ~ U V^T, the L and R of
+ * LowRankMat (include/LowRank_matrix.hpp:10,61); for a block kept dense
+ * (*dense = 1) U receives the m x n block and V is not written.  m and n are
+ * the point counts of the target and source nodes; pass NULL to only query. */
+int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32_t* rank, int32_t* dense, double* U,
+                    double* V);
+
+/* ---- tracing ------------------------------------------------------------
+ * CUDA events around every kernel launch that applies the operator, so that
+ * a caller can relate device time to the algorithmic bytes each launch must
+ * move.  No counterpart in the reference, which only times whole phases with
+ * omp_get_wtime (include/HDD_tree.hpp:77-81,95-99). */
+#define HODLR_TRACE_KINDS 16
+#define HODLR_TRACE_ZGEMV_FP64 0   /* z = V^T x, FP64 vectors */
+#define HODLR_TRACE_NEAR_FP64 1    /* near-field leaf panels, FP64 vectors */
+#define HODLR_TRACE_FAR_FP64 2     /* far-field panels (U z and dense far blocks), FP64 vectors */
+#define HODLR_TRACE_COMBINE_FP64 3 /* sum of the per-level output slots */
+#define HODLR_TRACE_ZGEMV_FP32 4   /* the same four for FP32 vectors (mixed-precision inner solve) */
+#define HODLR_TRACE_NEAR_FP32 5
+#define HODLR_TRACE_FAR_FP32 6
+#define HODLR_TRACE_COMBINE_FP32 7
+
+typedef struct hodlr_trace {
+  uint64_t launches[HODLR_TRACE_KINDS];
+  double total_ms[HODLR_TRACE_KINDS];         /* summed CUDA-event durations */
+  double bytes_per_launch[HODLR_TRACE_KINDS]; /* algorithmic bytes one launch must move */
+} hodlr_trace;
+
+/* Enable (on != 0) or disable tracing; enabling clears the counters. */
+int hodlr_trace_enable(hodlr_op* op, int on);
+/* Wait for the traced launches and return the accumulated figures. */
+int hodlr_trace_get(hodlr_op* op, hodlr_trace* out);
+/* Number of kernels this library has launched in the process so far. */
+uint64_t hodlr_kernel_launches(void);
+
 /* ---- host-only tree planning (no device needed) ------------------------ */
 typedef struct hodlr_tree hodlr_tree;
 
