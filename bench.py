@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""HODLR solve throughput on one GB300 (and N independent replicas).
+
+Workload (HODLR3D, mixed precision): NDIM=3, N=262144 points i.i.d. uniform
+in [0,1]^3 (numpy PCG64, seeded), A_ij = 1/(N^(2/3) |x_i - x_j|), A_ii = 1,
+d' = 0, Nmax = 64, eps_ACA = 1e-8; far-field U, V stored in FP32; each solve is
+FP64 iterative refinement around FP32 GMRES (restart 100) to a relative
+residual of 1e-8; right-hand sides i.i.d. N(0,1).
+
+A step is one solve on the device-resident operator (the reference's
+HODLRdD_matrix::solve, include/HDD_matrix.hpp:51-62), with its right-hand side
+already in HBM; the operator build (tree, ACA, leaf blocks) happens once
+before the timed region and is reported separately.  `e2e` repeats the steps
+through the host-pointer C ABI call (hodlr_solve), the copies in and out of
+pinned host memory inside the timed region.  The FP64 engine (FP64 factors,
+FP64 GMRES with x0 = b as the reference) is timed beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+With N > 1 (torchrun) every rank builds and solves its own instance
+(different seed): replicas, no collective on the data path.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_POINTS = 262144
+NDIM, NMAX, DPRIME, EPS = 3, 64, 0, 1e-8
+SEED = 20261203
+CPU_SAMPLE_ITERS = 4
+
+
+def workload(n, rank):
+    rng = np.random.default_rng(SEED + rank)
+    pts = rng.uniform(0.0, 1.0, (n, NDIM))
+    return pts, 1.0 / n ** (2.0 / 3.0)
+
+
+def config(n, impl_note):
+    return {"workload": f"HODLR3D solve, N={n} uniform [0,1]^3, A_ij=1/(N^(2/3) r), A_ii=1, d'=0, Nmax=64, "
+                        f"eps_ACA=1e-8, FP32 factors + FP64 iterative refinement to 1e-8 rel. residual",
+            "n": n, "ndim": NDIM, "nmax": NMAX, "dprime": DPRIME, "eps_aca": EPS, "tol": EPS, "restart": 100,
+            "rhs": "N(0,1), one per step", "l2": "inputs larger than L2 (the stored operator is several GB)",
+            "impl_note": impl_note}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) of this GPU while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id):
+        self.gpu_id = gpu_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu_id), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_hbm_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel):
+    """DRAM bytes per launch of `kernel` recorded from an ncu capture (profiles/ncu_traffic.txt)."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    try:
+        for ln in open(path):
+            parts = ln.split()
+            if len(parts) >= 2 and parts[0] == kernel and not ln.startswith("#"):
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(pts, scale, fp64_iters):
+    """The CPU oracle (the reference algorithm restated in C++, OpenMP over all
+    host cores) on the same workload: operator build, then a bounded sample of
+    CPU_SAMPLE_ITERS GMRES iterations scaled to a full FP64 solve."""
+    from oracle.oracle import OracleHODLR
+
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O = OracleHODLR(pts, [0.0] * NDIM, [1.0] * NDIM, nmax=NMAX, dprime=DPRIME, eps=EPS, kind=1, scale=scale,
+                    diag=1.0, rng_mode=1, threads=cores)
+    t_build = time.perf_counter() - t0
+    b = np.random.default_rng(7).standard_normal(len(pts))
+    t0 = time.perf_counter()
+    O.solve(b, restart=CPU_SAMPLE_ITERS, max_iter=CPU_SAMPLE_ITERS, tol=1e-300)
+    t_sample = time.perf_counter() - t0
+    per_iter = t_sample / (CPU_SAMPLE_ITERS + 1)  # the sample runs k iterations plus one initial and one restart matvec
+    solve_s = per_iter * (fp64_iters + 2)
+    return {"value": 1.0 / solve_s, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"CPU oracle (reference algorithm restated in C++, OpenMP) on the same N={len(pts)} operator; "
+                      f"{CPU_SAMPLE_ITERS} GMRES iterations timed ({t_sample:.2f} s) and scaled to the "
+                      f"{fp64_iters} iterations of the FP64 solve; build {t_build:.1f} s not included"}
+
+
+def run_gb300(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import hodlrnd_gb300 as h
+    from hodlrnd_gb300 import _lib
+
+    n = args.n
+    pts, scale = workload(n, rank)
+    kern = h.Kernel("inv_r", scale, 1.0)
+    box = ([0.0] * NDIM, [1.0] * NDIM)
+    common = dict(Nmax=NMAX, eps_ACA=EPS, INTERACTION_TYPE_ALLOWED=DPRIME, tol=EPS, device=local)
+    t0 = time.perf_counter()
+    M = h.HODLRdD_matrix(kern, pts, *box, precision="mixed", **common).Assemble_matrix_operators()
+    build_s = time.perf_counter() - t0
+    stats = M.statistics()
+    M64 = h.HODLRdD_matrix(kern, pts, *box, precision="fp64", **common).Assemble_matrix_operators()
+    stats64 = M64.statistics()
+
+    K, W = args.steps, args.warmup
+    g = torch.Generator(device="cuda").manual_seed(SEED + 1000 + rank)
+    B = torch.randn((K + W, n), generator=g, dtype=torch.float64, device="cuda")
+    X = torch.empty_like(B)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    for k in range(W):
+        M.solve_device(B[K + k].data_ptr(), X[K + k].data_ptr(), 1, sp)
+    torch.cuda.synchronize()
+
+    # ---- timed region: K solves, inputs resident in HBM
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    try:
+        gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        gpu_id = local
+    clocks = ClockSampler(gpu_id)
+    M.trace(True)
+    launches0 = _lib.lib().hodlr_kernel_launches()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    t_all0 = torch.cuda.Event(enable_timing=True)
+    t_all1 = torch.cuda.Event(enable_timing=True)
+    t_all0.record(stream)
+    infos = []
+    for k in range(K):
+        ev[k][0].record(stream)
+        infos.append(M.solve_device(B[k].data_ptr(), X[k].data_ptr(), 1, sp))
+        ev[k][1].record(stream)
+    t_all1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    launches = _lib.lib().hodlr_kernel_launches() - launches0
+    trace = M.trace()
+    M.trace(False)
+    total_ms = t_all0.elapsed_time(t_all1)
+    step_ms = np.array([a.elapsed_time(b) for a, b in ev])
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = K * world / (total_ms / 1e3)
+
+    # ---- FP64 engine on the same right-hand sides (the plain FP64 GPU path)
+    k64 = max(1, min(args.fp64_steps, K))
+    X64 = torch.empty_like(B[:k64])
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    infos64 = [M64.solve_device(B[k].data_ptr(), X64[k].data_ptr(), 1, sp) for k in range(k64)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_sps = k64 / (e0.elapsed_time(e1) / 1e3)
+
+    # ---- accuracy: residual of the mixed solution against the FP64 operator
+    x0 = X[0].cpu().numpy()
+    b0 = B[0].cpu().numpy()
+    r64 = float(np.linalg.norm(b0 - M64 * x0) / np.linalg.norm(b0))
+    x64 = X64[0].cpu().numpy()
+    mixed_vs_fp64 = float(np.linalg.norm(x0 - x64) / np.linalg.norm(x64))
+
+    # ---- end to end through the host-pointer C ABI (pinned host buffers)
+    hb = torch.empty((K, n), dtype=torch.float64, pin_memory=True)
+    hx = torch.empty((K, n), dtype=torch.float64, pin_memory=True)
+    hb.copy_(B[:K].cpu())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(K):
+        M.solve(hb[k].numpy(), out=hx[k].numpy())
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+
+    # ---- roofline of the dominant kernel (largest share of traced device time)
+    dom = max(trace.items(), key=lambda kv: kv[1]["total_ms"]) if trace else None
+    peak, peak_src = measured_hbm_peak()
+    roofline = None
+    if dom:
+        name, d = dom
+        per_launch_s = d["total_ms"] / d["launches"] / 1e3
+        achieved = d["bytes_per_launch"] / per_launch_s / 1e9
+        traffic = traffic_from_profiles(name)
+        roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                    "bytes_per_launch": d["bytes_per_launch"], "launches": d["launches"],
+                    "avg_launch_us": round(per_launch_s * 1e6, 2),
+                    "share_of_traced_ms": round(d["total_ms"] / sum(v["total_ms"] for v in trace.values()), 4),
+                    "traffic": traffic}
+
+    iters = [i["iterations"] for i in infos]
+    out = {"metric": "solves/s (mixed FP32/FP64 HODLR3D solve to 1e-8 rel. residual)", "value": round(value, 3),
+           "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 3),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+           "data": "synthetic (seeded uniform points, N(0,1) right-hand sides)", "config": config(n, "GB300 engine"),
+           "latency_ms": {"p50": round(float(np.percentile(step_ms, 50)), 3),
+                          "p99": round(float(np.percentile(step_ms, 99)), 3)},
+           "fp64_engine": {"value": round(fp64_sps, 3), "unit": "solves/s", "steps": k64,
+                           "iterations": [i["iterations"] for i in infos64],
+                           "speedup_mixed_vs_fp64": round(value / world / fp64_sps, 3)},
+           "solve": {"inner_iterations": iters, "outer_iterations": [i["outer_iterations"] for i in infos],
+                     "rel_residual_stored_operator": max(i["rel_residual"] for i in infos),
+                     "rel_residual_fp64_operator": r64, "rel_diff_vs_fp64_solution": mixed_vs_fp64},
+           "build": {"mixed_s": round(build_s, 3), "tree_s": round(stats["t_tree_s"], 3),
+                     "aca_s": round(stats["t_aca_s"], 3), "near_s": round(stats["t_near_s"], 3),
+                     "fp64_aca_s": round(stats64["t_aca_s"], 3), "far_blocks": stats["n_far_blocks"],
+                     "dense_far_blocks": stats["n_dense_far_blocks"], "max_rank": stats["max_rank"],
+                     "far_bytes_fp32": stats["far_bytes"], "far_bytes_fp64": stats64["far_bytes"],
+                     "near_bytes_fp64": stats64["near_bytes"], "device_bytes": stats["device_bytes"],
+                     "n_flop_reference_metric": stats["n_flop"]},
+           "roofline": roofline,
+           "trace": {k: {"launches": v["launches"], "ms": round(v["total_ms"], 3),
+                         "GBps": round(v["bytes_per_launch"] * v["launches"] / (v["total_ms"] / 1e3) / 1e9, 1)}
+                     for k, v in trace.items()},
+           "e2e": {"value": round(K * world / e2e_s, 3), "unit": "solves/s", "h2d_bytes_per_step": 8 * n,
+                   "d2h_bytes_per_step": 8 * n},
+           "gpu_launches": int(launches), "clocks": clk}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(pts, scale, int(np.median([i["iterations"] for i in infos64])))
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    M.close()
+    M64.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference's algorithm on the host cores: the CPU oracle (a C++
+    restatement of HODLRnD's tree, ACA, matvec and GMRES, OpenMP over blocks and
+    nodes).  The reference's own headers only build here against a project
+    shim and not on the GPU host.  Each step is a bounded sample: CPU_SAMPLE_ITERS
+    GMRES iterations, scaled to the iteration count of one full FP64 solve
+    (x0 = b, restart 100, tol 1e-8) run once during warm-up."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle.oracle import OracleHODLR
+
+    n = args.n
+    pts, scale = workload(n, 0)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O = OracleHODLR(pts, [0.0] * NDIM, [1.0] * NDIM, nmax=NMAX, dprime=DPRIME, eps=EPS, kind=1, scale=scale,
+                    diag=1.0, rng_mode=1, threads=cores)
+    t_build = time.perf_counter() - t0
+    rng = np.random.default_rng(SEED + 1000)
+    b = rng.standard_normal(n)
+    t0 = time.perf_counter()
+    _, full_iters, res = O.solve(b, restart=100, tol=EPS)
+    t_full = time.perf_counter() - t0
+    for _ in range(max(0, args.warmup - 1)):
+        O.solve(rng.standard_normal(n), restart=CPU_SAMPLE_ITERS, max_iter=CPU_SAMPLE_ITERS, tol=1e-300)
+    step_s = []
+    for _ in range(args.steps):
+        bb = rng.standard_normal(n)
+        t0 = time.perf_counter()
+        O.solve(bb, restart=CPU_SAMPLE_ITERS, max_iter=CPU_SAMPLE_ITERS, tol=1e-300)
+        dt = time.perf_counter() - t0
+        step_s.append(dt / (CPU_SAMPLE_ITERS + 1) * (full_iters + 2))
+    ms = float(np.mean(step_s)) * 1e3
+    value = 1e3 / ms
+    sample = (f"{CPU_SAMPLE_ITERS} GMRES iterations per step on the same N={n} operator, scaled to the {full_iters} "
+              f"iterations of one full FP64 solve (measured once: {t_full:.1f} s, rel. residual {res:.1e}); "
+              f"build {t_build:.1f} s not timed")
+    out = {"impl": "reference", "metric": "solves/s (mixed FP32/FP64 HODLR3D solve to 1e-8 rel. residual)",
+           "value": round(value, 5), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded uniform points, N(0,1) right-hand sides)",
+           "config": config(n, "CPU oracle: the reference algorithm restated in C++ (FP64 throughout)"),
+           "cpu_baseline": {"value": round(value, 5), "unit": "solves/s", "cores": cores, "kind": "port",
+                            "sample": sample},
+           "e2e": {"value": round(value, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--n", type=int, default=N_POINTS)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

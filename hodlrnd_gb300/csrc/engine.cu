@@ -194,6 +194,8 @@ struct hodlr_op {
   float* d_d32 = nullptr;
   double* d_io = nullptr;    // caller-order staging, n
   double* d_io2 = nullptr;
+  double* d_hb = nullptr;    // host-API staging of one right-hand side and its solution
+  double* d_hx = nullptr;
   double* d_part = nullptr;  // kVecCtas partials
   double* d_scal = nullptr;  // scalars
   double* h_scal = nullptr;  // pinned
@@ -897,6 +899,8 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
     op->d_r64 = op->mem.alloc_n<double>(size_t(n), "residual");
     op->d_io = op->mem.alloc_n<double>(size_t(n), "staging");
     op->d_io2 = op->mem.alloc_n<double>(size_t(n), "staging");
+    op->d_hb = op->mem.alloc_n<double>(size_t(n), "host staging");
+    op->d_hx = op->mem.alloc_n<double>(size_t(n), "host staging");
     op->d_part = op->mem.alloc_n<double>(size_t(kVecCtas), "partials");
     op->d_scal = op->mem.alloc_n<double>(8, "scalars");
     CK(cudaMallocHost(&op->h_scal, sizeof(double) * 8));
@@ -1015,14 +1019,17 @@ int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_so
     CK(cudaSetDevice(op->p.device));
     cudaStream_t st = op->ctx->stream;
     const int64_t n = op->n;
-    double* db = op->mem.alloc_n<double>(size_t(n * nrhs), "solve rhs");
-    double* dx = op->mem.alloc_n<double>(size_t(n * nrhs), "solve solution");
+    const bool staged = nrhs == 1;
+    double* db = staged ? op->d_hb : op->mem.alloc_n<double>(size_t(n * nrhs), "solve rhs");
+    double* dx = staged ? op->d_hx : op->mem.alloc_n<double>(size_t(n * nrhs), "solve solution");
     CK(cudaMemcpyAsync(db, b, sizeof(double) * size_t(n * nrhs), cudaMemcpyHostToDevice, st));
     const int rc = hodlr_solve_device(op, db, dx, nrhs, st, info);
     cudaMemcpyAsync(x, dx, sizeof(double) * size_t(n * nrhs), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
-    op->mem.release(db);
-    op->mem.release(dx);
+    if (!staged) {
+      op->mem.release(db);
+      op->mem.release(dx);
+    }
     return rc;
   });
 }

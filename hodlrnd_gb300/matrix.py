@@ -126,14 +126,20 @@ class HODLRdD_matrix:
         _lib.check(_lib.lib().hodlr_matvec_device(self._op, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), nrhs,
                                                   ctypes.c_void_p(stream)), self._ctx)
 
-    def solve(self, b, *, raise_on_stall=False):
+    def solve(self, b, *, out=None, raise_on_stall=False):
         """x with A x = b (HODLRdD_matrix::solve): FP64 GMRES with x0 = b, or
-        FP64 iterative refinement around FP32 GMRES in mixed precision."""
+        FP64 iterative refinement around FP32 GMRES in mixed precision.
+        `out` (same shape as b, float64, Fortran order) receives x in place."""
         self._need_op()
         b = np.asarray(b, dtype=np.float64)
         vec = b.ndim == 1
         B = np.asfortranarray(b.reshape(self.N, -1))
-        X = np.zeros_like(B, order="F")
+        if out is not None:
+            X = out.reshape(self.N, -1)
+            if X.dtype != np.float64 or not X.flags.f_contiguous:
+                raise ValueError("out must be a float64 Fortran-ordered array")
+        else:
+            X = np.zeros_like(B, order="F")
         info = _lib.HodlrSolveInfo()
         rc = _lib.lib().hodlr_solve(self._op, _dp(B), _dp(X), B.shape[1], ctypes.byref(info))
         self.last_solve = {k: getattr(info, k) for k, _ in info._fields_ if k != "reserved"}
