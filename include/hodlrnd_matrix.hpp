@@ -1,0 +1,129 @@
+// hodlrnd_matrix.hpp -- header-only C++17 facade over the C ABI (hodlrnd.h)
+// with the class and method names of HODLRnD's HODLRdD_matrix<Kernel>
+// (include/HDD_matrix.hpp:10-89), so that reference user code keeps its shape:
+//
+//   kernel_3d k;                                   // provides gpu_kernel_desc()
+//   hodlrnd::HODLRdD_matrix<kernel_3d> Kmat(&k, points, x1, x2, params);
+//   Kmat.Assemble_matrix_operators();
+//   std::vector<double> b = Kmat * x;              // operator*
+//   std::vector<double> y = Kmat.solve(b);         // GMRES, x0 = b
+//   Kmat.print_matrix_statistics();
+//
+// Differences a reference user sees:
+//  * the kernel describes itself with gpu_kernel_desc() (kind, scale, diag)
+//    instead of answering getMatrixEntry(i, j) per entry -- the GPU engine
+//    evaluates entries itself and never calls back into host code;
+//  * NDIM, Nmax, eps_ACA and INTERACTION_TYPE_ALLOWED are runtime fields of
+//    hodlr_params instead of compile-time constants (include/myHeaders.hpp:35-48);
+//  * points are a flat n x ndim row-major array (the x[] of ptsnD) and vectors
+//    are std::vector<double> instead of Eigen::VectorXd;
+//  * failures throw hodlrnd::Error carrying the C ABI's status and message.
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hodlrnd.h"
+
+namespace hodlrnd {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+inline void check(int rc, const hodlr_ctx* ctx) {
+  if (rc != HODLR_OK) throw Error(rc, hodlr_last_error(ctx));
+}
+
+inline hodlr_params default_params(int ndim) {
+  hodlr_params p;
+  hodlr_params_default(&p);
+  p.ndim = ndim;
+  return p;
+}
+
+template <class Kernel>
+class HODLRdD_matrix {
+ public:
+  // HODLRdD_matrix(Kernel*&, std::vector<ptsnD>*&, VectorXd x1, VectorXd x2)
+  // (include/HDD_matrix.hpp:20-33); points: n x ndim row major.
+  HODLRdD_matrix(Kernel* kernel, const std::vector<double>& points, const std::vector<double>& x1,
+                 const std::vector<double>& x2, const hodlr_params& params)
+      : kernel_(kernel), points_(points), x1_(x1), x2_(x2), p_(params) {
+    if (p_.ndim < 1 || x1.size() != size_t(p_.ndim) || x2.size() != size_t(p_.ndim) ||
+        points.size() % size_t(p_.ndim) != 0)
+      throw Error(HODLR_ERR_INVALID, "HODLRdD_matrix: points / box do not match ndim");
+    n_ = int64_t(points.size() / size_t(p_.ndim));
+    check(hodlr_ctx_create(&p_, &ctx_), nullptr);
+  }
+  HODLRdD_matrix(const HODLRdD_matrix&) = delete;
+  HODLRdD_matrix& operator=(const HODLRdD_matrix&) = delete;
+  ~HODLRdD_matrix() {
+    hodlr_op_destroy(op_);
+    hodlr_ctx_destroy(ctx_);
+  }
+
+  size_t get_size() const { return size_t(n_); }
+
+  // Assemble_matrix_operators (include/HDD_matrix.hpp:39-41)
+  void Assemble_matrix_operators() {
+    hodlr_op_destroy(op_);
+    op_ = nullptr;
+    const hodlr_kernel_desc kd = kernel_->gpu_kernel_desc();
+    check(hodlr_build(ctx_, points_.data(), n_, x1_.data(), x2_.data(), &kd, &op_), ctx_);
+  }
+
+  // operator* (include/HDD_matrix.hpp:43-47)
+  std::vector<double> operator*(const std::vector<double>& x) {
+    need_op();
+    std::vector<double> y(x.size());
+    check(hodlr_matvec(op_, x.data(), y.data(), 1), ctx_);
+    return y;
+  }
+
+  // solve (include/HDD_matrix.hpp:51-62); the reference's GMRES iteration count
+  // is in last_solve().iterations.
+  std::vector<double> solve(const std::vector<double>& b) {
+    need_op();
+    std::vector<double> x(b.size());
+    const int rc = hodlr_solve(op_, b.data(), x.data(), 1, &info_);
+    if (rc != HODLR_OK && rc != HODLR_ERR_NOT_CONVERGED) check(rc, ctx_);
+    return x;
+  }
+  const hodlr_solve_info& last_solve() const { return info_; }
+
+  hodlr_stats statistics() const {
+    hodlr_stats s;
+    check(hodlr_stats_get(op_, &s), ctx_);
+    return s;
+  }
+
+  // print_matrix_statistics (include/HDD_matrix.hpp:69-85)
+  void print_matrix_statistics() const {
+    const hodlr_stats s = statistics();
+    std::printf("Memory (in GB) : %g\nNumber of FLOP : %g\nCompression Ratio : %g\n", s.memory_gb, s.n_flop,
+                s.compression_ratio);
+    std::printf("Maximum rank across the Tree : %lld\nTime to Initialize (in s) : %g\nMatrix-Vector time (in s) : %g\n",
+                (long long)s.max_rank, s.t_build_s, s.t_matvec_s);
+  }
+
+  hodlr_op* handle() { return op_; }
+
+ private:
+  void need_op() const {
+    if (!op_) throw Error(HODLR_ERR_STATE, "call Assemble_matrix_operators() first");
+  }
+  Kernel* kernel_;
+  std::vector<double> points_, x1_, x2_;
+  hodlr_params p_;
+  int64_t n_ = 0;
+  hodlr_ctx* ctx_ = nullptr;
+  hodlr_op* op_ = nullptr;
+  hodlr_solve_info info_{};
+};
+
+}  // namespace hodlrnd
