@@ -31,7 +31,7 @@ def declared_symbols():
     for name in os.listdir(os.path.join(ROOT, "include")):
         if name.endswith(".h"):
             text = open(os.path.join(ROOT, "include", name)).read()
-            syms |= set(re.findall(r"^\s*(?:int|void|const char\s*\*)\s+(hodlr_\w+)\s*\(", text, re.M))
+            syms |= set(re.findall(r"^\s*(?:int|void|uint64_t|const char\s*\*)\s+(hodlr_\w+)\s*\(", text, re.M))
     return sorted(syms)
 
 
