@@ -21,8 +21,14 @@
 using namespace hodlr;
 
 namespace {
-
 thread_local std::string g_thread_err;
+}
+
+namespace hodlr {
+void set_thread_error(const std::string& msg) { g_thread_err = msg; }
+}  // namespace hodlr
+
+namespace {
 
 double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();

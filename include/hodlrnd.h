@@ -197,6 +197,39 @@ int hodlr_trace_get(hodlr_op* op, hodlr_trace* out);
 /* Number of kernels this library has launched in the process so far. */
 uint64_t hodlr_kernel_launches(void);
 
+/* ---- one block, no allocation -------------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * where they need a block compressed (a framework that owns all device memory
+ * through its own pool, a loop that cannot afford cudaMalloc's implicit
+ * synchronisation): partially pivoted ACA of the single block
+ * A(rows, cols), with the same kernel, pivoting, restarts and stopping rule as
+ * hodlr_build, and with its bookkeeping in a fixed static device array (about
+ * 136 KB per GPU, held until the process exits) instead of allocated memory.
+ *  d_points  device, ndim x ld doubles, coordinate k of point i at k*ld + i
+ *  d_rows    device, m point indices (the block's rows, in the order the ACA
+ *            walks them; the reference walks a node's points by increasing index)
+ *  d_cols    device, n point indices (columns)
+ *  seed      the restart heuristic's random stream (hodlr_build seeds each
+ *            block from its level, target and source node)
+ *  cap       columns available in d_factors, at most HODLR_NOALLOC_MAX_RANK
+ *  d_factors device, (m + n) * cap doubles: U (m x cap) then V (n x cap),
+ *            column major; the first *rank columns hold U and V with A ~ U V^T
+ *  *rank, *flags  on return (host): flags bit 0 = the block is to be kept dense
+ *            (rank reached min(m,n) - 1; the factors are then not a
+ *            representation), bit 1 = cap columns were not enough.
+ * m and n above HODLR_NOALLOC_MAX_POINTS, or cap above HODLR_NOALLOC_MAX_RANK,
+ * are rejected with HODLR_ERR_INVALID.  The first call on a device looks the
+ * static array up (cudaGetSymbolAddress) and must come before any stream
+ * capture on that device.  All calls share the array: calls whose GPU work
+ * overlaps (other streams or threads) race and must be serialised.  Blocks
+ * until the result is known (synchronises `stream`). */
+#define HODLR_NOALLOC_MAX_POINTS 16384
+#define HODLR_NOALLOC_MAX_RANK 512
+int hodlr_aca_block_noalloc(const double* d_points, int64_t ld, int32_t ndim, const int32_t* d_rows, int32_t m,
+                            const int32_t* d_cols, int32_t n, const hodlr_kernel_desc* kernel, double eps_aca,
+                            uint64_t seed, int32_t cap, double* d_factors, int32_t* rank, int32_t* flags,
+                            void* stream);
+
 /* ---- host-only tree planning (no device needed) ------------------------ */
 typedef struct hodlr_tree hodlr_tree;
 
