@@ -103,6 +103,7 @@ def lib():
     L.hodlr_stats_get.argtypes = [P, ctypes.POINTER(HodlrStats)]
     L.hodlr_get_permutation.argtypes = [P, I64]
     L.hodlr_get_blocks.argtypes = [P, I32, I64, I64, I32]
+    L.hodlr_set_solver.argtypes = [P, ctypes.c_int32, ctypes.c_double, ctypes.c_int64, ctypes.c_double, ctypes.c_int32]
     L.hodlr_get_block.argtypes = [P, ctypes.c_int64, I32, I32, I32, I32, D, D]
     L.hodlr_trace_enable.argtypes = [P, ctypes.c_int]
     L.hodlr_trace_get.argtypes = [P, ctypes.POINTER(HodlrTrace)]
@@ -115,7 +116,7 @@ def lib():
     for f in ("hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
               "hodlr_matvec_device", "hodlr_solve", "hodlr_solve_device", "hodlr_stats_get",
               "hodlr_get_permutation", "hodlr_get_blocks", "hodlr_tree_build", "hodlr_tree_sizes",
-              "hodlr_tree_get", "hodlr_tree_destroy", "hodlr_get_block", "hodlr_trace_enable", "hodlr_trace_get"):
+              "hodlr_tree_get", "hodlr_tree_destroy", "hodlr_get_block", "hodlr_trace_enable", "hodlr_trace_get", "hodlr_set_solver"):
         getattr(L, f).restype = ctypes.c_int
     _lib = L
     return L

@@ -161,6 +161,8 @@ struct Plan {
   int nitems_far = 0;
   ZBlock* zb = nullptr;
   int nzb = 0;
+  ZItem* zitems = nullptr;
+  int nzitems = 0;
 };
 
 }  // namespace
@@ -378,8 +380,19 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   plan.segs_far = upload(op->mem, segs, st, "far segments");
   plan.items_far = upload(op->mem, items, st, "far items");
   plan.nitems_far = int(items.size());
+  std::vector<ZItem> zit;
+  for (size_t q = 0; q < zb.size(); q++) {
+    if (zb[q].n <= 32) {
+      zit.push_back({int32_t(q), 0, zb[q].r});
+    } else {
+      for (int k0 = 0; k0 < zb[q].r; k0 += kZCols)
+        zit.push_back({int32_t(q), k0, std::min(kZCols, zb[q].r - k0)});
+    }
+  }
   plan.zb = upload(op->mem, zb, st, "far z blocks");
   plan.nzb = int(zb.size());
+  plan.zitems = upload(op->mem, zit, st, "far z items");
+  plan.nzitems = int(zit.size());
 }
 
 // ACA of every far block, in workspace-bounded batches; compacted factors go
@@ -659,7 +672,7 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
   Tracer& tr = op->tr;
   if (plan.nzb > 0) tr.start(kb + 0, st);
-  if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.nzb, in, ldin, 1, st)) != cudaSuccess) return e;
+  if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.zitems, plan.nzitems, in, ldin, 1, st)) != cudaSuccess) return e;
   if (plan.nzb > 0) tr.stop(st);
   tr.start(kb + 1, st);
   if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.items_near, plan.nitems_near, in, ldin,
@@ -895,6 +908,8 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
       op->plan32.nitems_far = op->plan64.nitems_far;
       op->plan32.zb = op->plan64.zb;
       op->plan32.nzb = op->plan64.nzb;
+      op->plan32.zitems = op->plan64.zitems;
+      op->plan32.nzitems = op->plan64.nzitems;
     }
     // work vectors
     const int64_t ldin = n + op->zlen;
@@ -950,7 +965,7 @@ int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nr
       CK(cudaMemcpyAsync(op->d_in64, op->d_io, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, st));
       if (op->nslots > 1) CK(cudaMemsetAsync(op->d_y64 + n, 0, sizeof(double) * size_t(n) * (op->nslots - 1), st));
       const Plan& pl = op->plan64;
-      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.nzb, op->d_in64, ldin, 1, st));
+      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, op->d_in64, ldin, 1, st));
       CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.items_near, pl.nitems_near, op->d_in64,
                        ldin, op->d_y64, n, op->nslots, 1, st));
       CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.items_far, pl.nitems_far, op->d_in64, ldin,
@@ -1037,6 +1052,27 @@ int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_so
       op->mem.release(dx);
     }
     return rc;
+  });
+}
+
+int hodlr_set_solver(hodlr_op* op, int32_t restart, double tol, int64_t max_iter, double inner_tol,
+                     int32_t max_outer) {
+  if (!op) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_set_solver: null argument");
+  if (restart < 0 || restart > 1000) return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_set_solver: restart in 0..1000");
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    op->p.restart = restart;
+    op->p.tol = tol;
+    op->p.max_iter = max_iter;
+    op->p.inner_tol = inner_tol;
+    op->p.max_outer = max_outer;
+    const int r = restart > 0 ? restart : 100;
+    if (op->p.precision == HODLR_PREC_MIXED) {
+      if (r > op->g32.restart) CK(gmres_alloc<float>(op->g32, op->n, r));
+    } else if (r > op->g64.restart) {
+      CK(gmres_alloc<double>(op->g64, op->n, r));
+    }
+    return HODLR_OK;
   });
 }
 

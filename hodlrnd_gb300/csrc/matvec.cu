@@ -13,13 +13,19 @@ __device__ __forceinline__ T ldg(const T* p) {
   return __ldg(p);
 }
 
-// Phase 1: z_b = V_b^T x_s, one warp per low-rank block.
+// Phase 1: z_b = V_b^T x_s.  A block with n <= 32 is one warp's item: lanes
+// form groups of npad (next power of two >= n) that each take one column.  A
+// larger block is split into items of up to kZCols columns; the warp strides
+// over the n rows with independent accumulators per column, so a 32768-point
+// block is spread over r / kZCols warps instead of one.
 template <typename TA, typename TX, typename TACC>
-__global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ zb, int nzb, TX* in, int64_t ld_in) {
+__global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
+                                                    int nitems, TX* in, int64_t ld_in) {
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (w >= nzb) return;
-  const ZBlock Z = zb[w];
+  if (w >= nitems) return;
+  const ZItem it = items[w];
+  const ZBlock Z = zb[it.zb];
   const TA* V = static_cast<const TA*>(Z.V);
   const TX* x = in + blockIdx.y * ld_in + Z.x_off;
   TX* z = in + blockIdx.y * ld_in + Z.z_off;
@@ -37,19 +43,23 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
       if (j == 0 && k < r) z[k] = TX(acc);
     }
   } else {
-    for (int k = 0; k < r; k++) {
-      const TA* v = V + int64_t(k) * n;
-      TACC a0 = 0, a1 = 0;
-      int j = lane;
-      for (; j + 32 < n; j += 64) {
-        a0 += TACC(ldg(v + j)) * TACC(x[j]);
-        a1 += TACC(ldg(v + j + 32)) * TACC(x[j + 32]);
-      }
-      if (j < n) a0 += TACC(ldg(v + j)) * TACC(x[j]);
-      TACC acc = a0 + a1;
+    const int k0 = it.k0, nk = it.nk;
+    TACC acc[kZCols];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) z[k] = TX(acc);
+    for (int c = 0; c < kZCols; c++) acc[c] = TACC(0);
+    const TA* v = V + int64_t(k0) * n;
+    for (int j = lane; j < n; j += 32) {
+      const TACC xj = TACC(x[j]);
+#pragma unroll
+      for (int c = 0; c < kZCols; c++)
+        if (c < nk) acc[c] += TACC(ldg(v + int64_t(c) * n + j)) * xj;
+    }
+#pragma unroll
+    for (int c = 0; c < kZCols; c++) {
+      TACC a = acc[c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      if (lane == 0 && c < nk) z[k0 + c] = TX(a);
     }
   }
 }
@@ -93,23 +103,23 @@ __global__ void __launch_bounds__(256)
   } else {
     const int i = it.chunk * 32 + lane;
     const bool act = i < m;
-    TACC a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    TACC a[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) a[q] = TACC(0);
     for (int64_t s = P.seg_begin; s < P.seg_end; s++) {
       const Seg S = segs[s];
       const TA* A = static_cast<const TA*>(S.A) + i;
       const TX* x = inc + S.in_off;
       if (act) {
         int j = 0;
-        for (; j + 3 < S.K; j += 4) {
-          a0 += TACC(ldg(A + int64_t(j) * m)) * TACC(x[j]);
-          a1 += TACC(ldg(A + int64_t(j + 1) * m)) * TACC(x[j + 1]);
-          a2 += TACC(ldg(A + int64_t(j + 2) * m)) * TACC(x[j + 2]);
-          a3 += TACC(ldg(A + int64_t(j + 3) * m)) * TACC(x[j + 3]);
+        for (; j + 7 < S.K; j += 8) {
+#pragma unroll
+          for (int q = 0; q < 8; q++) a[q] += TACC(ldg(A + int64_t(j + q) * m)) * TACC(x[j + q]);
         }
-        for (; j < S.K; j++) a0 += TACC(ldg(A + int64_t(j) * m)) * TACC(x[j]);
+        for (; j < S.K; j++) a[0] += TACC(ldg(A + int64_t(j) * m)) * TACC(x[j]);
       }
     }
-    if (act) yo[i] = TX((a0 + a1) + (a2 + a3));
+    if (act) yo[i] = TX(((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7])));
   }
 }
 
@@ -193,17 +203,17 @@ unsigned vec_grid(int64_t n) {
 
 }  // namespace
 
-cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, int nzb, void* in, int64_t ld_in, int nrhs,
-                         cudaStream_t st) {
-  if (nzb <= 0) return cudaSuccess;
+cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, void* in, int64_t ld_in,
+                         int nrhs, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
   count_launches(1);
-  dim3 g(warps_grid(nzb), unsigned(nrhs));
+  dim3 g(warps_grid(nitems), unsigned(nrhs));
   if (a == Prec::kD && x == Prec::kD)
-    zgemv_kernel<double, double, double><<<g, 256, 0, st>>>(zb, nzb, static_cast<double*>(in), ld_in);
+    zgemv_kernel<double, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(in), ld_in);
   else if (a == Prec::kF && x == Prec::kD)
-    zgemv_kernel<float, double, double><<<g, 256, 0, st>>>(zb, nzb, static_cast<double*>(in), ld_in);
+    zgemv_kernel<float, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(in), ld_in);
   else if (a == Prec::kF && x == Prec::kF)
-    zgemv_kernel<float, float, float><<<g, 256, 0, st>>>(zb, nzb, static_cast<float*>(in), ld_in);
+    zgemv_kernel<float, float, float><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<float*>(in), ld_in);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

@@ -47,13 +47,21 @@ struct ZBlock {
   int32_t n, r;
 };
 
+// One warp's share of phase 1: columns [k0, k0 + nk) of block zb (all of
+// them for blocks with n <= 32, at most kZCols for larger ones).
+struct ZItem {
+  int32_t zb;
+  int32_t k0, nk;
+};
+constexpr int kZCols = 4;
+
 // Element types: A = stored matrix, X = vectors, ACC = accumulation.
 enum class Prec { kD, kF };  // double, float
 
 // in:   input buffer [x (ld_in rows of x) | z], nrhs columns with leading dimension ld_in
 // y:    output slots, slot s of column c at y + (c * nslots + s) * ld_y
-cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, int nzb, void* in, int64_t ld_in, int nrhs,
-                         cudaStream_t st);
+cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, void* in, int64_t ld_in,
+                         int nrhs, cudaStream_t st);
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* items, int nitems,
                           const void* in, int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs,
                           cudaStream_t st);

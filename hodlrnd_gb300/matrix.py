@@ -157,6 +157,12 @@ class HODLRdD_matrix:
             _lib.check(rc, self._ctx)
         return self.last_solve
 
+    def set_solver(self, restart=100, tol=None, max_iter=0, inner_tol=0.0, max_outer=0):
+        """Solver settings for later solves (iterSolver's arguments, include/GMRES.hpp:56-63)."""
+        self._need_op()
+        _lib.check(_lib.lib().hodlr_set_solver(self._op, int(restart), float(tol) if tol else 0.0, int(max_iter),
+                                               float(inner_tol), int(max_outer)), self._ctx)
+
     # ------------------------------------------------------------ introspection
     def statistics(self):
         self._need_op()

@@ -134,6 +134,12 @@ int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_so
 int hodlr_solve_device(hodlr_op* op, const double* d_b, double* d_x, int64_t nrhs, void* stream,
                        hodlr_solve_info* info);
 
+/* Solver settings of an existing operator, as iterSolver takes them per solve
+ * (restart, max_iter, tol: include/GMRES.hpp:56-63); restart/tol/max_iter
+ * <= 0 select 100 / eps_aca / N, inner_tol and max_outer <= 0 the defaults. */
+int hodlr_set_solver(hodlr_op* op, int32_t restart, double tol, int64_t max_iter, double inner_tol,
+                     int32_t max_outer);
+
 typedef struct hodlr_stats {
   int64_t n, depth, n_leaves, n_far_blocks, n_dense_far_blocks, n_near_blocks, max_rank;
   double n_flop;            /* Node::compute_flop_count summed (include/HDD_node.hpp:182-202) */
