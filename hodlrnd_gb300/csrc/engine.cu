@@ -275,7 +275,7 @@ NearTiles near_tiles(const Tree& t, const NearList& nl) {
       d.m = int32_t(t.count[size_t(gt)]);
       d.n = int32_t(t.count[size_t(gs)]);
       d.off = out.total;
-      out.total += int64_t(d.m) * d.n;
+      out.total += (lead_dim(d.m) * d.n + 3) / 4 * 4;
       out.tiles.push_back(d);
     }
   return out;
@@ -309,7 +309,8 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
     p.seg_end = int64_t(segs.size());
     const int np = int(panels.size());
     panels.push_back(p);
-    const int chunks = p.m <= 32 ? 1 : int((p.m + 31) / 32);
+    const int rows = 32 * (a == Prec::kD ? 2 : 4);
+    const int chunks = p.m <= 32 ? 1 : int((p.m + rows - 1) / rows);
     for (int c = 0; c < chunks; c++) items.push_back({np, c});
   }
   plan.a_near = a;
@@ -369,7 +370,8 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
     if (p.seg_end > p.seg_begin) {
       const int np = int(panels.size());
       panels.push_back(p);
-      const int chunks = p.m <= 32 ? 1 : int((p.m + 31) / 32);
+      const int rows = 32 * (a == Prec::kD ? 2 : 4);
+      const int chunks = p.m <= 32 ? 1 : int((p.m + rows - 1) / rows);
       for (int c = 0; c < chunks; c++) items.push_back({np, c});
     }
     b = e;
@@ -549,8 +551,10 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
       op->rank[b] = out[q].rank;
       op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
       off[q] = bytes;
-      const uint64_t e = op->dense[b] ? uint64_t(mm[b]) * nn[b] : uint64_t(mm[b] + nn[b]) * uint64_t(op->rank[b]);
-      bytes += (e * esz + 255) / 256 * 256;
+      const uint64_t r = uint64_t(op->rank[b]);
+      const uint64_t ub = (uint64_t(lead_dim(mm[b])) * (op->dense[b] ? uint64_t(nn[b]) : r) * esz + 15) / 16 * 16;
+      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(lead_dim(nn[b])) * r * esz + 15) / 16 * 16;
+      bytes += ub + vb;
     }
     if (bytes > 0) {
       char* chunk = static_cast<char*>(op->mem.alloc(bytes, "far-field factors"));
@@ -564,7 +568,7 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
         c.s_map = desc[q].s_map;
         c.ws = desc[q].ws;
         c.u_dst = chunk + off[q];
-        c.v_dst = chunk + off[q] + uint64_t(mm[b]) * uint64_t(std::max(op->rank[b], 0)) * esz;
+        c.v_dst = chunk + off[q] + (uint64_t(lead_dim(mm[b])) * uint64_t(std::max(op->rank[b], 0)) * esz + 15) / 16 * 16;
         c.m = mm[b];
         c.n = nn[b];
         c.rank = op->rank[b];
@@ -1112,24 +1116,29 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
     if (rank) *rank = op->rank[size_t(b)];
     if (dense) *dense = op->dense[size_t(b)];
     const bool f32 = op->p.precision == HODLR_PREC_MIXED;
-    auto fetch = [&](const void* src, size_t count, double* dst) {
-      if (!dst || !src || count == 0) return;
+    // copy rows x cols (stored with leading dimension lead_dim(rows)) to a dense column-major dst
+    auto fetch = [&](const void* src, size_t rows, size_t cols, double* dst) {
+      if (!dst || !src || rows * cols == 0) return;
+      const size_t ld = size_t(lead_dim(int64_t(rows)));
+      std::vector<double> tmp(ld * cols);
       if (f32) {
-        std::vector<float> tmp(count);
-        CK(cudaMemcpy(tmp.data(), src, count * 4, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < count; i++) dst[i] = double(tmp[i]);
+        std::vector<float> t32(ld * cols);
+        CK(cudaMemcpy(t32.data(), src, t32.size() * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < t32.size(); i++) tmp[i] = double(t32[i]);
       } else {
-        CK(cudaMemcpy(dst, src, count * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(tmp.data(), src, tmp.size() * 8, cudaMemcpyDeviceToHost));
       }
+      for (size_t c = 0; c < cols; c++)
+        for (size_t r = 0; r < rows; r++) dst[c * rows + r] = tmp[c * ld + r];
     };
     CK(cudaSetDevice(op->p.device));
     CK(cudaStreamSynchronize(op->ctx->stream));
     if (op->dense[size_t(b)]) {
-      fetch(op->uptr[size_t(b)], size_t(mm) * size_t(nn), U);
+      fetch(op->uptr[size_t(b)], size_t(mm), size_t(nn), U);
     } else {
       const size_t r = size_t(std::max(op->rank[size_t(b)], 0));
-      fetch(op->uptr[size_t(b)], size_t(mm) * r, U);
-      fetch(op->vptr[size_t(b)], size_t(nn) * r, V);
+      fetch(op->uptr[size_t(b)], size_t(mm), r, U);
+      fetch(op->vptr[size_t(b)], size_t(nn), r, V);
     }
     return HODLR_OK;
   });

@@ -13,6 +13,42 @@ __device__ __forceinline__ T ldg(const T* p) {
   return __ldg(p);
 }
 
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+};
+
+template <typename TACC>
+__device__ __forceinline__ TACC dot16(const float4& a, const TACC* x) {
+  return TACC(a.x) * x[0] + TACC(a.y) * x[1] + TACC(a.z) * x[2] + TACC(a.w) * x[3];
+}
+template <typename TACC>
+__device__ __forceinline__ TACC dot16(const double2& a, const TACC* x) {
+  return TACC(a.x) * x[0] + TACC(a.y) * x[1];
+}
+__device__ __forceinline__ void axpy16(const float4& a, float s, float* acc) {
+  acc[0] += a.x * s;
+  acc[1] += a.y * s;
+  acc[2] += a.z * s;
+  acc[3] += a.w * s;
+}
+__device__ __forceinline__ void axpy16(const float4& a, double s, double* acc) {
+  acc[0] += double(a.x) * s;
+  acc[1] += double(a.y) * s;
+  acc[2] += double(a.z) * s;
+  acc[3] += double(a.w) * s;
+}
+__device__ __forceinline__ void axpy16(const double2& a, double s, double* acc) {
+  acc[0] += a.x * s;
+  acc[1] += a.y * s;
+}
+
 // Phase 1: z_b = V_b^T x_s.  A block with n <= 32 is one warp's item: lanes
 // form groups of npad (next power of two >= n) that each take one column.  A
 // larger block is split into items of up to kZCols columns; the warp strides
@@ -43,16 +79,25 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
       if (j == 0 && k < r) z[k] = TX(acc);
     }
   } else {
+    // 16 bytes per lane: RPL consecutive rows of kZCols columns
+    constexpr int RPL = 16 / int(sizeof(TA));
+    using VT = typename Vec16<TA>::type;
+    const int64_t ldv = lead_dim(n);
     const int k0 = it.k0, nk = it.nk;
     TACC acc[kZCols];
 #pragma unroll
     for (int c = 0; c < kZCols; c++) acc[c] = TACC(0);
-    const TA* v = V + int64_t(k0) * n;
-    for (int j = lane; j < n; j += 32) {
-      const TACC xj = TACC(x[j]);
+    const TA* v = V + int64_t(k0) * ldv;
+    for (int j = lane * RPL; j < n; j += 32 * RPL) {
+      TACC xv[RPL];
+#pragma unroll
+      for (int q = 0; q < RPL; q++) xv[q] = (j + q < n) ? TACC(x[j + q]) : TACC(0);
 #pragma unroll
       for (int c = 0; c < kZCols; c++)
-        if (c < nk) acc[c] += TACC(ldg(v + int64_t(c) * n + j)) * xj;
+        if (c < nk) {
+          const VT a = __ldg(reinterpret_cast<const VT*>(v + int64_t(c) * ldv + j));
+          acc[c] += dot16<TACC>(a, xv);
+        }
     }
 #pragma unroll
     for (int c = 0; c < kZCols; c++) {
@@ -101,25 +146,39 @@ __global__ void __launch_bounds__(256)
     for (int o = mpad; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (sl == 0 && i < m) yo[i] = TX(acc);
   } else {
-    const int i = it.chunk * 32 + lane;
+    // 16 bytes per lane: rows [i, i + RPL) of each column
+    constexpr int RPL = 16 / int(sizeof(TA));
+    using VT = typename Vec16<TA>::type;
+    const int64_t ld = lead_dim(m);
+    const int i = it.chunk * 32 * RPL + lane * RPL;
     const bool act = i < m;
-    TACC a[8];
+    TACC a0[RPL], a1[RPL];
 #pragma unroll
-    for (int q = 0; q < 8; q++) a[q] = TACC(0);
+    for (int q = 0; q < RPL; q++) a0[q] = a1[q] = TACC(0);
     for (int64_t s = P.seg_begin; s < P.seg_end; s++) {
       const Seg S = segs[s];
       const TA* A = static_cast<const TA*>(S.A) + i;
       const TX* x = inc + S.in_off;
       if (act) {
         int j = 0;
-        for (; j + 7 < S.K; j += 8) {
-#pragma unroll
-          for (int q = 0; q < 8; q++) a[q] += TACC(ldg(A + int64_t(j + q) * m)) * TACC(x[j + q]);
+        for (; j + 3 < S.K; j += 4) {
+          const VT v0 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j) * ld));
+          const VT v1 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 1) * ld));
+          const VT v2 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 2) * ld));
+          const VT v3 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 3) * ld));
+          axpy16(v0, TACC(x[j]), a0);
+          axpy16(v1, TACC(x[j + 1]), a1);
+          axpy16(v2, TACC(x[j + 2]), a0);
+          axpy16(v3, TACC(x[j + 3]), a1);
         }
-        for (; j < S.K; j++) a[0] += TACC(ldg(A + int64_t(j) * m)) * TACC(x[j]);
+        for (; j < S.K; j++) axpy16(__ldg(reinterpret_cast<const VT*>(A + int64_t(j) * ld)), TACC(x[j]), a0);
       }
     }
-    if (act) yo[i] = TX(((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7])));
+    if (act) {
+#pragma unroll
+      for (int q = 0; q < RPL; q++)
+        if (i + q < m) yo[i + q] = TX(a0[q] + a1[q]);
+    }
   }
 }
 
@@ -151,9 +210,14 @@ __global__ void __launch_bounds__(256) assemble_kernel(PointsDev P, KernelDev K,
   if (w >= ntiles) return;
   const TileDesc T = tiles[w];
   TO* o = out + T.off;
-  const int64_t total = int64_t(T.m) * T.n;
+  const int64_t ld = lead_dim(T.m);
+  const int64_t total = ld * T.n;
   for (int64_t e = lane; e < total; e += 32) {
-    const int i = int(e % T.m), j = int(e / T.m);
+    const int i = int(e % ld), j = int(e / ld);
+    if (i >= T.m) {
+      o[e] = TO(0);
+      continue;
+    }
     double xi[D];
     load_point<D>(P, T.t_begin + i, xi);
     o[e] = TO(kernel_entry<D>(P, K, T.t_begin + i, T.s_begin + j, xi));
@@ -166,28 +230,37 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
                                                       const CompactDesc* __restrict__ blocks, int nblocks) {
   const CompactDesc B = blocks[blockIdx.x];
   TO* u = static_cast<TO*>(B.u_dst);
+  const int64_t ldu = lead_dim(B.m), ldv = lead_dim(B.n);
   if (B.dense) {
-    const int64_t total = int64_t(B.m) * B.n;
+    const int64_t total = ldu * B.n;
     for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
-      const int i = int(e % B.m), j = int(e / B.m);
+      const int i = int(e % ldu), j = int(e / ldu);
+      if (i >= B.m) {
+        u[e] = TO(0);
+        continue;
+      }
       double xi[D];
       load_point<D>(P, B.t_begin + i, xi);
       u[e] = TO(kernel_entry<D>(P, K, B.t_begin + i, B.s_begin + j, xi));
     }
   } else {
     const double* U = ws + B.ws;
+    for (int64_t e = threadIdx.x; e < (ldu - B.m) * B.rank; e += blockDim.x)
+      u[B.m + (e % (ldu - B.m)) + (e / (ldu - B.m)) * ldu] = TO(0);
     const int64_t nu = int64_t(B.m) * B.rank;
     for (int64_t e = threadIdx.x; e < nu; e += blockDim.x) {
       const int i = int(e % B.m), k = int(e / B.m);
-      u[(lmap[B.t_map + i] - B.t_begin) + int64_t(k) * B.m] = TO(U[e]);
+      u[(lmap[B.t_map + i] - B.t_begin) + int64_t(k) * ldu] = TO(U[e]);
     }
     // V follows U's full workspace (m x cap); its first rank columns are contiguous
     const double* Vw = ws + B.ws + int64_t(B.m) * B.cap;
     TO* v = static_cast<TO*>(B.v_dst);
+    for (int64_t e = threadIdx.x; e < (ldv - B.n) * B.rank; e += blockDim.x)
+      v[B.n + (e % (ldv - B.n)) + (e / (ldv - B.n)) * ldv] = TO(0);
     const int64_t nv = int64_t(B.n) * B.rank;
     for (int64_t e = threadIdx.x; e < nv; e += blockDim.x) {
       const int j = int(e % B.n), k = int(e / B.n);
-      v[(lmap[B.s_map + j] - B.s_begin) + int64_t(k) * B.n] = TO(Vw[e]);
+      v[(lmap[B.s_map + j] - B.s_begin) + int64_t(k) * ldv] = TO(Vw[e]);
     }
   }
 }

@@ -28,8 +28,13 @@ struct Panel {
   int32_t slot;       // output slot
 };
 
+// Leading dimension of a stored m-row matrix: matrices with more than 32 rows
+// are read 16 bytes per lane, so their columns are padded (with zeros) to a
+// multiple of 4 rows and start on 16-byte boundaries.
+__host__ __device__ inline int64_t lead_dim(int64_t m) { return m > 32 ? (m + 3) / 4 * 4 : m; }
+
 struct Seg {
-  const void* A;   // m x K column major (element type of the launch)
+  const void* A;   // m x K column major with leading dimension lead_dim(m)
   int64_t in_off;  // offset of the K inputs in the input buffer
   int32_t K;
   int32_t pad;
@@ -41,7 +46,7 @@ struct Item {
 };
 
 struct ZBlock {
-  const void* V;   // n x r column major
+  const void* V;   // n x r column major, leading dimension lead_dim(n)
   int64_t x_off;   // tree position of the source node
   int64_t z_off;   // offset of z_b in the input buffer
   int32_t n, r;
@@ -73,8 +78,8 @@ cudaError_t launch_combine(Prec x, const void* y, int64_t ld_y, int nslots, int6
 cudaError_t launch_gather(const void* src, Prec sp, int64_t ld_src, const int64_t* perm, int64_t n, int nrhs, void* dst,
                           Prec dp, int64_t ld_dst, cudaStream_t st);
 
-// Dense blocks from the kernel: tile t is out + off[t], m x n column major,
-// A(t_begin + i, s_begin + j).
+// Dense blocks from the kernel: tile t is out + off[t], m x n column major with
+// leading dimension lead_dim(m) (padding rows zero), A(t_begin + i, s_begin + j).
 struct TileDesc {
   int64_t t_begin, s_begin;
   int64_t off;  // element offset in the output array
@@ -85,7 +90,8 @@ cudaError_t launch_assemble(int ndim, const PointsDev& P, const KernelDev& K, co
 
 // Far-block compaction after ACA: for each listed block copy U (m x rank) and
 // V (n x rank) out of its ACA workspace (FP64) into u_dst/v_dst in the stored
-// precision, or, for a block kept dense, evaluate its m x n tile into u_dst.
+// precision, or, for a block kept dense, evaluate its m x n tile into u_dst;
+// leading dimensions lead_dim(m), lead_dim(n), padding rows zero.
 struct CompactDesc {
   int64_t t_begin, s_begin;
   int64_t t_map, s_map;  // offsets of the nodes' reference-order maps (low-rank blocks)
