@@ -163,6 +163,13 @@ struct Plan {
   int nzb = 0;
   ZItem* zitems = nullptr;
   int nzitems = 0;
+  ZFix* zfix = nullptr;
+  int nzfix = 0;
+  PanelFix* pfix_far = nullptr;
+  int npfix_far = 0;
+  int64_t nzpart = 0, nypart = 0;  // partial-sum scratch (elements of the vector type)
+  void* zpart = nullptr;
+  void* ypart = nullptr;
 };
 
 }  // namespace
@@ -309,9 +316,9 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
     p.seg_end = int64_t(segs.size());
     const int np = int(panels.size());
     panels.push_back(p);
-    const int rows = 32 * (a == Prec::kD ? 2 : 4);
+    const int rows = rows_per_item(a);
     const int chunks = p.m <= 32 ? 1 : int((p.m + rows - 1) / rows);
-    for (int c = 0; c < chunks; c++) items.push_back({np, c});
+    for (int c = 0; c < chunks; c++) items.push_back({np, c, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
   }
   plan.a_near = a;
   plan.panels_near = upload(op->mem, panels, st, "near panels");
@@ -319,6 +326,9 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
   plan.items_near = upload(op->mem, items, st, "near items");
   plan.nitems_near = int(items.size());
 }
+
+// Columns one far-panel item takes before its panel chunk is split over items.
+constexpr int kPanelCols = 256;
 
 // Far-field plan from the per-block storage pointers.
 void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const std::vector<const void*>& vptr, Prec a,
@@ -328,6 +338,8 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   std::vector<Seg> segs;
   std::vector<Item> items;
   std::vector<ZBlock> zb;
+  std::vector<PanelFix> pfix;
+  int64_t nypart = 0;
   int64_t zoff = op->n;
   size_t b = 0;
   while (b < op->far.size()) {
@@ -370,9 +382,32 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
     if (p.seg_end > p.seg_begin) {
       const int np = int(panels.size());
       panels.push_back(p);
-      const int rows = 32 * (a == Prec::kD ? 2 : 4);
-      const int chunks = p.m <= 32 ? 1 : int((p.m + rows - 1) / rows);
-      for (int c = 0; c < chunks; c++) items.push_back({np, c});
+      if (p.m <= 32) {
+        items.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+      } else {
+        // runs of segments with about kPanelCols columns each bound one item's work
+        std::vector<std::pair<int32_t, int32_t>> groups;
+        int32_t gb = int32_t(p.seg_begin), cols = 0;
+        for (int64_t q = p.seg_begin; q < p.seg_end; q++) {
+          if (cols > 0 && cols + segs[size_t(q)].K > kPanelCols) {
+            groups.push_back({gb, int32_t(q)});
+            gb = int32_t(q);
+            cols = 0;
+          }
+          cols += segs[size_t(q)].K;
+        }
+        groups.push_back({gb, int32_t(p.seg_end)});
+        const int rows = rows_per_item(a);
+        const int chunks = int((p.m + rows - 1) / rows);
+        for (int c = 0; c < chunks; c++) {
+          if (groups.size() == 1) {
+            items.push_back({np, c, groups[0].first, groups[0].second, -1});
+            continue;
+          }
+          pfix.push_back({np, c, int32_t(nypart), int32_t(groups.size())});
+          for (auto& g : groups) items.push_back({np, c, g.first, g.second, int32_t(nypart++)});
+        }
+      }
     }
     b = e;
   }
@@ -383,18 +418,38 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   plan.items_far = upload(op->mem, items, st, "far items");
   plan.nitems_far = int(items.size());
   std::vector<ZItem> zit;
+  std::vector<ZFix> zfix;
+  int64_t nzpart = 0;
   for (size_t q = 0; q < zb.size(); q++) {
-    if (zb[q].n <= 32) {
-      zit.push_back({int32_t(q), 0, zb[q].r});
-    } else {
-      for (int k0 = 0; k0 < zb[q].r; k0 += kZCols)
-        zit.push_back({int32_t(q), k0, std::min(kZCols, zb[q].r - k0)});
+    const int n = zb[q].n, r = zb[q].r;
+    if (n <= 32) {
+      zit.push_back({int32_t(q), 0, r, 0, n, -1});
+      continue;
+    }
+    const int chunks = (n + kZRows - 1) / kZRows;
+    for (int k0 = 0; k0 < r; k0 += kZCols) {
+      const int nk = std::min(kZCols, r - k0);
+      if (chunks == 1) {
+        zit.push_back({int32_t(q), k0, nk, 0, n, -1});
+        continue;
+      }
+      for (int c = 0; c < nk; c++) zfix.push_back({zb[q].z_off + k0 + c, int32_t(nzpart + c), chunks});
+      for (int h = 0; h < chunks; h++) {
+        zit.push_back({int32_t(q), k0, nk, h * kZRows, std::min(n, (h + 1) * kZRows), int32_t(nzpart)});
+        nzpart += kZCols;
+      }
     }
   }
   plan.zb = upload(op->mem, zb, st, "far z blocks");
   plan.nzb = int(zb.size());
   plan.zitems = upload(op->mem, zit, st, "far z items");
   plan.nzitems = int(zit.size());
+  plan.zfix = upload(op->mem, zfix, st, "far z fix-ups");
+  plan.nzfix = int(zfix.size());
+  plan.pfix_far = upload(op->mem, pfix, st, "far panel fix-ups");
+  plan.npfix_far = int(pfix.size());
+  plan.nzpart = nzpart;
+  plan.nypart = nypart * rows_per_item(a);
 }
 
 // ACA of every far block, in workspace-bounded batches; compacted factors go
@@ -676,16 +731,18 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
   Tracer& tr = op->tr;
   if (plan.nzb > 0) tr.start(kb + 0, st);
-  if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.zitems, plan.nzitems, in, ldin, 1, st)) != cudaSuccess) return e;
+  if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.zitems, plan.nzitems, plan.zfix, plan.nzfix, plan.zpart, in, ldin,
+                        1, st)) != cudaSuccess)
+    return e;
   if (plan.nzb > 0) tr.stop(st);
   tr.start(kb + 1, st);
-  if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.items_near, plan.nitems_near, in, ldin,
-                         yslots, n, op->nslots, 1, st)) != cudaSuccess)
+  if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.items_near, plan.nitems_near, nullptr, 0,
+                         nullptr, in, ldin, yslots, n, op->nslots, 1, st)) != cudaSuccess)
     return e;
   tr.stop(st);
   if (plan.nitems_far > 0) tr.start(kb + 2, st);
-  if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.items_far, plan.nitems_far, in, ldin,
-                         yslots, n, op->nslots, 1, st)) != cudaSuccess)
+  if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.items_far, plan.nitems_far, plan.pfix_far,
+                         plan.npfix_far, plan.ypart, in, ldin, yslots, n, op->nslots, 1, st)) != cudaSuccess)
     return e;
   if (plan.nitems_far > 0) tr.stop(st);
   tr.start(kb + 3, st);
@@ -919,7 +976,17 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
       op->plan32.nzb = op->plan64.nzb;
       op->plan32.zitems = op->plan64.zitems;
       op->plan32.nzitems = op->plan64.nzitems;
+      op->plan32.zfix = op->plan64.zfix;
+      op->plan32.nzfix = op->plan64.nzfix;
+      op->plan32.pfix_far = op->plan64.pfix_far;
+      op->plan32.npfix_far = op->plan64.npfix_far;
+      op->plan32.nzpart = op->plan64.nzpart;
+      op->plan32.nypart = op->plan64.nypart;
+      op->plan32.zpart = op->mem.alloc(size_t(std::max<int64_t>(op->plan32.nzpart, 1)) * 4, "z partial sums (FP32)");
+      op->plan32.ypart = op->mem.alloc(size_t(std::max<int64_t>(op->plan32.nypart, 1)) * 4, "row partial sums (FP32)");
     }
+    op->plan64.zpart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nzpart, 1)) * 8, "z partial sums");
+    op->plan64.ypart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nypart, 1)) * 8, "row partial sums");
     // work vectors
     const int64_t ldin = n + op->zlen;
     op->d_in64 = op->mem.alloc_n<double>(size_t(ldin), "matvec input");
@@ -974,11 +1041,12 @@ int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nr
       CK(cudaMemcpyAsync(op->d_in64, op->d_io, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, st));
       if (op->nslots > 1) CK(cudaMemsetAsync(op->d_y64 + n, 0, sizeof(double) * size_t(n) * (op->nslots - 1), st));
       const Plan& pl = op->plan64;
-      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, op->d_in64, ldin, 1, st));
-      CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.items_near, pl.nitems_near, op->d_in64,
-                       ldin, op->d_y64, n, op->nslots, 1, st));
-      CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.items_far, pl.nitems_far, op->d_in64, ldin,
-                       op->d_y64, n, op->nslots, 1, st));
+      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, pl.zfix, pl.nzfix, pl.zpart, op->d_in64, ldin, 1,
+                      st));
+      CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.items_near, pl.nitems_near, nullptr, 0,
+                       nullptr, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
+      CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.items_far, pl.nitems_far, pl.pfix_far,
+                       pl.npfix_far, pl.ypart, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
       CK(launch_combine(Prec::kD, op->d_y64, n, op->nslots, n, 1, op->d_perm, d_y + c * n, Prec::kD, n, st));
     }
     return HODLR_OK;

@@ -51,12 +51,12 @@ __device__ __forceinline__ void axpy16(const double2& a, double s, double* acc) 
 
 // Phase 1: z_b = V_b^T x_s.  A block with n <= 32 is one warp's item: lanes
 // form groups of npad (next power of two >= n) that each take one column.  A
-// larger block is split into items of up to kZCols columns; the warp strides
-// over the n rows with independent accumulators per column, so a 32768-point
-// block is spread over r / kZCols warps instead of one.
+// larger block is split into items of up to kZCols columns by kZRows rows; a
+// block with more rows than that writes one partial sum per item and column
+// and zfix_kernel adds them in order.
 template <typename TA, typename TX, typename TACC>
 __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
-                                                    int nitems, TX* in, int64_t ld_in) {
+                                                    int nitems, TX* __restrict__ zpart, TX* in, int64_t ld_in) {
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= nitems) return;
@@ -79,41 +79,69 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
       if (j == 0 && k < r) z[k] = TX(acc);
     }
   } else {
-    // 16 bytes per lane: RPL consecutive rows of kZCols columns
+    // 16 bytes per lane: RPL consecutive rows of kZCols columns, two row
+    // groups per step so that 2 * kZCols loads are in flight per lane
     constexpr int RPL = 16 / int(sizeof(TA));
     using VT = typename Vec16<TA>::type;
     const int64_t ldv = lead_dim(n);
-    const int k0 = it.k0, nk = it.nk;
+    const int k0 = it.k0, nk = it.nk, j1 = it.j1;
     TACC acc[kZCols];
 #pragma unroll
     for (int c = 0; c < kZCols; c++) acc[c] = TACC(0);
     const TA* v = V + int64_t(k0) * ldv;
-    for (int j = lane * RPL; j < n; j += 32 * RPL) {
-      TACC xv[RPL];
+    for (int j = it.j0 + lane * RPL; j < j1; j += 64 * RPL) {
+      const int j2 = j + 32 * RPL;
+      TACC xa[RPL], xb[RPL];
 #pragma unroll
-      for (int q = 0; q < RPL; q++) xv[q] = (j + q < n) ? TACC(x[j + q]) : TACC(0);
+      for (int q = 0; q < RPL; q++) {
+        xa[q] = (j + q < j1) ? TACC(x[j + q]) : TACC(0);
+        xb[q] = (j2 + q < j1) ? TACC(x[j2 + q]) : TACC(0);
+      }
+      VT va[kZCols], vb[kZCols];
 #pragma unroll
-      for (int c = 0; c < kZCols; c++)
-        if (c < nk) {
-          const VT a = __ldg(reinterpret_cast<const VT*>(v + int64_t(c) * ldv + j));
-          acc[c] += dot16<TACC>(a, xv);
-        }
+      for (int c = 0; c < kZCols; c++) {
+        if (c < nk) va[c] = __ldg(reinterpret_cast<const VT*>(v + int64_t(c) * ldv + j));
+        if (c < nk && j2 < j1) vb[c] = __ldg(reinterpret_cast<const VT*>(v + int64_t(c) * ldv + j2));
+      }
+#pragma unroll
+      for (int c = 0; c < kZCols; c++) {
+        if (c < nk) acc[c] += dot16<TACC>(va[c], xa);
+        if (c < nk && j2 < j1) acc[c] += dot16<TACC>(vb[c], xb);
+      }
     }
 #pragma unroll
     for (int c = 0; c < kZCols; c++) {
       TACC a = acc[c];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if (lane == 0 && c < nk) z[k0 + c] = TX(a);
+      if (lane == 0 && c < nk) {
+        if (it.part < 0)
+          z[k0 + c] = TX(a);
+        else
+          zpart[it.part + c] = TX(a);
+      }
     }
   }
 }
 
-// Phase 2: one warp per (panel, 32-row chunk).
+template <typename TX>
+__global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const TX* __restrict__ zpart, TX* in,
+                            int64_t ld_in) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nfix) return;
+  const ZFix F = fix[f];
+  TX acc = TX(0);
+  for (int q = 0; q < F.count; q++) acc += zpart[F.part + q * kZCols];
+  in[blockIdx.y * ld_in + F.zpos] = acc;
+}
+
+// Phase 2: one warp per item (a row chunk of a panel times a run of its
+// segments).
 template <typename TA, typename TX, typename TACC>
 __global__ void __launch_bounds__(256)
     panel_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
-                 int nitems, const TX* __restrict__ in, int64_t ld_in, TX* __restrict__ y, int64_t ld_y, int nslots) {
+                 int nitems, TX* __restrict__ ypart, const TX* __restrict__ in, int64_t ld_in, TX* __restrict__ y,
+                 int64_t ld_y, int nslots) {
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= nitems) return;
@@ -128,7 +156,7 @@ __global__ void __launch_bounds__(256)
     const int slices = 32 / mpad;
     const int i = lane & (mpad - 1), sl = lane / mpad;
     TACC acc = 0;
-    for (int64_t s = P.seg_begin; s < P.seg_end; s++) {
+    for (int64_t s = it.seg_b; s < it.seg_e; s++) {
       const Seg S = segs[s];
       const TA* A = static_cast<const TA*>(S.A);
       const TX* x = inc + S.in_off;
@@ -155,7 +183,7 @@ __global__ void __launch_bounds__(256)
     TACC a0[RPL], a1[RPL];
 #pragma unroll
     for (int q = 0; q < RPL; q++) a0[q] = a1[q] = TACC(0);
-    for (int64_t s = P.seg_begin; s < P.seg_end; s++) {
+    for (int64_t s = it.seg_b; s < it.seg_e; s++) {
       const Seg S = segs[s];
       const TA* A = static_cast<const TA*>(S.A) + i;
       const TX* x = inc + S.in_off;
@@ -175,11 +203,30 @@ __global__ void __launch_bounds__(256)
       }
     }
     if (act) {
+      TX* dst = it.part < 0 ? yo + i : ypart + int64_t(it.part) * (32 * RPL) + lane * RPL;
 #pragma unroll
       for (int q = 0; q < RPL; q++)
-        if (i + q < m) yo[i + q] = TX(a0[q] + a1[q]);
+        if (i + q < m) dst[q] = TX(a0[q] + a1[q]);
     }
   }
+}
+
+// Adds the partial row blocks of split panel chunks, in part order.
+template <typename TX>
+__global__ void __launch_bounds__(256) panel_fix_kernel(const Panel* __restrict__ panels,
+                                                        const PanelFix* __restrict__ fix, int nfix, int rows,
+                                                        const TX* __restrict__ ypart, TX* __restrict__ y, int64_t ld_y,
+                                                        int nslots) {
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const int f = int(t / rows), q = int(t % rows);
+  if (f >= nfix) return;
+  const PanelFix F = fix[f];
+  const Panel P = panels[F.panel];
+  const int i = F.chunk * rows + q;
+  if (i >= P.m) return;
+  TX acc = TX(0);
+  for (int g = 0; g < F.count; g++) acc += ypart[int64_t(F.part + g) * rows + q];
+  y[(int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin + i] = acc;
 }
 
 template <typename TX, typename TO>
@@ -276,42 +323,68 @@ unsigned vec_grid(int64_t n) {
 
 }  // namespace
 
-cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, void* in, int64_t ld_in,
-                         int nrhs, cudaStream_t st) {
+cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
+                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st) {
   if (nitems <= 0) return cudaSuccess;
-  count_launches(1);
+  count_launches(nfix > 0 ? 2 : 1);
   dim3 g(warps_grid(nitems), unsigned(nrhs));
-  if (a == Prec::kD && x == Prec::kD)
-    zgemv_kernel<double, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(in), ld_in);
-  else if (a == Prec::kF && x == Prec::kD)
-    zgemv_kernel<float, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(in), ld_in);
-  else if (a == Prec::kF && x == Prec::kF)
-    zgemv_kernel<float, float, float><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<float*>(in), ld_in);
-  else
+  dim3 gf(unsigned((nfix + 255) / 256), unsigned(nrhs));
+  if (a == Prec::kD && x == Prec::kD) {
+    zgemv_kernel<double, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(zpart),
+                                                            static_cast<double*>(in), ld_in);
+    if (nfix > 0)
+      zfix_kernel<double><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const double*>(zpart), static_cast<double*>(in),
+                                               ld_in);
+  } else if (a == Prec::kF && x == Prec::kD) {
+    zgemv_kernel<float, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(zpart),
+                                                           static_cast<double*>(in), ld_in);
+    if (nfix > 0)
+      zfix_kernel<double><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const double*>(zpart), static_cast<double*>(in),
+                                               ld_in);
+  } else if (a == Prec::kF && x == Prec::kF) {
+    zgemv_kernel<float, float, float><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<float*>(zpart),
+                                                         static_cast<float*>(in), ld_in);
+    if (nfix > 0)
+      zfix_kernel<float><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const float*>(zpart), static_cast<float*>(in),
+                                              ld_in);
+  } else {
     return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* items, int nitems,
-                          const void* in, int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs,
-                          cudaStream_t st) {
+                          const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y,
+                          int64_t ld_y, int nslots, int nrhs, cudaStream_t st) {
   if (nitems <= 0) return cudaSuccess;
-  count_launches(1);
+  count_launches(nfix > 0 ? 2 : 1);
   dim3 g(warps_grid(nitems), unsigned(nrhs));
-  if (a == Prec::kD && x == Prec::kD)
-    panel_kernel<double, double, double><<<g, 256, 0, st>>>(panels, segs, items, nitems,
+  const int rows = rows_per_item(a);
+  dim3 gf(unsigned((int64_t(nfix) * rows + 255) / 256), unsigned(nrhs));
+  if (a == Prec::kD && x == Prec::kD) {
+    panel_kernel<double, double, double><<<g, 256, 0, st>>>(panels, segs, items, nitems, static_cast<double*>(ypart),
                                                             static_cast<const double*>(in), ld_in,
                                                             static_cast<double*>(y), ld_y, nslots);
-  else if (a == Prec::kF && x == Prec::kD)
-    panel_kernel<float, double, double><<<g, 256, 0, st>>>(panels, segs, items, nitems,
+    if (nfix > 0)
+      panel_fix_kernel<double><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const double*>(ypart),
+                                                    static_cast<double*>(y), ld_y, nslots);
+  } else if (a == Prec::kF && x == Prec::kD) {
+    panel_kernel<float, double, double><<<g, 256, 0, st>>>(panels, segs, items, nitems, static_cast<double*>(ypart),
                                                            static_cast<const double*>(in), ld_in,
                                                            static_cast<double*>(y), ld_y, nslots);
-  else if (a == Prec::kF && x == Prec::kF)
-    panel_kernel<float, float, float><<<g, 256, 0, st>>>(panels, segs, items, nitems,
+    if (nfix > 0)
+      panel_fix_kernel<double><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const double*>(ypart),
+                                                    static_cast<double*>(y), ld_y, nslots);
+  } else if (a == Prec::kF && x == Prec::kF) {
+    panel_kernel<float, float, float><<<g, 256, 0, st>>>(panels, segs, items, nitems, static_cast<float*>(ypart),
                                                          static_cast<const float*>(in), ld_in,
                                                          static_cast<float*>(y), ld_y, nslots);
-  else
+    if (nfix > 0)
+      panel_fix_kernel<float><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const float*>(ypart),
+                                                   static_cast<float*>(y), ld_y, nslots);
+  } else {
     return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

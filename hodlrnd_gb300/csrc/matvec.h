@@ -40,10 +40,27 @@ struct Seg {
   int32_t pad;
 };
 
+// One warp's share of phase 2: rows chunk * kRowsPerItem(prec) ... of the
+// panel (all of them when m <= 32) times segments [seg_b, seg_e).  A panel
+// chunk whose columns are split over several items writes partial sums
+// (part >= 0: rows at ypart[part * rows_per_item]) that a fix-up pass adds
+// in a fixed order; otherwise part < 0 and the item writes its output slot.
 struct Item {
   int32_t panel;
-  int32_t chunk;  // 32-row chunk of the panel (panels with m <= 32 have one item)
+  int32_t chunk;
+  int32_t seg_b, seg_e;
+  int32_t part;
 };
+
+// Sum of `count` partial row blocks (parts part .. part+count-1) into the
+// output slot of rows chunk * rows_per_item .. of the panel.
+struct PanelFix {
+  int32_t panel;
+  int32_t chunk;
+  int32_t part;
+  int32_t count;
+}; 
+
 
 struct ZBlock {
   const void* V;   // n x r column major, leading dimension lead_dim(n)
@@ -56,20 +73,33 @@ struct ZBlock {
 // them for blocks with n <= 32, at most kZCols for larger ones).
 struct ZItem {
   int32_t zb;
-  int32_t k0, nk;
+  int32_t k0, nk;  // columns k0 .. k0 + nk - 1
+  int32_t j0, j1;  // rows j0 .. j1 - 1 (all rows when n <= 32)
+  int32_t part;    // < 0: write z; else partial sums at zpart[part + c]
 };
 constexpr int kZCols = 4;
+constexpr int kZRows = 4096;  // rows per item for blocks with n > 32
+
+// z[zpos] = sum_{q < count} zpart[part + q * kZCols]
+struct ZFix {
+  int64_t zpos;
+  int32_t part;
+  int32_t count;
+};
 
 // Element types: A = stored matrix, X = vectors, ACC = accumulation.
 enum class Prec { kD, kF };  // double, float
 
 // in:   input buffer [x (ld_in rows of x) | z], nrhs columns with leading dimension ld_in
 // y:    output slots, slot s of column c at y + (c * nslots + s) * ld_y
-cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, void* in, int64_t ld_in,
-                         int nrhs, cudaStream_t st);
+// zpart / ypart: scratch of the vector precision (one column of partials).
+cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
+                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st);
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* items, int nitems,
-                          const void* in, int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs,
-                          cudaStream_t st);
+                          const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y,
+                          int64_t ld_y, int nslots, int nrhs, cudaStream_t st);
+// rows handled by one big-panel item for stored element size `a`
+inline int rows_per_item(Prec a) { return a == Prec::kD ? 64 : 128; }
 // out[perm[i] + c*ld_out] (or out[i + c*ld_out] when perm == NULL) =
 //   sum_s y[(c*nslots + s)*ld_y + i], i < n
 cudaError_t launch_combine(Prec x, const void* y, int64_t ld_y, int nslots, int64_t n, int nrhs, const int64_t* perm,
