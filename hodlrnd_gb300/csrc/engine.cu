@@ -269,7 +269,7 @@ struct NearTiles {
   int64_t total = 0;
 };
 
-NearTiles near_tiles(const Tree& t, const NearList& nl) {
+NearTiles near_tiles(const Tree& t, const NearList& nl, int esz) {
   NearTiles out;
   const int L = t.levels - 1;
   for (int64_t k = 0; k + 1 < int64_t(nl.leaf_ptr.size()); k++)
@@ -282,7 +282,7 @@ NearTiles near_tiles(const Tree& t, const NearList& nl) {
       d.m = int32_t(t.count[size_t(gt)]);
       d.n = int32_t(t.count[size_t(gs)]);
       d.off = out.total;
-      out.total += (lead_dim(d.m) * d.n + 3) / 4 * 4;
+      out.total += (stored_elems(d.m, d.n, esz) + 3) / 4 * 4;
       out.tiles.push_back(d);
     }
   return out;
@@ -420,22 +420,24 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   std::vector<ZItem> zit;
   std::vector<ZFix> zfix;
   int64_t nzpart = 0;
+  const int T = int(tile_rows(a == Prec::kD ? 8 : 4));
   for (size_t q = 0; q < zb.size(); q++) {
     const int n = zb[q].n, r = zb[q].r;
     if (n <= 32) {
-      zit.push_back({int32_t(q), 0, r, 0, n, -1});
+      zit.push_back({int32_t(q), 0, r, 0, 0, -1});
       continue;
     }
-    const int chunks = (n + kZRows - 1) / kZRows;
+    const int ntiles = (n + T - 1) / T;
+    const int groups = (ntiles + kZTiles - 1) / kZTiles;
     for (int k0 = 0; k0 < r; k0 += kZCols) {
       const int nk = std::min(kZCols, r - k0);
-      if (chunks == 1) {
-        zit.push_back({int32_t(q), k0, nk, 0, n, -1});
+      if (groups == 1) {
+        zit.push_back({int32_t(q), k0, nk, 0, ntiles, -1});
         continue;
       }
-      for (int c = 0; c < nk; c++) zfix.push_back({zb[q].z_off + k0 + c, int32_t(nzpart + c), chunks});
-      for (int h = 0; h < chunks; h++) {
-        zit.push_back({int32_t(q), k0, nk, h * kZRows, std::min(n, (h + 1) * kZRows), int32_t(nzpart)});
+      for (int c = 0; c < nk; c++) zfix.push_back({zb[q].z_off + k0 + c, int32_t(nzpart + c), groups});
+      for (int g = 0; g < groups; g++) {
+        zit.push_back({int32_t(q), k0, nk, g * kZTiles, std::min(ntiles, (g + 1) * kZTiles), int32_t(nzpart)});
         nzpart += kZCols;
       }
     }
@@ -606,13 +608,14 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
       op->rank[b] = out[q].rank;
       op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
       off[q] = bytes;
-      const uint64_t r = uint64_t(op->rank[b]);
-      const uint64_t ub = (uint64_t(lead_dim(mm[b])) * (op->dense[b] ? uint64_t(nn[b]) : r) * esz + 15) / 16 * 16;
-      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(lead_dim(nn[b])) * r * esz + 15) / 16 * 16;
+      const int64_t r = op->rank[b];
+      const uint64_t ub = (uint64_t(stored_elems(mm[b], op->dense[b] ? nn[b] : r, int(esz))) * esz + 15) / 16 * 16;
+      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(stored_elems(nn[b], r, int(esz))) * esz + 15) / 16 * 16;
       bytes += ub + vb;
     }
     if (bytes > 0) {
       char* chunk = static_cast<char*>(op->mem.alloc(bytes, "far-field factors"));
+      CK(cudaMemsetAsync(chunk, 0, bytes, st));  // tile padding rows must read as zero
       for (size_t q = 0; q < batch.size(); q++) {
         const size_t b = batch[q];
         if (out[q].flags & kAcaOverflow) continue;
@@ -623,7 +626,8 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
         c.s_map = desc[q].s_map;
         c.ws = desc[q].ws;
         c.u_dst = chunk + off[q];
-        c.v_dst = chunk + off[q] + (uint64_t(lead_dim(mm[b])) * uint64_t(std::max(op->rank[b], 0)) * esz + 15) / 16 * 16;
+        c.v_dst = chunk + off[q] +
+                  (uint64_t(stored_elems(mm[b], std::max(op->rank[b], 0), int(esz))) * esz + 15) / 16 * 16;
         c.m = mm[b];
         c.n = nn[b];
         c.rank = op->rank[b];
@@ -940,16 +944,23 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
     op->d_perm = upload(op->mem, op->tree.perm, st, "permutation");
     op->d_lmap = upload(op->mem, reference_order_map(op->tree), st, "reference-order map");
     // near field
-    const NearTiles nt = near_tiles(op->tree, op->near);
+    const NearTiles nt = near_tiles(op->tree, op->near, 8);
     PointsDev P{op->d_pts, n};
     KernelDev K{kernel->kind, kernel->scale, kernel->diag};
     TileDesc* d_tiles = upload(op->mem, nt.tiles, st, "near tile descriptors");
     double* near64 = op->mem.alloc_n<double>(size_t(std::max<int64_t>(nt.total, 1)), "near field (FP64)");
+    CK(cudaMemsetAsync(near64, 0, sizeof(double) * size_t(std::max<int64_t>(nt.total, 1)), st));
     CK(launch_assemble(d, P, K, d_tiles, int(nt.tiles.size()), near64, Prec::kD, st));
     float* near32 = nullptr;
+    NearTiles nt32;
     if (op->p.precision == HODLR_PREC_MIXED) {
-      near32 = op->mem.alloc_n<float>(size_t(std::max<int64_t>(nt.total, 1)), "near field (FP32)");
-      CK(launch_assemble(d, P, K, d_tiles, int(nt.tiles.size()), near32, Prec::kF, st));
+      nt32 = near_tiles(op->tree, op->near, 4);
+      TileDesc* d_tiles32 = upload(op->mem, nt32.tiles, st, "near tile descriptors");
+      near32 = op->mem.alloc_n<float>(size_t(std::max<int64_t>(nt32.total, 1)), "near field (FP32)");
+      CK(cudaMemsetAsync(near32, 0, sizeof(float) * size_t(std::max<int64_t>(nt32.total, 1)), st));
+      CK(launch_assemble(d, P, K, d_tiles32, int(nt32.tiles.size()), near32, Prec::kF, st));
+      CK(cudaStreamSynchronize(st));
+      op->mem.release(d_tiles32);
     }
     CK(cudaStreamSynchronize(st));
     op->mem.release(d_tiles);
@@ -966,7 +977,7 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
     build_near_plan(op.get(), nt, near64, Prec::kD, op->plan64, st);
     build_far_plan(op.get(), uptr, vptr, fp, op->plan64, st);
     if (op->p.precision == HODLR_PREC_MIXED) {
-      build_near_plan(op.get(), nt, near32, Prec::kF, op->plan32, st);
+      build_near_plan(op.get(), nt32, near32, Prec::kF, op->plan32, st);
       op->plan32.a_far = Prec::kF;
       op->plan32.panels_far = op->plan64.panels_far;
       op->plan32.segs_far = op->plan64.segs_far;
@@ -1189,20 +1200,22 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
     if (rank) *rank = op->rank[size_t(b)];
     if (dense) *dense = op->dense[size_t(b)];
     const bool f32 = op->p.precision == HODLR_PREC_MIXED;
-    // copy rows x cols (stored with leading dimension lead_dim(rows)) to a dense column-major dst
+    // copy a stored rows x cols matrix (tiled layout, matvec.h) to a dense column-major dst
     auto fetch = [&](const void* src, size_t rows, size_t cols, double* dst) {
       if (!dst || !src || rows * cols == 0) return;
-      const size_t ld = size_t(lead_dim(int64_t(rows)));
-      std::vector<double> tmp(ld * cols);
+      const int esz = f32 ? 4 : 8;
+      const size_t total = size_t(stored_elems(int64_t(rows), int64_t(cols), esz));
+      std::vector<double> tmp(total);
       if (f32) {
-        std::vector<float> t32(ld * cols);
-        CK(cudaMemcpy(t32.data(), src, t32.size() * 4, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < t32.size(); i++) tmp[i] = double(t32[i]);
+        std::vector<float> t32(total);
+        CK(cudaMemcpy(t32.data(), src, total * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < total; i++) tmp[i] = double(t32[i]);
       } else {
-        CK(cudaMemcpy(tmp.data(), src, tmp.size() * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(tmp.data(), src, total * 8, cudaMemcpyDeviceToHost));
       }
       for (size_t c = 0; c < cols; c++)
-        for (size_t r = 0; r < rows; r++) dst[c * rows + r] = tmp[c * ld + r];
+        for (size_t r = 0; r < rows; r++)
+          dst[c * rows + r] = tmp[size_t(elem_offset(int64_t(r), int64_t(c), int64_t(rows), int64_t(cols), esz))];
     };
     CK(cudaSetDevice(op->p.device));
     CK(cudaStreamSynchronize(op->ctx->stream));

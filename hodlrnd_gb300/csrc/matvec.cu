@@ -51,9 +51,9 @@ __device__ __forceinline__ void axpy16(const double2& a, double s, double* acc) 
 
 // Phase 1: z_b = V_b^T x_s.  A block with n <= 32 is one warp's item: lanes
 // form groups of npad (next power of two >= n) that each take one column.  A
-// larger block is split into items of up to kZCols columns by kZRows rows; a
-// block with more rows than that writes one partial sum per item and column
-// and zfix_kernel adds them in order.
+// larger block is split into items of up to kZCols columns by kZTiles row
+// tiles; a block with more tiles than that writes one partial sum per item and
+// column, and zfix_kernel adds them in order.
 template <typename TA, typename TX, typename TACC>
 __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
                                                     int nitems, TX* __restrict__ zpart, TX* in, int64_t ld_in) {
@@ -79,47 +79,48 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
       if (j == 0 && k < r) z[k] = TX(acc);
     }
   } else {
-    // 16 bytes per lane: RPL consecutive rows of kZCols columns, two row
-    // groups per step so that 2 * kZCols loads are in flight per lane
+    // One tile at a time: each lane holds RPL rows of x; every column of the
+    // tile is a 16-byte load per lane (the warp streams the tile), reduced
+    // across the warp; lane c keeps the running sum of column k0 + c.
     constexpr int RPL = 16 / int(sizeof(TA));
+    constexpr int T = 32 * RPL;
     using VT = typename Vec16<TA>::type;
-    const int64_t ldv = lead_dim(n);
-    const int k0 = it.k0, nk = it.nk, j1 = it.j1;
-    TACC acc[kZCols];
+    const int k0 = it.k0, nk = it.nk;
+    TACC run = TACC(0);
+    for (int t = it.t0; t < it.t1; t++) {
+      const int rows = min(T, n - t * T);
+      const int64_t h = tile_height(n, t, int(sizeof(TA)));
+      const TA* tile = V + int64_t(t) * T * r + int64_t(k0) * h + lane * RPL;
+      TACC xv[RPL];
 #pragma unroll
-    for (int c = 0; c < kZCols; c++) acc[c] = TACC(0);
-    const TA* v = V + int64_t(k0) * ldv;
-    for (int j = it.j0 + lane * RPL; j < j1; j += 64 * RPL) {
-      const int j2 = j + 32 * RPL;
-      TACC xa[RPL], xb[RPL];
+      for (int q = 0; q < RPL; q++) xv[q] = (lane * RPL + q < rows) ? TACC(x[t * T + lane * RPL + q]) : TACC(0);
+      const bool act = lane * RPL < rows;
+      int c = 0;
+      for (; c + 7 < nk; c += 8) {
+        TACC sc[8];
 #pragma unroll
-      for (int q = 0; q < RPL; q++) {
-        xa[q] = (j + q < j1) ? TACC(x[j + q]) : TACC(0);
-        xb[q] = (j2 + q < j1) ? TACC(x[j2 + q]) : TACC(0);
+        for (int u = 0; u < 8; u++)
+          sc[u] = act ? dot16<TACC>(__ldg(reinterpret_cast<const VT*>(tile + int64_t(c + u) * h)), xv) : TACC(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+          for (int u = 0; u < 8; u++) sc[u] += __shfl_xor_sync(0xffffffffu, sc[u], o);
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          if (lane == c + u) run += sc[u];
       }
-      VT va[kZCols], vb[kZCols];
+      for (; c < nk; c++) {
+        TACC sc = act ? dot16<TACC>(__ldg(reinterpret_cast<const VT*>(tile + int64_t(c) * h)), xv) : TACC(0);
 #pragma unroll
-      for (int c = 0; c < kZCols; c++) {
-        if (c < nk) va[c] = __ldg(reinterpret_cast<const VT*>(v + int64_t(c) * ldv + j));
-        if (c < nk && j2 < j1) vb[c] = __ldg(reinterpret_cast<const VT*>(v + int64_t(c) * ldv + j2));
-      }
-#pragma unroll
-      for (int c = 0; c < kZCols; c++) {
-        if (c < nk) acc[c] += dot16<TACC>(va[c], xa);
-        if (c < nk && j2 < j1) acc[c] += dot16<TACC>(vb[c], xb);
+        for (int o = 16; o > 0; o >>= 1) sc += __shfl_xor_sync(0xffffffffu, sc, o);
+        if (lane == c) run += sc;
       }
     }
-#pragma unroll
-    for (int c = 0; c < kZCols; c++) {
-      TACC a = acc[c];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-      if (lane == 0 && c < nk) {
-        if (it.part < 0)
-          z[k0 + c] = TX(a);
-        else
-          zpart[it.part + c] = TX(a);
-      }
+    if (lane < nk) {
+      if (it.part < 0)
+        z[k0 + lane] = TX(run);
+      else
+        zpart[it.part + lane] = TX(run);
     }
   }
 }
@@ -174,36 +175,40 @@ __global__ void __launch_bounds__(256)
     for (int o = mpad; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (sl == 0 && i < m) yo[i] = TX(acc);
   } else {
-    // 16 bytes per lane: rows [i, i + RPL) of each column
+    // Item chunk = row tile t: every segment's tile is streamed column by
+    // column, 16 bytes per lane (rows t*T + lane*RPL ..).
     constexpr int RPL = 16 / int(sizeof(TA));
+    constexpr int T = 32 * RPL;
     using VT = typename Vec16<TA>::type;
-    const int64_t ld = lead_dim(m);
-    const int i = it.chunk * 32 * RPL + lane * RPL;
-    const bool act = i < m;
+    const int t = it.chunk;
+    const int rows = min(T, m - t * T);
+    const int64_t h = tile_height(m, t, int(sizeof(TA)));
+    const bool act = lane * RPL < rows;
     TACC a0[RPL], a1[RPL];
 #pragma unroll
     for (int q = 0; q < RPL; q++) a0[q] = a1[q] = TACC(0);
     for (int64_t s = it.seg_b; s < it.seg_e; s++) {
       const Seg S = segs[s];
-      const TA* A = static_cast<const TA*>(S.A) + i;
+      const TA* A = static_cast<const TA*>(S.A) + int64_t(t) * T * S.K + lane * RPL;
       const TX* x = inc + S.in_off;
       if (act) {
         int j = 0;
         for (; j + 3 < S.K; j += 4) {
-          const VT v0 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j) * ld));
-          const VT v1 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 1) * ld));
-          const VT v2 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 2) * ld));
-          const VT v3 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 3) * ld));
+          const VT v0 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j) * h));
+          const VT v1 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 1) * h));
+          const VT v2 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 2) * h));
+          const VT v3 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 3) * h));
           axpy16(v0, TACC(x[j]), a0);
           axpy16(v1, TACC(x[j + 1]), a1);
           axpy16(v2, TACC(x[j + 2]), a0);
           axpy16(v3, TACC(x[j + 3]), a1);
         }
-        for (; j < S.K; j++) axpy16(__ldg(reinterpret_cast<const VT*>(A + int64_t(j) * ld)), TACC(x[j]), a0);
+        for (; j < S.K; j++) axpy16(__ldg(reinterpret_cast<const VT*>(A + int64_t(j) * h)), TACC(x[j]), a0);
       }
     }
     if (act) {
-      TX* dst = it.part < 0 ? yo + i : ypart + int64_t(it.part) * (32 * RPL) + lane * RPL;
+      const int i = t * T + lane * RPL;
+      TX* dst = it.part < 0 ? yo + i : ypart + int64_t(it.part) * T + lane * RPL;
 #pragma unroll
       for (int q = 0; q < RPL; q++)
         if (i + q < m) dst[q] = TX(a0[q] + a1[q]);
@@ -257,17 +262,12 @@ __global__ void __launch_bounds__(256) assemble_kernel(PointsDev P, KernelDev K,
   if (w >= ntiles) return;
   const TileDesc T = tiles[w];
   TO* o = out + T.off;
-  const int64_t ld = lead_dim(T.m);
-  const int64_t total = ld * T.n;
+  const int64_t total = int64_t(T.m) * T.n;
   for (int64_t e = lane; e < total; e += 32) {
-    const int i = int(e % ld), j = int(e / ld);
-    if (i >= T.m) {
-      o[e] = TO(0);
-      continue;
-    }
+    const int i = int(e % T.m), j = int(e / T.m);
     double xi[D];
     load_point<D>(P, T.t_begin + i, xi);
-    o[e] = TO(kernel_entry<D>(P, K, T.t_begin + i, T.s_begin + j, xi));
+    o[elem_offset(i, j, T.m, T.n, int(sizeof(TO)))] = TO(kernel_entry<D>(P, K, T.t_begin + i, T.s_begin + j, xi));
   }
 }
 
@@ -277,37 +277,29 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
                                                       const CompactDesc* __restrict__ blocks, int nblocks) {
   const CompactDesc B = blocks[blockIdx.x];
   TO* u = static_cast<TO*>(B.u_dst);
-  const int64_t ldu = lead_dim(B.m), ldv = lead_dim(B.n);
+  constexpr int esz = int(sizeof(TO));
   if (B.dense) {
-    const int64_t total = ldu * B.n;
+    const int64_t total = int64_t(B.m) * B.n;
     for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
-      const int i = int(e % ldu), j = int(e / ldu);
-      if (i >= B.m) {
-        u[e] = TO(0);
-        continue;
-      }
+      const int i = int(e % B.m), j = int(e / B.m);
       double xi[D];
       load_point<D>(P, B.t_begin + i, xi);
-      u[e] = TO(kernel_entry<D>(P, K, B.t_begin + i, B.s_begin + j, xi));
+      u[elem_offset(i, j, B.m, B.n, esz)] = TO(kernel_entry<D>(P, K, B.t_begin + i, B.s_begin + j, xi));
     }
   } else {
     const double* U = ws + B.ws;
-    for (int64_t e = threadIdx.x; e < (ldu - B.m) * B.rank; e += blockDim.x)
-      u[B.m + (e % (ldu - B.m)) + (e / (ldu - B.m)) * ldu] = TO(0);
     const int64_t nu = int64_t(B.m) * B.rank;
     for (int64_t e = threadIdx.x; e < nu; e += blockDim.x) {
       const int i = int(e % B.m), k = int(e / B.m);
-      u[(lmap[B.t_map + i] - B.t_begin) + int64_t(k) * ldu] = TO(U[e]);
+      u[elem_offset(lmap[B.t_map + i] - B.t_begin, k, B.m, B.rank, esz)] = TO(U[e]);
     }
     // V follows U's full workspace (m x cap); its first rank columns are contiguous
     const double* Vw = ws + B.ws + int64_t(B.m) * B.cap;
     TO* v = static_cast<TO*>(B.v_dst);
-    for (int64_t e = threadIdx.x; e < (ldv - B.n) * B.rank; e += blockDim.x)
-      v[B.n + (e % (ldv - B.n)) + (e / (ldv - B.n)) * ldv] = TO(0);
     const int64_t nv = int64_t(B.n) * B.rank;
     for (int64_t e = threadIdx.x; e < nv; e += blockDim.x) {
       const int j = int(e % B.n), k = int(e / B.n);
-      v[(lmap[B.s_map + j] - B.s_begin) + int64_t(k) * ldv] = TO(Vw[e]);
+      v[elem_offset(lmap[B.s_map + j] - B.s_begin, k, B.n, B.rank, esz)] = TO(Vw[e]);
     }
   }
 }

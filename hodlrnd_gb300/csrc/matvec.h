@@ -28,13 +28,32 @@ struct Panel {
   int32_t slot;       // output slot
 };
 
-// Leading dimension of a stored m-row matrix: matrices with more than 32 rows
-// are read 16 bytes per lane, so their columns are padded (with zeros) to a
-// multiple of 4 rows and start on 16-byte boundaries.
-__host__ __device__ inline int64_t lead_dim(int64_t m) { return m > 32 ? (m + 3) / 4 * 4 : m; }
+// Storage of an m x K matrix (near tiles, dense far blocks, factors U and V).
+// With m <= 32 it is plain column major.  Larger matrices are read 16 bytes
+// per lane, 32 lanes per warp, so they are cut into row tiles of
+// tile_rows(esz) = 512 / esz rows (128 FP32, 64 FP64), each tile stored
+// column major on its own with its height rounded up to 4 rows (zero padding):
+// a warp working on one tile then streams one contiguous region.
+__host__ __device__ inline int64_t tile_rows(int esz) { return 512 / esz; }
+__host__ __device__ inline int64_t tile_height(int64_t m, int64_t t, int esz) {
+  const int64_t T = tile_rows(esz);
+  int64_t rows = m - t * T;
+  if (rows > T) rows = T;
+  return (rows + 3) / 4 * 4;
+}
+__host__ __device__ inline int64_t stored_elems(int64_t m, int64_t K, int esz) {
+  if (m <= 32) return m * K;
+  const int64_t T = tile_rows(esz), full = m / T, rem = m - full * T;
+  return (full * T + (rem + 3) / 4 * 4) * K;
+}
+__host__ __device__ inline int64_t elem_offset(int64_t i, int64_t k, int64_t m, int64_t K, int esz) {
+  if (m <= 32) return k * m + i;
+  const int64_t T = tile_rows(esz), t = i / T;
+  return t * T * K + k * tile_height(m, t, esz) + (i - t * T);
+}
 
 struct Seg {
-  const void* A;   // m x K column major with leading dimension lead_dim(m)
+  const void* A;   // m x K, stored as above
   int64_t in_off;  // offset of the K inputs in the input buffer
   int32_t K;
   int32_t pad;
@@ -63,7 +82,7 @@ struct PanelFix {
 
 
 struct ZBlock {
-  const void* V;   // n x r column major, leading dimension lead_dim(n)
+  const void* V;   // n x r, stored as above
   int64_t x_off;   // tree position of the source node
   int64_t z_off;   // offset of z_b in the input buffer
   int32_t n, r;
@@ -73,12 +92,12 @@ struct ZBlock {
 // them for blocks with n <= 32, at most kZCols for larger ones).
 struct ZItem {
   int32_t zb;
-  int32_t k0, nk;  // columns k0 .. k0 + nk - 1
-  int32_t j0, j1;  // rows j0 .. j1 - 1 (all rows when n <= 32)
+  int32_t k0, nk;  // columns k0 .. k0 + nk - 1 (nk <= kZCols)
+  int32_t t0, t1;  // row tiles t0 .. t1 - 1 (blocks with n > 32)
   int32_t part;    // < 0: write z; else partial sums at zpart[part + c]
 };
-constexpr int kZCols = 4;
-constexpr int kZRows = 4096;  // rows per item for blocks with n > 32
+constexpr int kZCols = 32;  // columns per item (one running sum per lane)
+constexpr int kZTiles = 8;  // row tiles per item
 
 // z[zpos] = sum_{q < count} zpart[part + q * kZCols]
 struct ZFix {
@@ -108,8 +127,8 @@ cudaError_t launch_combine(Prec x, const void* y, int64_t ld_y, int nslots, int6
 cudaError_t launch_gather(const void* src, Prec sp, int64_t ld_src, const int64_t* perm, int64_t n, int nrhs, void* dst,
                           Prec dp, int64_t ld_dst, cudaStream_t st);
 
-// Dense blocks from the kernel: tile t is out + off[t], m x n column major with
-// leading dimension lead_dim(m) (padding rows zero), A(t_begin + i, s_begin + j).
+// Dense blocks from the kernel: tile t is out + off[t], m x n stored as above
+// (the caller zeroes the padding), A(t_begin + i, s_begin + j).
 struct TileDesc {
   int64_t t_begin, s_begin;
   int64_t off;  // element offset in the output array
@@ -120,8 +139,8 @@ cudaError_t launch_assemble(int ndim, const PointsDev& P, const KernelDev& K, co
 
 // Far-block compaction after ACA: for each listed block copy U (m x rank) and
 // V (n x rank) out of its ACA workspace (FP64) into u_dst/v_dst in the stored
-// precision, or, for a block kept dense, evaluate its m x n tile into u_dst;
-// leading dimensions lead_dim(m), lead_dim(n), padding rows zero.
+// precision and layout, or, for a block kept dense, evaluate its m x n block
+// into u_dst (the caller zeroes the padding).
 struct CompactDesc {
   int64_t t_begin, s_begin;
   int64_t t_map, s_map;  // offsets of the nodes' reference-order maps (low-rank blocks)
