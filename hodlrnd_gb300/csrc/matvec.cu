@@ -79,48 +79,45 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
       if (j == 0 && k < r) z[k] = TX(acc);
     }
   } else {
-    // One tile at a time: each lane holds RPL rows of x; every column of the
-    // tile is a 16-byte load per lane (the warp streams the tile), reduced
-    // across the warp; lane c keeps the running sum of column k0 + c.
+    // One tile at a time: each lane holds RPL rows of x and a running partial
+    // sum per column (kZCols registers), so the up-to-32 column loads of a
+    // tile are independent; one reduce-scatter across the warp at the end
+    // leaves column k0 + c's sum in lane c.
     constexpr int RPL = 16 / int(sizeof(TA));
     constexpr int T = 32 * RPL;
     using VT = typename Vec16<TA>::type;
     const int k0 = it.k0, nk = it.nk;
-    TACC run = TACC(0);
+    TACC acc[kZCols];
+#pragma unroll
+    for (int c = 0; c < kZCols; c++) acc[c] = TACC(0);
     for (int t = it.t0; t < it.t1; t++) {
       const int rows = min(T, n - t * T);
+      if (lane * RPL >= rows) continue;
       const int64_t h = tile_height(n, t, int(sizeof(TA)));
       const TA* tile = V + int64_t(t) * T * r + int64_t(k0) * h + lane * RPL;
       TACC xv[RPL];
 #pragma unroll
       for (int q = 0; q < RPL; q++) xv[q] = (lane * RPL + q < rows) ? TACC(x[t * T + lane * RPL + q]) : TACC(0);
-      const bool act = lane * RPL < rows;
-      int c = 0;
-      for (; c + 7 < nk; c += 8) {
-        TACC sc[8];
 #pragma unroll
-        for (int u = 0; u < 8; u++)
-          sc[u] = act ? dot16<TACC>(__ldg(reinterpret_cast<const VT*>(tile + int64_t(c + u) * h)), xv) : TACC(0);
+      for (int c = 0; c < kZCols; c++)
+        if (c < nk) acc[c] += dot16<TACC>(__ldg(reinterpret_cast<const VT*>(tile + int64_t(c) * h)), xv);
+    }
+    // reduce-scatter: after the round with offset o each lane keeps o sums
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
+    for (int o = kZCols / 2; o >= 1; o >>= 1) {
+      const bool upper = (lane & o) != 0;
 #pragma unroll
-          for (int u = 0; u < 8; u++) sc[u] += __shfl_xor_sync(0xffffffffu, sc[u], o);
-#pragma unroll
-        for (int u = 0; u < 8; u++)
-          if (lane == c + u) run += sc[u];
-      }
-      for (; c < nk; c++) {
-        TACC sc = act ? dot16<TACC>(__ldg(reinterpret_cast<const VT*>(tile + int64_t(c) * h)), xv) : TACC(0);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) sc += __shfl_xor_sync(0xffffffffu, sc, o);
-        if (lane == c) run += sc;
+      for (int i = 0; i < o; i++) {
+        const TACC send = upper ? acc[i] : acc[i + o];
+        const TACC keep = upper ? acc[i + o] : acc[i];
+        acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
       }
     }
     if (lane < nk) {
       if (it.part < 0)
-        z[k0 + lane] = TX(run);
+        z[k0 + lane] = TX(acc[0]);
       else
-        zpart[it.part + lane] = TX(run);
+        zpart[it.part + lane] = TX(acc[0]);
     }
   }
 }
@@ -175,8 +172,10 @@ __global__ void __launch_bounds__(256)
     for (int o = mpad; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     if (sl == 0 && i < m) yo[i] = TX(acc);
   } else {
-    // Item chunk = row tile t: every segment's tile is streamed column by
-    // column, 16 bytes per lane (rows t*T + lane*RPL ..).
+    // Item chunk = row tile t.  Segment descriptors and input values are
+    // fetched 32 at a time with one coalesced load and broadcast by shuffle,
+    // so the loads of the matrix columns (16 bytes per lane) have no
+    // dependent global load in front of them.
     constexpr int RPL = 16 / int(sizeof(TA));
     constexpr int T = 32 * RPL;
     using VT = typename Vec16<TA>::type;
@@ -187,23 +186,37 @@ __global__ void __launch_bounds__(256)
     TACC a0[RPL], a1[RPL];
 #pragma unroll
     for (int q = 0; q < RPL; q++) a0[q] = a1[q] = TACC(0);
-    for (int64_t s = it.seg_b; s < it.seg_e; s++) {
-      const Seg S = segs[s];
-      const TA* A = static_cast<const TA*>(S.A) + int64_t(t) * T * S.K + lane * RPL;
-      const TX* x = inc + S.in_off;
-      if (act) {
-        int j = 0;
-        for (; j + 3 < S.K; j += 4) {
-          const VT v0 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j) * h));
-          const VT v1 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 1) * h));
-          const VT v2 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 2) * h));
-          const VT v3 = __ldg(reinterpret_cast<const VT*>(A + int64_t(j + 3) * h));
-          axpy16(v0, TACC(x[j]), a0);
-          axpy16(v1, TACC(x[j + 1]), a1);
-          axpy16(v2, TACC(x[j + 2]), a0);
-          axpy16(v3, TACC(x[j + 3]), a1);
+    for (int sb = it.seg_b; sb < it.seg_e; sb += 32) {
+      const int ns = min(32, it.seg_e - sb);
+      Seg mine{};
+      if (lane < ns) mine = segs[sb + lane];
+      for (int u = 0; u < ns; u++) {
+        const unsigned long long ap =
+            __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(mine.A), u);
+        const long long in_off = __shfl_sync(0xffffffffu, static_cast<long long>(mine.in_off), u);
+        const int K = __shfl_sync(0xffffffffu, mine.K, u);
+        const TA* A = reinterpret_cast<const TA*>(ap) + int64_t(t) * T * K + lane * RPL;
+        const TX* x = inc + in_off;
+        for (int j0 = 0; j0 < K; j0 += 32) {
+          const int jn = min(32, K - j0);
+          const TACC xl = lane < jn ? TACC(x[j0 + lane]) : TACC(0);
+          int jj = 0;
+          for (; jj + 7 < jn; jj += 8) {
+            VT v[8];
+#pragma unroll
+            for (int w2 = 0; w2 < 8; w2++)
+              v[w2] = act ? __ldg(reinterpret_cast<const VT*>(A + int64_t(j0 + jj + w2) * h)) : VT{};
+#pragma unroll
+            for (int w2 = 0; w2 < 8; w2 += 2) {
+              axpy16(v[w2], __shfl_sync(0xffffffffu, xl, jj + w2), a0);
+              axpy16(v[w2 + 1], __shfl_sync(0xffffffffu, xl, jj + w2 + 1), a1);
+            }
+          }
+          for (; jj < jn; jj++) {
+            const VT v = act ? __ldg(reinterpret_cast<const VT*>(A + int64_t(j0 + jj) * h)) : VT{};
+            axpy16(v, __shfl_sync(0xffffffffu, xl, jj), a0);
+          }
         }
-        for (; j < S.K; j++) axpy16(__ldg(reinterpret_cast<const VT*>(A + int64_t(j) * h)), TACC(x[j]), a0);
       }
     }
     if (act) {
