@@ -153,12 +153,14 @@ struct Plan {
   Prec a_near = Prec::kD, a_far = Prec::kD;
   Panel* panels_near = nullptr;
   Seg* segs_near = nullptr;
-  Item* items_near = nullptr;
-  int nitems_near = 0;
+  Item* small_near = nullptr;  // items of panels with at most 32 rows
+  Item* big_near = nullptr;    // items of larger panels (row tiles)
+  int nsmall_near = 0, nbig_near = 0;
   Panel* panels_far = nullptr;
   Seg* segs_far = nullptr;
-  Item* items_far = nullptr;
-  int nitems_far = 0;
+  Item* small_far = nullptr;
+  Item* big_far = nullptr;
+  int nsmall_far = 0, nbig_far = 0;
   ZBlock* zb = nullptr;
   int nzb = 0;
   ZItem* zitems = nullptr;
@@ -293,7 +295,7 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
   const int L = t.levels - 1;
   std::vector<Panel> panels;
   std::vector<Seg> segs;
-  std::vector<Item> items;
+  std::vector<Item> small, big;
   const size_t esz = a == Prec::kD ? 8 : 4;
   size_t q = 0;
   for (int64_t k = 0; k + 1 < int64_t(op->near.leaf_ptr.size()); k++) {
@@ -316,15 +318,21 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
     p.seg_end = int64_t(segs.size());
     const int np = int(panels.size());
     panels.push_back(p);
-    const int rows = rows_per_item(a);
-    const int chunks = p.m <= 32 ? 1 : int((p.m + rows - 1) / rows);
-    for (int c = 0; c < chunks; c++) items.push_back({np, c, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+    if (p.m <= 32) {
+      small.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+    } else {
+      const int rows = rows_per_item(a);
+      for (int c = 0; c < int((p.m + rows - 1) / rows); c++)
+        big.push_back({np, c, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+    }
   }
   plan.a_near = a;
   plan.panels_near = upload(op->mem, panels, st, "near panels");
   plan.segs_near = upload(op->mem, segs, st, "near segments");
-  plan.items_near = upload(op->mem, items, st, "near items");
-  plan.nitems_near = int(items.size());
+  plan.small_near = upload(op->mem, small, st, "near items");
+  plan.big_near = upload(op->mem, big, st, "near items");
+  plan.nsmall_near = int(small.size());
+  plan.nbig_near = int(big.size());
 }
 
 // Columns one far-panel item takes before its panel chunk is split over items.
@@ -336,7 +344,7 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   const Tree& t = op->tree;
   std::vector<Panel> panels;
   std::vector<Seg> segs;
-  std::vector<Item> items;
+  std::vector<Item> small, big;
   std::vector<ZBlock> zb;
   std::vector<PanelFix> pfix;
   int64_t nypart = 0;
@@ -383,7 +391,7 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
       const int np = int(panels.size());
       panels.push_back(p);
       if (p.m <= 32) {
-        items.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+        small.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
       } else {
         // runs of segments with about kPanelCols columns each bound one item's work
         std::vector<std::pair<int32_t, int32_t>> groups;
@@ -401,11 +409,11 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
         const int chunks = int((p.m + rows - 1) / rows);
         for (int c = 0; c < chunks; c++) {
           if (groups.size() == 1) {
-            items.push_back({np, c, groups[0].first, groups[0].second, -1});
+            big.push_back({np, c, groups[0].first, groups[0].second, -1});
             continue;
           }
           pfix.push_back({np, c, int32_t(nypart), int32_t(groups.size())});
-          for (auto& g : groups) items.push_back({np, c, g.first, g.second, int32_t(nypart++)});
+          for (auto& g : groups) big.push_back({np, c, g.first, g.second, int32_t(nypart++)});
         }
       }
     }
@@ -415,30 +423,32 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   plan.a_far = a;
   plan.panels_far = upload(op->mem, panels, st, "far panels");
   plan.segs_far = upload(op->mem, segs, st, "far segments");
-  plan.items_far = upload(op->mem, items, st, "far items");
-  plan.nitems_far = int(items.size());
+  plan.small_far = upload(op->mem, small, st, "far items");
+  plan.big_far = upload(op->mem, big, st, "far items");
+  plan.nsmall_far = int(small.size());
+  plan.nbig_far = int(big.size());
+  // V^T x items: up to 32 sixteen-byte loads of columns by a run of rows of
+  // about kZItemBytes; blocks with more rows split into partial sums
   std::vector<ZItem> zit;
   std::vector<ZFix> zfix;
   int64_t nzpart = 0;
-  const int T = int(tile_rows(a == Prec::kD ? 8 : 4));
+  const int esz = a == Prec::kD ? 8 : 4;
+  const int cmax = 32 * (16 / esz);
   for (size_t q = 0; q < zb.size(); q++) {
     const int n = zb[q].n, r = zb[q].r;
-    if (n <= 32) {
-      zit.push_back({int32_t(q), 0, r, 0, 0, -1});
-      continue;
-    }
-    const int ntiles = (n + T - 1) / T;
-    const int groups = (ntiles + kZTiles - 1) / kZTiles;
-    for (int k0 = 0; k0 < r; k0 += kZCols) {
-      const int nk = std::min(kZCols, r - k0);
+    const int rp = int(vpad(r, esz));
+    for (int k0 = 0; k0 < rp; k0 += cmax) {
+      const int nk = std::min(cmax, rp - k0);
+      const int rows = std::max(1, kZItemBytes / (nk * esz));
+      const int groups = (n + rows - 1) / rows;
       if (groups == 1) {
-        zit.push_back({int32_t(q), k0, nk, 0, ntiles, -1});
+        zit.push_back({int32_t(q), k0, nk, 0, n, -1});
         continue;
       }
-      for (int c = 0; c < nk; c++) zfix.push_back({zb[q].z_off + k0 + c, int32_t(nzpart + c), groups});
+      for (int c = 0; c < nk && k0 + c < r; c++) zfix.push_back({zb[q].z_off + k0 + c, int32_t(nzpart + c), groups});
       for (int g = 0; g < groups; g++) {
-        zit.push_back({int32_t(q), k0, nk, g * kZTiles, std::min(ntiles, (g + 1) * kZTiles), int32_t(nzpart)});
-        nzpart += kZCols;
+        zit.push_back({int32_t(q), k0, nk, g * rows, std::min(n, (g + 1) * rows), int32_t(nzpart)});
+        nzpart += kZPart;
       }
     }
   }
@@ -610,7 +620,7 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
       off[q] = bytes;
       const int64_t r = op->rank[b];
       const uint64_t ub = (uint64_t(stored_elems(mm[b], op->dense[b] ? nn[b] : r, int(esz))) * esz + 15) / 16 * 16;
-      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(stored_elems(nn[b], r, int(esz))) * esz + 15) / 16 * 16;
+      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(nn[b]) * uint64_t(vpad(r, int(esz))) * esz + 15) / 16 * 16;
       bytes += ub + vb;
     }
     if (bytes > 0) {
@@ -740,15 +750,18 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
     return e;
   if (plan.nzb > 0) tr.stop(st);
   tr.start(kb + 1, st);
-  if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.items_near, plan.nitems_near, nullptr, 0,
-                         nullptr, in, ldin, yslots, n, op->nslots, 1, st)) != cudaSuccess)
+  if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.small_near, plan.nsmall_near,
+                         plan.big_near, plan.nbig_near, nullptr, 0, nullptr, in, ldin, yslots, n, op->nslots, 1, st)) !=
+      cudaSuccess)
     return e;
   tr.stop(st);
-  if (plan.nitems_far > 0) tr.start(kb + 2, st);
-  if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.items_far, plan.nitems_far, plan.pfix_far,
-                         plan.npfix_far, plan.ypart, in, ldin, yslots, n, op->nslots, 1, st)) != cudaSuccess)
+  const bool far = plan.nsmall_far + plan.nbig_far > 0;
+  if (far) tr.start(kb + 2, st);
+  if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.small_far, plan.nsmall_far, plan.big_far,
+                         plan.nbig_far, plan.pfix_far, plan.npfix_far, plan.ypart, in, ldin, yslots, n, op->nslots, 1,
+                         st)) != cudaSuccess)
     return e;
-  if (plan.nitems_far > 0) tr.stop(st);
+  if (far) tr.stop(st);
   tr.start(kb + 3, st);
   e = launch_combine(px, yslots, n, op->nslots, n, 1, nullptr, y, px, n, st);
   tr.stop(st);
@@ -981,8 +994,10 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
       op->plan32.a_far = Prec::kF;
       op->plan32.panels_far = op->plan64.panels_far;
       op->plan32.segs_far = op->plan64.segs_far;
-      op->plan32.items_far = op->plan64.items_far;
-      op->plan32.nitems_far = op->plan64.nitems_far;
+      op->plan32.small_far = op->plan64.small_far;
+      op->plan32.big_far = op->plan64.big_far;
+      op->plan32.nsmall_far = op->plan64.nsmall_far;
+      op->plan32.nbig_far = op->plan64.nbig_far;
       op->plan32.zb = op->plan64.zb;
       op->plan32.nzb = op->plan64.nzb;
       op->plan32.zitems = op->plan64.zitems;
@@ -1054,10 +1069,11 @@ int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nr
       const Plan& pl = op->plan64;
       CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, pl.zfix, pl.nzfix, pl.zpart, op->d_in64, ldin, 1,
                       st));
-      CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.items_near, pl.nitems_near, nullptr, 0,
-                       nullptr, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
-      CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.items_far, pl.nitems_far, pl.pfix_far,
-                       pl.npfix_far, pl.ypart, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
+      CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.small_near, pl.nsmall_near, pl.big_near,
+                       pl.nbig_near, nullptr, 0, nullptr, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
+      CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.small_far, pl.nsmall_far, pl.big_far,
+                       pl.nbig_far, pl.pfix_far, pl.npfix_far, pl.ypart, op->d_in64, ldin, op->d_y64, n, op->nslots, 1,
+                       st));
       CK(launch_combine(Prec::kD, op->d_y64, n, op->nslots, n, 1, op->d_perm, d_y + c * n, Prec::kD, n, st));
     }
     return HODLR_OK;
@@ -1224,7 +1240,20 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
     } else {
       const size_t r = size_t(std::max(op->rank[size_t(b)], 0));
       fetch(op->uptr[size_t(b)], size_t(mm), r, U);
-      fetch(op->vptr[size_t(b)], size_t(nn), r, V);
+      if (V && op->vptr[size_t(b)] && r > 0) {  // V is row major, nn x vpad(r)
+        const int esz = f32 ? 4 : 8;
+        const size_t rp = size_t(vpad(int64_t(r), esz));
+        std::vector<double> tmp(size_t(nn) * rp);
+        if (f32) {
+          std::vector<float> t32(tmp.size());
+          CK(cudaMemcpy(t32.data(), op->vptr[size_t(b)], t32.size() * 4, cudaMemcpyDeviceToHost));
+          for (size_t i = 0; i < t32.size(); i++) tmp[i] = double(t32[i]);
+        } else {
+          CK(cudaMemcpy(tmp.data(), op->vptr[size_t(b)], tmp.size() * 8, cudaMemcpyDeviceToHost));
+        }
+        for (size_t k = 0; k < r; k++)
+          for (size_t j = 0; j < size_t(nn); j++) V[k * size_t(nn) + j] = tmp[j * rp + k];
+      }
     }
     return HODLR_OK;
   });

@@ -49,75 +49,63 @@ __device__ __forceinline__ void axpy16(const double2& a, double s, double* acc) 
   acc[1] += a.y * s;
 }
 
-// Phase 1: z_b = V_b^T x_s.  A block with n <= 32 is one warp's item: lanes
-// form groups of npad (next power of two >= n) that each take one column.  A
-// larger block is split into items of up to kZCols columns by kZTiles row
-// tiles; a block with more tiles than that writes one partial sum per item and
-// column, and zfix_kernel adds them in order.
+// Phase 1: z_b = V_b^T x_s with V_b stored row major (n x vpad(r)).  The
+// CPL = 16 / sizeof(TA) columns of a 16-byte load belong to one lane; P lanes
+// cover a row's nk columns and the warp's G = 32 / P lane groups take
+// consecutive rows, so each load instruction of the warp reads G whole rows,
+// one contiguous run.  Each lane keeps CPL running sums; the groups are added
+// by shuffles once at the end.  A block with more rows than one item takes
+// writes partial sums (zfix_kernel adds them in order).
 template <typename TA, typename TX, typename TACC>
 __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
                                                     int nitems, TX* __restrict__ zpart, TX* in, int64_t ld_in) {
+  constexpr int CPL = 16 / int(sizeof(TA));
+  using VT = typename Vec16<TA>::type;
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= nitems) return;
   const ZItem it = items[w];
   const ZBlock Z = zb[it.zb];
-  const TA* V = static_cast<const TA*>(Z.V);
+  const int64_t rp = vpad(Z.r, int(sizeof(TA)));
   const TX* x = in + blockIdx.y * ld_in + Z.x_off;
   TX* z = in + blockIdx.y * ld_in + Z.z_off;
-  const int n = Z.n, r = Z.r;
-  if (n <= 32) {
-    int npad = 1;
-    while (npad < n) npad <<= 1;
-    const int slices = 32 / npad;
-    const int j = lane & (npad - 1), c = lane / npad;
-    const TACC xj = j < n ? TACC(x[j]) : TACC(0);
-    for (int k0 = 0; k0 < r; k0 += slices) {
-      const int k = k0 + c;
-      TACC acc = (k < r && j < n) ? TACC(ldg(V + int64_t(k) * n + j)) * xj : TACC(0);
-      for (int o = 1; o < npad; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (j == 0 && k < r) z[k] = TX(acc);
+  const int lanes = (it.nk + CPL - 1) / CPL;
+  int P = 1;
+  while (P < lanes) P <<= 1;
+  const int G = 32 / P, g = lane / P, p = lane % P;
+  const bool cact = p < lanes;
+  const TA* Vc = static_cast<const TA*>(Z.V) + it.k0 + p * CPL;
+  TACC acc[CPL];
+#pragma unroll
+  for (int q = 0; q < CPL; q++) acc[q] = TACC(0);
+  int j = it.j0 + g;
+  for (; j + 3 * G < it.j1; j += 4 * G) {
+    VT v[4];
+    TACC xs[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      v[u] = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j + u * G) * rp)) : VT{};
+      xs[u] = TACC(x[j + u * G]);
     }
-  } else {
-    // One tile at a time: each lane holds RPL rows of x and a running partial
-    // sum per column (kZCols registers), so the up-to-32 column loads of a
-    // tile are independent; one reduce-scatter across the warp at the end
-    // leaves column k0 + c's sum in lane c.
-    constexpr int RPL = 16 / int(sizeof(TA));
-    constexpr int T = 32 * RPL;
-    using VT = typename Vec16<TA>::type;
-    const int k0 = it.k0, nk = it.nk;
-    TACC acc[kZCols];
 #pragma unroll
-    for (int c = 0; c < kZCols; c++) acc[c] = TACC(0);
-    for (int t = it.t0; t < it.t1; t++) {
-      const int rows = min(T, n - t * T);
-      if (lane * RPL >= rows) continue;
-      const int64_t h = tile_height(n, t, int(sizeof(TA)));
-      const TA* tile = V + int64_t(t) * T * r + int64_t(k0) * h + lane * RPL;
-      TACC xv[RPL];
+    for (int u = 0; u < 4; u++) axpy16(v[u], xs[u], acc);
+  }
+  for (; j < it.j1; j += G) {
+    const VT v = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j) * rp)) : VT{};
+    axpy16(v, TACC(x[j]), acc);
+  }
+  for (int o = P; o < 32; o <<= 1)
 #pragma unroll
-      for (int q = 0; q < RPL; q++) xv[q] = (lane * RPL + q < rows) ? TACC(x[t * T + lane * RPL + q]) : TACC(0);
+    for (int q = 0; q < CPL; q++) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+  if (g == 0 && cact) {
 #pragma unroll
-      for (int c = 0; c < kZCols; c++)
-        if (c < nk) acc[c] += dot16<TACC>(__ldg(reinterpret_cast<const VT*>(tile + int64_t(c) * h)), xv);
-    }
-    // reduce-scatter: after the round with offset o each lane keeps o sums
-#pragma unroll
-    for (int o = kZCols / 2; o >= 1; o >>= 1) {
-      const bool upper = (lane & o) != 0;
-#pragma unroll
-      for (int i = 0; i < o; i++) {
-        const TACC send = upper ? acc[i] : acc[i + o];
-        const TACC keep = upper ? acc[i + o] : acc[i];
-        acc[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    for (int q = 0; q < CPL; q++) {
+      const int c = p * CPL + q;
+      if (it.part < 0) {
+        if (it.k0 + c < Z.r) z[it.k0 + c] = TX(acc[q]);
+      } else {
+        zpart[it.part + c] = TX(acc[q]);
       }
-    }
-    if (lane < nk) {
-      if (it.part < 0)
-        z[k0 + lane] = TX(acc[0]);
-      else
-        zpart[it.part + lane] = TX(acc[0]);
     }
   }
 }
@@ -129,17 +117,18 @@ __global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const TX* __
   if (f >= nfix) return;
   const ZFix F = fix[f];
   TX acc = TX(0);
-  for (int q = 0; q < F.count; q++) acc += zpart[F.part + q * kZCols];
+  for (int q = 0; q < F.count; q++) acc += zpart[F.part + q * kZPart];
   in[blockIdx.y * ld_in + F.zpos] = acc;
 }
 
-// Phase 2: one warp per item (a row chunk of a panel times a run of its
-// segments).
+// Phase 2, panels of at most 32 rows (leaves): lanes form groups of mpad
+// (next power of two >= m) rows; the 32 / mpad groups take interleaved
+// columns of each segment; the groups are added by shuffles at the end.
 template <typename TA, typename TX, typename TACC>
 __global__ void __launch_bounds__(256)
-    panel_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
-                 int nitems, TX* __restrict__ ypart, const TX* __restrict__ in, int64_t ld_in, TX* __restrict__ y,
-                 int64_t ld_y, int nslots) {
+    panel_small_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
+                       int nitems, const TX* __restrict__ in, int64_t ld_in, TX* __restrict__ y, int64_t ld_y,
+                       int nslots) {
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= nitems) return;
@@ -148,84 +137,86 @@ __global__ void __launch_bounds__(256)
   const int m = P.m;
   const TX* inc = in + blockIdx.y * ld_in;
   TX* yo = y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin;
-  if (m <= 32) {
-    int mpad = 1;
-    while (mpad < m) mpad <<= 1;
-    const int slices = 32 / mpad;
-    const int i = lane & (mpad - 1), sl = lane / mpad;
-    TACC acc = 0;
-    for (int64_t s = it.seg_b; s < it.seg_e; s++) {
-      const Seg S = segs[s];
-      const TA* A = static_cast<const TA*>(S.A);
-      const TX* x = inc + S.in_off;
-      if (i < m) {
-        int j = sl;
-        TACC a1 = 0;
-        for (; j + slices < S.K; j += 2 * slices) {
-          acc += TACC(ldg(A + int64_t(j) * m + i)) * TACC(x[j]);
-          a1 += TACC(ldg(A + int64_t(j + slices) * m + i)) * TACC(x[j + slices]);
-        }
-        if (j < S.K) acc += TACC(ldg(A + int64_t(j) * m + i)) * TACC(x[j]);
-        acc += a1;
+  int mpad = 1;
+  while (mpad < m) mpad <<= 1;
+  const int slices = 32 / mpad;
+  const int i = lane & (mpad - 1), sl = lane / mpad;
+  TACC acc = 0, a1 = 0;
+  for (int64_t s = it.seg_b; s < it.seg_e; s++) {
+    const Seg S = segs[s];
+    const TA* A = static_cast<const TA*>(S.A);
+    const TX* x = inc + S.in_off;
+    if (i < m) {
+      int j = sl;
+      for (; j + slices < S.K; j += 2 * slices) {
+        acc += TACC(ldg(A + int64_t(j) * m + i)) * TACC(x[j]);
+        a1 += TACC(ldg(A + int64_t(j + slices) * m + i)) * TACC(x[j + slices]);
+      }
+      if (j < S.K) acc += TACC(ldg(A + int64_t(j) * m + i)) * TACC(x[j]);
+    }
+  }
+  acc += a1;
+  for (int o = mpad; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (sl == 0 && i < m) yo[i] = TX(acc);
+}
+
+// Phase 2, panels of more than 32 rows: item chunk = row tile t of the
+// panel; every segment's tile is streamed column by column, 16 bytes per
+// lane (rows t*T + lane*RPL ..).  Input values come 32 at a time from one
+// coalesced load and are broadcast by shuffle.
+template <typename TA, typename TX, typename TACC>
+__global__ void __launch_bounds__(256)
+    panel_tile_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
+                      int nitems, TX* __restrict__ ypart, const TX* __restrict__ in, int64_t ld_in,
+                      TX* __restrict__ y, int64_t ld_y, int nslots) {
+  constexpr int RPL = 16 / int(sizeof(TA));
+  constexpr int T = 32 * RPL;
+  using VT = typename Vec16<TA>::type;
+  const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= nitems) return;
+  const Item it = items[w];
+  const Panel P = panels[it.panel];
+  const int m = P.m;
+  const TX* inc = in + blockIdx.y * ld_in;
+  const int t = it.chunk;
+  const int rows = min(T, m - t * T);
+  const int64_t h = tile_height(m, t, int(sizeof(TA)));
+  const bool act = lane * RPL < rows;
+  TACC a0[RPL], a1[RPL];
+#pragma unroll
+  for (int q = 0; q < RPL; q++) a0[q] = a1[q] = TACC(0);
+  for (int64_t s = it.seg_b; s < it.seg_e; s++) {
+    const Seg S = segs[s];
+    const TA* A = static_cast<const TA*>(S.A) + int64_t(t) * T * S.K + lane * RPL;
+    const TX* x = inc + S.in_off;
+    for (int j0 = 0; j0 < S.K; j0 += 32) {
+      const int jn = min(32, S.K - j0);
+      const TACC xl = lane < jn ? TACC(x[j0 + lane]) : TACC(0);
+      const TA* Aj = A + int64_t(j0) * h;
+      int jj = 0;
+      for (; jj + 3 < jn; jj += 4) {
+        VT v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) v[u] = act ? __ldg(reinterpret_cast<const VT*>(Aj + int64_t(jj + u) * h)) : VT{};
+        axpy16(v[0], __shfl_sync(0xffffffffu, xl, jj), a0);
+        axpy16(v[1], __shfl_sync(0xffffffffu, xl, jj + 1), a1);
+        axpy16(v[2], __shfl_sync(0xffffffffu, xl, jj + 2), a0);
+        axpy16(v[3], __shfl_sync(0xffffffffu, xl, jj + 3), a1);
+      }
+      for (; jj < jn; jj++) {
+        const VT v = act ? __ldg(reinterpret_cast<const VT*>(Aj + int64_t(jj) * h)) : VT{};
+        axpy16(v, __shfl_sync(0xffffffffu, xl, jj), a0);
       }
     }
-    for (int o = mpad; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (sl == 0 && i < m) yo[i] = TX(acc);
-  } else {
-    // Item chunk = row tile t.  Segment descriptors and input values are
-    // fetched 32 at a time with one coalesced load and broadcast by shuffle,
-    // so the loads of the matrix columns (16 bytes per lane) have no
-    // dependent global load in front of them.
-    constexpr int RPL = 16 / int(sizeof(TA));
-    constexpr int T = 32 * RPL;
-    using VT = typename Vec16<TA>::type;
-    const int t = it.chunk;
-    const int rows = min(T, m - t * T);
-    const int64_t h = tile_height(m, t, int(sizeof(TA)));
-    const bool act = lane * RPL < rows;
-    TACC a0[RPL], a1[RPL];
+  }
+  if (act) {
+    const int i = t * T + lane * RPL;
+    TX* dst = it.part < 0 ? y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin + i
+                          : ypart + int64_t(it.part) * T + lane * RPL;
 #pragma unroll
-    for (int q = 0; q < RPL; q++) a0[q] = a1[q] = TACC(0);
-    for (int sb = it.seg_b; sb < it.seg_e; sb += 32) {
-      const int ns = min(32, it.seg_e - sb);
-      Seg mine{};
-      if (lane < ns) mine = segs[sb + lane];
-      for (int u = 0; u < ns; u++) {
-        const unsigned long long ap =
-            __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(mine.A), u);
-        const long long in_off = __shfl_sync(0xffffffffu, static_cast<long long>(mine.in_off), u);
-        const int K = __shfl_sync(0xffffffffu, mine.K, u);
-        const TA* A = reinterpret_cast<const TA*>(ap) + int64_t(t) * T * K + lane * RPL;
-        const TX* x = inc + in_off;
-        for (int j0 = 0; j0 < K; j0 += 32) {
-          const int jn = min(32, K - j0);
-          const TACC xl = lane < jn ? TACC(x[j0 + lane]) : TACC(0);
-          int jj = 0;
-          for (; jj + 7 < jn; jj += 8) {
-            VT v[8];
-#pragma unroll
-            for (int w2 = 0; w2 < 8; w2++)
-              v[w2] = act ? __ldg(reinterpret_cast<const VT*>(A + int64_t(j0 + jj + w2) * h)) : VT{};
-#pragma unroll
-            for (int w2 = 0; w2 < 8; w2 += 2) {
-              axpy16(v[w2], __shfl_sync(0xffffffffu, xl, jj + w2), a0);
-              axpy16(v[w2 + 1], __shfl_sync(0xffffffffu, xl, jj + w2 + 1), a1);
-            }
-          }
-          for (; jj < jn; jj++) {
-            const VT v = act ? __ldg(reinterpret_cast<const VT*>(A + int64_t(j0 + jj) * h)) : VT{};
-            axpy16(v, __shfl_sync(0xffffffffu, xl, jj), a0);
-          }
-        }
-      }
-    }
-    if (act) {
-      const int i = t * T + lane * RPL;
-      TX* dst = it.part < 0 ? yo + i : ypart + int64_t(it.part) * T + lane * RPL;
-#pragma unroll
-      for (int q = 0; q < RPL; q++)
-        if (i + q < m) dst[q] = TX(a0[q] + a1[q]);
-    }
+    for (int q = 0; q < RPL; q++)
+      if (i + q < m) dst[q] = TX(a0[q] + a1[q]);
   }
 }
 
@@ -306,13 +297,14 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
       const int i = int(e % B.m), k = int(e / B.m);
       u[elem_offset(lmap[B.t_map + i] - B.t_begin, k, B.m, B.rank, esz)] = TO(U[e]);
     }
-    // V follows U's full workspace (m x cap); its first rank columns are contiguous
+    // V follows U's full workspace (m x cap); stored row major, n x vpad(rank)
     const double* Vw = ws + B.ws + int64_t(B.m) * B.cap;
     TO* v = static_cast<TO*>(B.v_dst);
+    const int64_t rp = vpad(B.rank, esz);
     const int64_t nv = int64_t(B.n) * B.rank;
     for (int64_t e = threadIdx.x; e < nv; e += blockDim.x) {
       const int j = int(e % B.n), k = int(e / B.n);
-      v[elem_offset(lmap[B.s_map + j] - B.s_begin, k, B.n, B.rank, esz)] = TO(Vw[e]);
+      v[(lmap[B.s_map + j] - B.s_begin) * rp + k] = TO(Vw[e]);
     }
   }
 }
@@ -328,68 +320,71 @@ unsigned vec_grid(int64_t n) {
 
 }  // namespace
 
+template <typename TA, typename TX, typename TACC>
+static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix, void* zpart, void* in,
+                    int64_t ld_in, int nrhs, cudaStream_t st) {
+  dim3 g(warps_grid(nitems), unsigned(nrhs));
+  zgemv_kernel<TA, TX, TACC><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<TX*>(zpart), static_cast<TX*>(in), ld_in);
+  if (nfix > 0) {
+    dim3 gf(unsigned((nfix + 255) / 256), unsigned(nrhs));
+    zfix_kernel<TX><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const TX*>(zpart), static_cast<TX*>(in), ld_in);
+  }
+}
+
 cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
                          void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st) {
   if (nitems <= 0) return cudaSuccess;
   count_launches(nfix > 0 ? 2 : 1);
-  dim3 g(warps_grid(nitems), unsigned(nrhs));
-  dim3 gf(unsigned((nfix + 255) / 256), unsigned(nrhs));
-  if (a == Prec::kD && x == Prec::kD) {
-    zgemv_kernel<double, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(zpart),
-                                                            static_cast<double*>(in), ld_in);
-    if (nfix > 0)
-      zfix_kernel<double><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const double*>(zpart), static_cast<double*>(in),
-                                               ld_in);
-  } else if (a == Prec::kF && x == Prec::kD) {
-    zgemv_kernel<float, double, double><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<double*>(zpart),
-                                                           static_cast<double*>(in), ld_in);
-    if (nfix > 0)
-      zfix_kernel<double><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const double*>(zpart), static_cast<double*>(in),
-                                               ld_in);
-  } else if (a == Prec::kF && x == Prec::kF) {
-    zgemv_kernel<float, float, float><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<float*>(zpart),
-                                                         static_cast<float*>(in), ld_in);
-    if (nfix > 0)
-      zfix_kernel<float><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const float*>(zpart), static_cast<float*>(in),
-                                              ld_in);
-  } else {
+  if (a == Prec::kD && x == Prec::kD)
+    zgemv_t<double, double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+  else if (a == Prec::kF && x == Prec::kD)
+    zgemv_t<float, double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+  else if (a == Prec::kF && x == Prec::kF)
+    zgemv_t<float, float, float>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+  else
     return cudaErrorInvalidValue;
-  }
   return cudaGetLastError();
 }
 
-cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* items, int nitems,
-                          const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y,
-                          int64_t ld_y, int nslots, int nrhs, cudaStream_t st) {
-  if (nitems <= 0) return cudaSuccess;
-  count_launches(nfix > 0 ? 2 : 1);
-  dim3 g(warps_grid(nitems), unsigned(nrhs));
-  const int rows = rows_per_item(a);
-  dim3 gf(unsigned((int64_t(nfix) * rows + 255) / 256), unsigned(nrhs));
-  if (a == Prec::kD && x == Prec::kD) {
-    panel_kernel<double, double, double><<<g, 256, 0, st>>>(panels, segs, items, nitems, static_cast<double*>(ypart),
-                                                            static_cast<const double*>(in), ld_in,
-                                                            static_cast<double*>(y), ld_y, nslots);
-    if (nfix > 0)
-      panel_fix_kernel<double><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const double*>(ypart),
-                                                    static_cast<double*>(y), ld_y, nslots);
-  } else if (a == Prec::kF && x == Prec::kD) {
-    panel_kernel<float, double, double><<<g, 256, 0, st>>>(panels, segs, items, nitems, static_cast<double*>(ypart),
-                                                           static_cast<const double*>(in), ld_in,
-                                                           static_cast<double*>(y), ld_y, nslots);
-    if (nfix > 0)
-      panel_fix_kernel<double><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const double*>(ypart),
-                                                    static_cast<double*>(y), ld_y, nslots);
-  } else if (a == Prec::kF && x == Prec::kF) {
-    panel_kernel<float, float, float><<<g, 256, 0, st>>>(panels, segs, items, nitems, static_cast<float*>(ypart),
-                                                         static_cast<const float*>(in), ld_in,
-                                                         static_cast<float*>(y), ld_y, nslots);
-    if (nfix > 0)
-      panel_fix_kernel<float><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const float*>(ypart),
-                                                   static_cast<float*>(y), ld_y, nslots);
-  } else {
-    return cudaErrorInvalidValue;
+template <typename TA, typename TX, typename TACC>
+static void panels_t(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big, int nbig,
+                     const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y, int64_t ld_y,
+                     int nslots, int nrhs, cudaStream_t st) {
+  if (nbig > 0) {
+    dim3 g(warps_grid(nbig), unsigned(nrhs));
+    panel_tile_kernel<TA, TX, TACC><<<g, 256, 0, st>>>(panels, segs, big, nbig, static_cast<TX*>(ypart),
+                                                       static_cast<const TX*>(in), ld_in, static_cast<TX*>(y), ld_y,
+                                                       nslots);
   }
+  if (nsmall > 0) {
+    dim3 g(warps_grid(nsmall), unsigned(nrhs));
+    panel_small_kernel<TA, TX, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TX*>(in), ld_in,
+                                                        static_cast<TX*>(y), ld_y, nslots);
+  }
+  if (nfix > 0) {
+    const int rows = int(tile_rows(int(sizeof(TA))));
+    dim3 gf(unsigned((int64_t(nfix) * rows + 255) / 256), unsigned(nrhs));
+    panel_fix_kernel<TX><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const TX*>(ypart),
+                                             static_cast<TX*>(y), ld_y, nslots);
+  }
+}
+
+cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
+                          const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
+                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st) {
+  if (nsmall + nbig <= 0) return cudaSuccess;
+  count_launches(uint64_t(nbig > 0) + uint64_t(nsmall > 0) + uint64_t(nfix > 0));
+  if (a == Prec::kD && x == Prec::kD)
+    panels_t<double, double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y,
+                                     nslots, nrhs, st);
+  else if (a == Prec::kF && x == Prec::kD)
+    panels_t<float, double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y,
+                                    nslots, nrhs, st);
+  else if (a == Prec::kF && x == Prec::kF)
+    panels_t<float, float, float>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots,
+                                  nrhs, st);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 

@@ -81,8 +81,15 @@ struct PanelFix {
 }; 
 
 
+// V factors are stored row major, n x vpad(r): each row's r values padded to a
+// multiple of one 16-byte load.
+__host__ __device__ inline int64_t vpad(int64_t r, int esz) {
+  const int64_t c = 16 / esz;
+  return (r + c - 1) / c * c;
+}
+
 struct ZBlock {
-  const void* V;   // n x r, stored as above
+  const void* V;   // n x vpad(r), row major
   int64_t x_off;   // tree position of the source node
   int64_t z_off;   // offset of z_b in the input buffer
   int32_t n, r;
@@ -92,14 +99,14 @@ struct ZBlock {
 // them for blocks with n <= 32, at most kZCols for larger ones).
 struct ZItem {
   int32_t zb;
-  int32_t k0, nk;  // columns k0 .. k0 + nk - 1 (nk <= kZCols)
-  int32_t t0, t1;  // row tiles t0 .. t1 - 1 (blocks with n > 32)
-  int32_t part;    // < 0: write z; else partial sums at zpart[part + c]
+  int32_t k0, nk;  // (padded) columns k0 .. k0 + nk - 1, at most 32 loads of 16 bytes
+  int32_t j0, j1;  // rows j0 .. j1 - 1
+  int32_t part;    // < 0: write z; else partial sums at zpart[part + c], c < nk
 };
-constexpr int kZCols = 32;  // columns per item (one running sum per lane)
-constexpr int kZTiles = 8;  // row tiles per item
+constexpr int kZPart = 128;          // partial-sum stride of one item (>= any nk)
+constexpr int kZItemBytes = 1 << 16;  // V bytes one item reads at most (when the block has that many)
 
-// z[zpos] = sum_{q < count} zpart[part + q * kZCols]
+// z[zpos] = sum_{q < count} zpart[part + q * kZPart]
 struct ZFix {
   int64_t zpos;
   int32_t part;
@@ -114,9 +121,10 @@ enum class Prec { kD, kF };  // double, float
 // zpart / ypart: scratch of the vector precision (one column of partials).
 cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
                          void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st);
-cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* items, int nitems,
-                          const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y,
-                          int64_t ld_y, int nslots, int nrhs, cudaStream_t st);
+// `small` items belong to panels of at most 32 rows, `big` ones to larger panels.
+cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
+                          const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
+                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st);
 // rows handled by one big-panel item for stored element size `a`
 inline int rows_per_item(Prec a) { return a == Prec::kD ? 64 : 128; }
 // out[perm[i] + c*ld_out] (or out[i + c*ld_out] when perm == NULL) =
