@@ -121,9 +121,11 @@ __global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const TX* __
   in[blockIdx.y * ld_in + F.zpos] = acc;
 }
 
-// Phase 2, panels of at most 32 rows (leaves): lanes form groups of mpad
-// (next power of two >= m) rows; the 32 / mpad groups take interleaved
-// columns of each segment; the groups are added by shuffles at the end.
+// Phase 2, panels of at most 32 rows (leaves): lanes form 32 / mpad slices of
+// mpad lanes (mpad = next power of two >= m), one lane per row; slice sl
+// walks segments sl, sl + slices, ... of the item on its own, four columns
+// per step, so a warp has several small tiles in flight at once.  The slices
+// are added by shuffles at the end.
 template <typename TA, typename TX, typename TACC>
 __global__ void __launch_bounds__(256)
     panel_small_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
@@ -141,21 +143,26 @@ __global__ void __launch_bounds__(256)
   while (mpad < m) mpad <<= 1;
   const int slices = 32 / mpad;
   const int i = lane & (mpad - 1), sl = lane / mpad;
-  TACC acc = 0, a1 = 0;
-  for (int64_t s = it.seg_b; s < it.seg_e; s++) {
-    const Seg S = segs[s];
-    const TA* A = static_cast<const TA*>(S.A);
-    const TX* x = inc + S.in_off;
-    if (i < m) {
-      int j = sl;
-      for (; j + slices < S.K; j += 2 * slices) {
-        acc += TACC(ldg(A + int64_t(j) * m + i)) * TACC(x[j]);
-        a1 += TACC(ldg(A + int64_t(j + slices) * m + i)) * TACC(x[j + slices]);
+  TACC a0 = 0, a1 = 0;
+  if (i < m) {
+    for (int64_t s = it.seg_b + sl; s < it.seg_e; s += slices) {
+      const Seg S = segs[s];
+      const TA* A = static_cast<const TA*>(S.A) + i;
+      const TX* x = inc + S.in_off;
+      int j = 0;
+      for (; j + 3 < S.K; j += 4) {
+        const TA v0 = ldg(A + int64_t(j) * m), v1 = ldg(A + int64_t(j + 1) * m);
+        const TA v2 = ldg(A + int64_t(j + 2) * m), v3 = ldg(A + int64_t(j + 3) * m);
+        const TX x0 = x[j], x1 = x[j + 1], x2 = x[j + 2], x3 = x[j + 3];
+        a0 += TACC(v0) * TACC(x0);
+        a1 += TACC(v1) * TACC(x1);
+        a0 += TACC(v2) * TACC(x2);
+        a1 += TACC(v3) * TACC(x3);
       }
-      if (j < S.K) acc += TACC(ldg(A + int64_t(j) * m + i)) * TACC(x[j]);
+      for (; j < S.K; j++) a0 += TACC(ldg(A + int64_t(j) * m)) * TACC(x[j]);
     }
   }
-  acc += a1;
+  TACC acc = a0 + a1;
   for (int o = mpad; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (sl == 0 && i < m) yo[i] = TX(acc);
 }
