@@ -26,6 +26,7 @@ HODLR_KERNEL_EXP_NEG_R = 4
 
 HODLR_PREC_FP64 = 0
 HODLR_PREC_MIXED = 1
+HODLR_PREC_FP32_FACTORS = 2
 
 
 class HodlrParams(ctypes.Structure):

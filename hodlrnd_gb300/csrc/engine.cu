@@ -474,7 +474,7 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
   uptr.assign(nb, nullptr);
   vptr.assign(nb, nullptr);
   if (nb == 0) return;
-  const Prec fp = op->p.precision == HODLR_PREC_MIXED ? Prec::kF : Prec::kD;
+  const Prec fp = op->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
   const size_t esz = fp == Prec::kD ? 8 : 4;
   const int cap0 = op->p.rank_cap > 0 ? op->p.rank_cap : 64;
   std::vector<int32_t> cap(nb);
@@ -692,7 +692,7 @@ void compute_stats(hodlr_op* op) {
   s.n_flop = flop;
   s.memory_gb = 8e-9 * flop;
   s.compression_ratio = flop / (double(op->n) * double(op->n));
-  const double fesz = op->p.precision == HODLR_PREC_MIXED ? 4.0 : 8.0;
+  const double fesz = op->p.precision == HODLR_PREC_FP64 ? 8.0 : 4.0;
   s.near_bytes = uint64_t(s.near_entries * 8.0 * (op->p.precision == HODLR_PREC_MIXED ? 1.5 : 1.0));
   s.far_bytes = uint64_t((s.far_entries + s.dense_far_entries) * fesz);
   s.device_bytes = op->mem.used;
@@ -745,8 +745,10 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
   Tracer& tr = op->tr;
   if (plan.nzb > 0) tr.start(kb + 0, st);
+  // FP32 factors with FP64 vectors: compensated FP32 accumulation
+  const bool df = plan.a_far == Prec::kF && px == Prec::kD;
   if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.zitems, plan.nzitems, plan.zfix, plan.nzfix, plan.zpart, in, ldin,
-                        1, st)) != cudaSuccess)
+                        1, st, df)) != cudaSuccess)
     return e;
   if (plan.nzb > 0) tr.stop(st);
   tr.start(kb + 1, st);
@@ -759,7 +761,7 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   if (far) tr.start(kb + 2, st);
   if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.small_far, plan.nsmall_far, plan.big_far,
                          plan.nbig_far, plan.pfix_far, plan.npfix_far, plan.ypart, in, ldin, yslots, n, op->nslots, 1,
-                         st)) != cudaSuccess)
+                         st, df)) != cudaSuccess)
     return e;
   if (far) tr.stop(st);
   tr.start(kb + 3, st);
@@ -782,7 +784,8 @@ void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr
   const int restart = p.restart > 0 ? p.restart : 100;
   const double t0 = now_s();
   if (p.precision != HODLR_PREC_MIXED) {
-    // HODLRdD_matrix::solve: x0 = b, iterSolver(100, N, eps_ACA) (HDD_matrix.hpp:51-62)
+    // HODLRdD_matrix::solve: x0 = b, iterSolver(100, N, eps_ACA) (HDD_matrix.hpp:51-62);
+    // with FP32 factors the same FP64 GMRES runs on the FP32-stored operator
     CK(cudaMemcpyAsync(x, b, sizeof(double) * size_t(op->n), cudaMemcpyDeviceToDevice, st));
     TreeMatvec<double> A = [op, st](const double* xi, double* yo) {
       return apply_tree<double>(op, op->plan64, xi, yo, op->d_in64, op->d_y64, st);
@@ -888,7 +891,7 @@ int hodlr_ctx_create(const hodlr_params* params, hodlr_ctx** out) {
   if (!(p.eps_aca > 0.0) || !(p.eps_aca < 1.0))
     return fail(nullptr, HODLR_ERR_INVALID, "eps_aca must be in (0, 1) (values >= 1 select a fixed rank in the "
                                             "reference, which this engine does not support)");
-  if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED)
+  if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED && p.precision != HODLR_PREC_FP32_FACTORS)
     return fail(nullptr, HODLR_ERR_INVALID, "unknown precision");
   if (p.restart < 0 || p.restart > 1000) return fail(nullptr, HODLR_ERR_INVALID, "restart must be in 0..1000");
   int ndev = 0;
@@ -986,7 +989,7 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
     const double t3 = now_s();
     op->st.t_aca_s = t3 - t2;
     // plans
-    const Prec fp = op->p.precision == HODLR_PREC_MIXED ? Prec::kF : Prec::kD;
+    const Prec fp = op->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
     build_near_plan(op.get(), nt, near64, Prec::kD, op->plan64, st);
     build_far_plan(op.get(), uptr, vptr, fp, op->plan64, st);
     if (op->p.precision == HODLR_PREC_MIXED) {
@@ -1067,13 +1070,14 @@ int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nr
       CK(cudaMemcpyAsync(op->d_in64, op->d_io, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, st));
       if (op->nslots > 1) CK(cudaMemsetAsync(op->d_y64 + n, 0, sizeof(double) * size_t(n) * (op->nslots - 1), st));
       const Plan& pl = op->plan64;
+      const bool df = pl.a_far == Prec::kF;
       CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, pl.zfix, pl.nzfix, pl.zpart, op->d_in64, ldin, 1,
-                      st));
+                      st, df));
       CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.small_near, pl.nsmall_near, pl.big_near,
                        pl.nbig_near, nullptr, 0, nullptr, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
       CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.small_far, pl.nsmall_far, pl.big_far,
                        pl.nbig_far, pl.pfix_far, pl.npfix_far, pl.ypart, op->d_in64, ldin, op->d_y64, n, op->nslots, 1,
-                       st));
+                       st, df));
       CK(launch_combine(Prec::kD, op->d_y64, n, op->nslots, n, 1, op->d_perm, d_y + c * n, Prec::kD, n, st));
     }
     return HODLR_OK;
@@ -1215,7 +1219,7 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
     if (n) *n = nn;
     if (rank) *rank = op->rank[size_t(b)];
     if (dense) *dense = op->dense[size_t(b)];
-    const bool f32 = op->p.precision == HODLR_PREC_MIXED;
+    const bool f32 = op->p.precision != HODLR_PREC_FP64;
     // copy a stored rows x cols matrix (tiled layout, matvec.h) to a dense column-major dst
     auto fetch = [&](const void* src, size_t rows, size_t cols, double* dst) {
       if (!dst || !src || rows * cols == 0) return;

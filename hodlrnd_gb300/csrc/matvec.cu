@@ -24,29 +24,109 @@ struct Vec16<double> {
   using type = double2;
 };
 
-template <typename TACC>
-__device__ __forceinline__ TACC dot16(const float4& a, const TACC* x) {
-  return TACC(a.x) * x[0] + TACC(a.y) * x[1] + TACC(a.z) * x[2] + TACC(a.w) * x[3];
+// Accumulators.  Acc<float> and Acc<double> are plain sums.  Acc<DF> is a
+// compensated FP32 accumulator: the running value is hi + lo, each product
+// of an FP32 matrix entry with an FP64 input split as xh + xl is formed
+// exactly with an FMA (p + e == v * xh), and each addition keeps its
+// rounding error (TwoSum), following Ogita, Rump and Oishi, "Accurate sum
+// and dot product", SIAM J. Sci. Comput. 26 (2005), algorithm Dot2.  The
+// result is about as accurate as FP64 accumulation while using only the
+// FP32 pipe (GB300's FP64 rate is far below what a streaming matvec needs).
+struct DF {
+  float hi, lo;
+};
+
+template <typename T>
+struct Acc;
+
+template <>
+struct Acc<float> {
+  using A = float;
+  using X = float;
+  static __device__ __forceinline__ X in(float v) { return v; }
+  static __device__ __forceinline__ X in(double v) { return float(v); }
+  static __device__ __forceinline__ A zero() { return 0.f; }
+  static __device__ __forceinline__ void fma(A& a, float v, X x) { a += v * x; }
+  static __device__ __forceinline__ A add(A a, A b) { return a + b; }
+  static __device__ __forceinline__ A shfl_xor(A a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+  static __device__ __forceinline__ X shfl(X x, int src) { return __shfl_sync(0xffffffffu, x, src); }
+  static __device__ __forceinline__ double value(A a) { return double(a); }
+};
+
+template <>
+struct Acc<double> {
+  using A = double;
+  using X = double;
+  static __device__ __forceinline__ X in(float v) { return double(v); }
+  static __device__ __forceinline__ X in(double v) { return v; }
+  static __device__ __forceinline__ A zero() { return 0.0; }
+  static __device__ __forceinline__ void fma(A& a, float v, X x) { a += double(v) * x; }
+  static __device__ __forceinline__ void fma(A& a, double v, X x) { a += v * x; }
+  static __device__ __forceinline__ A add(A a, A b) { return a + b; }
+  static __device__ __forceinline__ A shfl_xor(A a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+  static __device__ __forceinline__ X shfl(X x, int src) { return __shfl_sync(0xffffffffu, x, src); }
+  static __device__ __forceinline__ double value(A a) { return a; }
+};
+
+template <>
+struct Acc<DF> {
+  using A = DF;
+  using X = DF;
+  static __device__ __forceinline__ X in(double v) {
+    const float h = __double2float_rn(v);
+    return DF{h, __double2float_rn(v - double(h))};
+  }
+  static __device__ __forceinline__ X in(float v) { return DF{v, 0.f}; }
+  static __device__ __forceinline__ A zero() { return DF{0.f, 0.f}; }
+  // a += v * (x.hi + x.lo)
+  static __device__ __forceinline__ void fma(A& a, float v, X x) {
+    const float p = __fmul_rn(v, x.hi);
+    float e = __fmaf_rn(v, x.hi, -p);
+    e = __fmaf_rn(v, x.lo, e);
+    const float s = __fadd_rn(a.hi, p);
+    const float bb = __fsub_rn(s, a.hi);
+    const float t = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    a.hi = s;
+    a.lo = __fadd_rn(a.lo, __fadd_rn(t, e));
+  }
+  static __device__ __forceinline__ A add(A a, A b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float t = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    return DF{s, __fadd_rn(__fadd_rn(a.lo, b.lo), t)};
+  }
+  static __device__ __forceinline__ A shfl_xor(A a, int o) {
+    return DF{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+  }
+  static __device__ __forceinline__ X shfl(X x, int src) {
+    return DF{__shfl_sync(0xffffffffu, x.hi, src), __shfl_sync(0xffffffffu, x.lo, src)};
+  }
+  static __device__ __forceinline__ double value(A a) { return double(a.hi) + double(a.lo); }
+};
+
+// acc[q] += a[q] * x for the components of a 16-byte vector
+template <typename TACC, typename X>
+__device__ __forceinline__ void axpy16(const float4& a, X x, typename Acc<TACC>::A* acc) {
+  Acc<TACC>::fma(acc[0], a.x, x);
+  Acc<TACC>::fma(acc[1], a.y, x);
+  Acc<TACC>::fma(acc[2], a.z, x);
+  Acc<TACC>::fma(acc[3], a.w, x);
 }
-template <typename TACC>
-__device__ __forceinline__ TACC dot16(const double2& a, const TACC* x) {
-  return TACC(a.x) * x[0] + TACC(a.y) * x[1];
+template <typename TACC, typename X>
+__device__ __forceinline__ void axpy16(const double2& a, X x, typename Acc<TACC>::A* acc) {
+  Acc<TACC>::fma(acc[0], a.x, x);
+  Acc<TACC>::fma(acc[1], a.y, x);
 }
-__device__ __forceinline__ void axpy16(const float4& a, float s, float* acc) {
-  acc[0] += a.x * s;
-  acc[1] += a.y * s;
-  acc[2] += a.z * s;
-  acc[3] += a.w * s;
+
+template <typename T>
+__device__ __forceinline__ T vzero();
+template <>
+__device__ __forceinline__ float4 vzero<float4>() {
+  return make_float4(0.f, 0.f, 0.f, 0.f);
 }
-__device__ __forceinline__ void axpy16(const float4& a, double s, double* acc) {
-  acc[0] += double(a.x) * s;
-  acc[1] += double(a.y) * s;
-  acc[2] += double(a.z) * s;
-  acc[3] += double(a.w) * s;
-}
-__device__ __forceinline__ void axpy16(const double2& a, double s, double* acc) {
-  acc[0] += a.x * s;
-  acc[1] += a.y * s;
+template <>
+__device__ __forceinline__ double2 vzero<double2>() {
+  return make_double2(0.0, 0.0);
 }
 
 // Phase 1: z_b = V_b^T x_s with V_b stored row major (n x vpad(r)).  The
@@ -75,36 +155,37 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
   const int G = 32 / P, g = lane / P, p = lane % P;
   const bool cact = p < lanes;
   const TA* Vc = static_cast<const TA*>(Z.V) + it.k0 + p * CPL;
-  TACC acc[CPL];
+  using AC = Acc<TACC>;
+  typename AC::A acc[CPL];
 #pragma unroll
-  for (int q = 0; q < CPL; q++) acc[q] = TACC(0);
+  for (int q = 0; q < CPL; q++) acc[q] = AC::zero();
   int j = it.j0 + g;
   for (; j + 3 * G < it.j1; j += 4 * G) {
     VT v[4];
-    TACC xs[4];
+    typename AC::X xs[4];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
-      v[u] = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j + u * G) * rp)) : VT{};
-      xs[u] = TACC(x[j + u * G]);
+      v[u] = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j + u * G) * rp)) : vzero<VT>();
+      xs[u] = AC::in(x[j + u * G]);
     }
 #pragma unroll
-    for (int u = 0; u < 4; u++) axpy16(v[u], xs[u], acc);
+    for (int u = 0; u < 4; u++) axpy16<TACC>(v[u], xs[u], acc);
   }
   for (; j < it.j1; j += G) {
-    const VT v = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j) * rp)) : VT{};
-    axpy16(v, TACC(x[j]), acc);
+    const VT v = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j) * rp)) : vzero<VT>();
+    axpy16<TACC>(v, AC::in(x[j]), acc);
   }
   for (int o = P; o < 32; o <<= 1)
 #pragma unroll
-    for (int q = 0; q < CPL; q++) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    for (int q = 0; q < CPL; q++) acc[q] = AC::add(acc[q], AC::shfl_xor(acc[q], o));
   if (g == 0 && cact) {
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
       const int c = p * CPL + q;
       if (it.part < 0) {
-        if (it.k0 + c < Z.r) z[it.k0 + c] = TX(acc[q]);
+        if (it.k0 + c < Z.r) z[it.k0 + c] = TX(AC::value(acc[q]));
       } else {
-        zpart[it.part + c] = TX(acc[q]);
+        zpart[it.part + c] = TX(AC::value(acc[q]));
       }
     }
   }
@@ -143,7 +224,8 @@ __global__ void __launch_bounds__(256)
   while (mpad < m) mpad <<= 1;
   const int slices = 32 / mpad;
   const int i = lane & (mpad - 1), sl = lane / mpad;
-  TACC a0 = 0, a1 = 0;
+  using AC = Acc<TACC>;
+  typename AC::A a0 = AC::zero(), a1 = AC::zero();
   if (i < m) {
     for (int64_t s = it.seg_b + sl; s < it.seg_e; s += slices) {
       const Seg S = segs[s];
@@ -154,17 +236,17 @@ __global__ void __launch_bounds__(256)
         const TA v0 = ldg(A + int64_t(j) * m), v1 = ldg(A + int64_t(j + 1) * m);
         const TA v2 = ldg(A + int64_t(j + 2) * m), v3 = ldg(A + int64_t(j + 3) * m);
         const TX x0 = x[j], x1 = x[j + 1], x2 = x[j + 2], x3 = x[j + 3];
-        a0 += TACC(v0) * TACC(x0);
-        a1 += TACC(v1) * TACC(x1);
-        a0 += TACC(v2) * TACC(x2);
-        a1 += TACC(v3) * TACC(x3);
+        AC::fma(a0, v0, AC::in(x0));
+        AC::fma(a1, v1, AC::in(x1));
+        AC::fma(a0, v2, AC::in(x2));
+        AC::fma(a1, v3, AC::in(x3));
       }
-      for (; j < S.K; j++) a0 += TACC(ldg(A + int64_t(j) * m)) * TACC(x[j]);
+      for (; j < S.K; j++) AC::fma(a0, ldg(A + int64_t(j) * m), AC::in(x[j]));
     }
   }
-  TACC acc = a0 + a1;
-  for (int o = mpad; o < 32; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if (sl == 0 && i < m) yo[i] = TX(acc);
+  typename AC::A acc = AC::add(a0, a1);
+  for (int o = mpad; o < 32; o <<= 1) acc = AC::add(acc, AC::shfl_xor(acc, o));
+  if (sl == 0 && i < m) yo[i] = TX(AC::value(acc));
 }
 
 // Phase 2, panels of more than 32 rows: item chunk = row tile t of the
@@ -190,30 +272,32 @@ __global__ void __launch_bounds__(256)
   const int rows = min(T, m - t * T);
   const int64_t h = tile_height(m, t, int(sizeof(TA)));
   const bool act = lane * RPL < rows;
-  TACC a0[RPL], a1[RPL];
+  using AC = Acc<TACC>;
+  typename AC::A a0[RPL], a1[RPL];
 #pragma unroll
-  for (int q = 0; q < RPL; q++) a0[q] = a1[q] = TACC(0);
+  for (int q = 0; q < RPL; q++) a0[q] = a1[q] = AC::zero();
   for (int64_t s = it.seg_b; s < it.seg_e; s++) {
     const Seg S = segs[s];
     const TA* A = static_cast<const TA*>(S.A) + int64_t(t) * T * S.K + lane * RPL;
     const TX* x = inc + S.in_off;
     for (int j0 = 0; j0 < S.K; j0 += 32) {
       const int jn = min(32, S.K - j0);
-      const TACC xl = lane < jn ? TACC(x[j0 + lane]) : TACC(0);
+      const typename AC::X xl = AC::in(lane < jn ? x[j0 + lane] : TX(0));
       const TA* Aj = A + int64_t(j0) * h;
       int jj = 0;
       for (; jj + 3 < jn; jj += 4) {
         VT v[4];
 #pragma unroll
-        for (int u = 0; u < 4; u++) v[u] = act ? __ldg(reinterpret_cast<const VT*>(Aj + int64_t(jj + u) * h)) : VT{};
-        axpy16(v[0], __shfl_sync(0xffffffffu, xl, jj), a0);
-        axpy16(v[1], __shfl_sync(0xffffffffu, xl, jj + 1), a1);
-        axpy16(v[2], __shfl_sync(0xffffffffu, xl, jj + 2), a0);
-        axpy16(v[3], __shfl_sync(0xffffffffu, xl, jj + 3), a1);
+        for (int u = 0; u < 4; u++)
+          v[u] = act ? __ldg(reinterpret_cast<const VT*>(Aj + int64_t(jj + u) * h)) : vzero<VT>();
+        axpy16<TACC>(v[0], AC::shfl(xl, jj), a0);
+        axpy16<TACC>(v[1], AC::shfl(xl, jj + 1), a1);
+        axpy16<TACC>(v[2], AC::shfl(xl, jj + 2), a0);
+        axpy16<TACC>(v[3], AC::shfl(xl, jj + 3), a1);
       }
       for (; jj < jn; jj++) {
-        const VT v = act ? __ldg(reinterpret_cast<const VT*>(Aj + int64_t(jj) * h)) : VT{};
-        axpy16(v, __shfl_sync(0xffffffffu, xl, jj), a0);
+        const VT v = act ? __ldg(reinterpret_cast<const VT*>(Aj + int64_t(jj) * h)) : vzero<VT>();
+        axpy16<TACC>(v, AC::shfl(xl, jj), a0);
       }
     }
   }
@@ -223,7 +307,7 @@ __global__ void __launch_bounds__(256)
                           : ypart + int64_t(it.part) * T + lane * RPL;
 #pragma unroll
     for (int q = 0; q < RPL; q++)
-      if (i + q < m) dst[q] = TX(a0[q] + a1[q]);
+      if (i + q < m) dst[q] = TX(AC::value(AC::add(a0[q], a1[q])));
   }
 }
 
@@ -339,11 +423,13 @@ static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix
 }
 
 cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
-                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st) {
+                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st, bool df) {
   if (nitems <= 0) return cudaSuccess;
   count_launches(nfix > 0 ? 2 : 1);
   if (a == Prec::kD && x == Prec::kD)
     zgemv_t<double, double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+  else if (a == Prec::kF && x == Prec::kD && df)
+    zgemv_t<float, double, DF>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else if (a == Prec::kF && x == Prec::kD)
     zgemv_t<float, double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else if (a == Prec::kF && x == Prec::kF)
@@ -378,12 +464,15 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
 
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
-                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st) {
+                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st, bool df) {
   if (nsmall + nbig <= 0) return cudaSuccess;
   count_launches(uint64_t(nbig > 0) + uint64_t(nsmall > 0) + uint64_t(nfix > 0));
   if (a == Prec::kD && x == Prec::kD)
     panels_t<double, double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y,
                                      nslots, nrhs, st);
+  else if (a == Prec::kF && x == Prec::kD && df)
+    panels_t<float, double, DF>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots,
+                                nrhs, st);
   else if (a == Prec::kF && x == Prec::kD)
     panels_t<float, double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y,
                                     nslots, nrhs, st);

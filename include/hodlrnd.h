@@ -61,6 +61,9 @@ typedef struct hodlr_kernel_desc {
 #define HODLR_PREC_FP64 0  /* everything FP64 (the reference's arithmetic, include/myHeaders.hpp:66-72) */
 #define HODLR_PREC_MIXED 1 /* far-field U, V in FP32; FP64 near field; solve = FP64 iterative
                               refinement around an FP32 inner GMRES */
+#define HODLR_PREC_FP32_FACTORS 2 /* far-field U, V in FP32, every product accumulated in compensated
+                                     FP32 (FP64-level accuracy); FP64 near field; FP64 GMRES as the
+                                     reference's solve, on the FP32-stored operator */
 
 /* ---- parameters -------------------------------------------------------- */
 typedef struct hodlr_params {

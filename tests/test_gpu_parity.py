@@ -137,6 +137,29 @@ def test_mixed_precision_solve_reaches_tolerance():
     M32.close()
 
 
+def test_fp32_factor_solve_reaches_tolerance():
+    """FP32-stored factors, products accumulated in compensated FP32, FP64 GMRES
+    (x0 = b, as the reference): converges on the stored operator in about the
+    FP64 iteration count, to the same solution within the factor rounding."""
+    c = cases.REF_CASES["hodlr3d_n4096"]
+    f = dict(np.load(os.path.join(GOLDEN, "ref_hodlr3d_n4096.npz")))
+    M64 = build(c, f["points"])
+    M32 = build(c, f["points"], precision="fp32_factors")
+    y64, y32 = M64 * f["x"], M32 * f["x"]
+    assert rel(y32, y64) < 1e-6
+    x64 = M64.solve(f["b"])
+    it64 = M64.last_solve["iterations"]
+    x32 = M32.solve(f["b"])
+    info = M32.last_solve
+    assert info["converged"] == 1 and info["rel_residual"] <= c["eps"]
+    assert abs(info["iterations"] - it64) <= 3
+    assert rel(x32, x64) < 1e-5
+    r = f["b"] - M64 * x32
+    assert np.linalg.norm(r) / np.linalg.norm(f["b"]) < 1e-6
+    M64.close()
+    M32.close()
+
+
 def _oracle_compare(pts, lo, hi, nmax, dp, eps, kind, scale, diag):
     O = OracleHODLR(pts, lo, hi, nmax=nmax, dprime=dp, eps=eps, kind=kind, scale=scale, diag=diag, rng_mode=1)
     M = HODLRdD_matrix(Kernel(kind, scale, diag), pts, lo, hi, Nmax=nmax, eps_ACA=eps, INTERACTION_TYPE_ALLOWED=dp)
