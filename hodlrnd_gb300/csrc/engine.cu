@@ -201,6 +201,7 @@ struct hodlr_op {
   Plan plan32;        // MIXED inner operator (all FP32)
   // work vectors
   double* d_in64 = nullptr;  // [x | z], n + zlen
+  void* d_in2 = nullptr;     // [x | z] as (hi, lo) FP32 pairs: FP32 factors with FP64 vectors
   double* d_y64 = nullptr;   // nslots x n
   float* d_in32 = nullptr;
   float* d_y32 = nullptr;
@@ -745,9 +746,14 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
   Tracer& tr = op->tr;
   if (plan.nzb > 0) tr.start(kb + 0, st);
-  // FP32 factors with FP64 vectors: compensated FP32 accumulation
+  // FP32 factors with FP64 vectors: compensated FP32 accumulation on split inputs
   const bool df = plan.a_far == Prec::kF && px == Prec::kD;
-  if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.zitems, plan.nzitems, plan.zfix, plan.nzfix, plan.zpart, in, ldin,
+  void* fin = in;
+  if (df) {
+    fin = op->d_in2;
+    if ((e = launch_split(reinterpret_cast<const double*>(in), fin, n, st)) != cudaSuccess) return e;
+  }
+  if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.zitems, plan.nzitems, plan.zfix, plan.nzfix, plan.zpart, fin, ldin,
                         1, st, df)) != cudaSuccess)
     return e;
   if (plan.nzb > 0) tr.stop(st);
@@ -760,7 +766,7 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   const bool far = plan.nsmall_far + plan.nbig_far > 0;
   if (far) tr.start(kb + 2, st);
   if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.small_far, plan.nsmall_far, plan.big_far,
-                         plan.nbig_far, plan.pfix_far, plan.npfix_far, plan.ypart, in, ldin, yslots, n, op->nslots, 1,
+                         plan.nbig_far, plan.pfix_far, plan.npfix_far, plan.ypart, fin, ldin, yslots, n, op->nslots, 1,
                          st, df)) != cudaSuccess)
     return e;
   if (far) tr.stop(st);
@@ -1019,6 +1025,7 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
     // work vectors
     const int64_t ldin = n + op->zlen;
     op->d_in64 = op->mem.alloc_n<double>(size_t(ldin), "matvec input");
+    if (op->p.precision != HODLR_PREC_FP64) op->d_in2 = op->mem.alloc(size_t(ldin) * 8, "matvec input (FP32 pairs)");
     op->d_y64 = op->mem.alloc_n<double>(size_t(n) * size_t(op->nslots), "matvec slots");
     op->d_b64 = op->mem.alloc_n<double>(size_t(n), "rhs");
     op->d_x64 = op->mem.alloc_n<double>(size_t(n), "solution");
@@ -1071,13 +1078,18 @@ int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nr
       if (op->nslots > 1) CK(cudaMemsetAsync(op->d_y64 + n, 0, sizeof(double) * size_t(n) * (op->nslots - 1), st));
       const Plan& pl = op->plan64;
       const bool df = pl.a_far == Prec::kF;
-      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, pl.zfix, pl.nzfix, pl.zpart, op->d_in64, ldin, 1,
-                      st, df));
+      void* fin = op->d_in64;
+      if (df) {
+        fin = op->d_in2;
+        CK(launch_split(op->d_in64, fin, n, st));
+      }
+      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, pl.zfix, pl.nzfix, pl.zpart, fin, ldin, 1, st,
+                      df));
       CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.small_near, pl.nsmall_near, pl.big_near,
                        pl.nbig_near, nullptr, 0, nullptr, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
       CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.small_far, pl.nsmall_far, pl.big_far,
-                       pl.nbig_far, pl.pfix_far, pl.npfix_far, pl.ypart, op->d_in64, ldin, op->d_y64, n, op->nslots, 1,
-                       st, df));
+                       pl.nbig_far, pl.pfix_far, pl.npfix_far, pl.ypart, fin, ldin, op->d_y64, n, op->nslots, 1, st,
+                       df));
       CK(launch_combine(Prec::kD, op->d_y64, n, op->nslots, n, 1, op->d_perm, d_y + c * n, Prec::kD, n, st));
     }
     return HODLR_OK;

@@ -77,7 +77,13 @@ struct Acc<DF> {
     return DF{h, __double2float_rn(v - double(h))};
   }
   static __device__ __forceinline__ X in(float v) { return DF{v, 0.f}; }
+  static __device__ __forceinline__ X in(float2 v) { return DF{v.x, v.y}; }
   static __device__ __forceinline__ A zero() { return DF{0.f, 0.f}; }
+  // hi + lo renormalised (FastTwoSum) as an input pair
+  static __device__ __forceinline__ float2 to_pair(A a) {
+    const float s = __fadd_rn(a.hi, a.lo);
+    return make_float2(s, __fsub_rn(a.lo, __fsub_rn(s, a.hi)));
+  }
   // a += v * (x.hi + x.lo)
   static __device__ __forceinline__ void fma(A& a, float v, X x) {
     const float p = __fmul_rn(v, x.hi);
@@ -102,6 +108,33 @@ struct Acc<DF> {
     return DF{__shfl_sync(0xffffffffu, x.hi, src), __shfl_sync(0xffffffffu, x.lo, src)};
   }
   static __device__ __forceinline__ double value(A a) { return double(a.hi) + double(a.lo); }
+};
+
+// Element types of a launch: the input vector buffer [x | z] (TI) and the
+// outputs and partial sums (TY).  Compensated accumulation reads its inputs
+// pre-split into (hi, lo) FP32 pairs, so its hot loops use no FP64 operation.
+template <typename TACC>
+struct IO;
+template <>
+struct IO<float> {
+  using TI = float;
+  using TY = float;
+  static __device__ __forceinline__ TI from_double(double v) { return float(v); }
+};
+template <>
+struct IO<double> {
+  using TI = double;
+  using TY = double;
+  static __device__ __forceinline__ TI from_double(double v) { return v; }
+};
+template <>
+struct IO<DF> {
+  using TI = float2;
+  using TY = double;
+  static __device__ __forceinline__ TI from_double(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - double(h)));
+  }
 };
 
 // acc[q] += a[q] * x for the components of a 16-byte vector
@@ -129,6 +162,15 @@ __device__ __forceinline__ double2 vzero<double2>() {
   return make_double2(0.0, 0.0);
 }
 
+template <typename TACC>
+__device__ __forceinline__ typename IO<TACC>::TI to_input(typename Acc<TACC>::A a) {
+  return typename IO<TACC>::TI(Acc<TACC>::value(a));
+}
+template <>
+__device__ __forceinline__ float2 to_input<DF>(DF a) {
+  return Acc<DF>::to_pair(a);
+}
+
 // Phase 1: z_b = V_b^T x_s with V_b stored row major (n x vpad(r)).  The
 // CPL = 16 / sizeof(TA) columns of a 16-byte load belong to one lane; P lanes
 // cover a row's nk columns and the warp's G = 32 / P lane groups take
@@ -136,9 +178,11 @@ __device__ __forceinline__ double2 vzero<double2>() {
 // one contiguous run.  Each lane keeps CPL running sums; the groups are added
 // by shuffles once at the end.  A block with more rows than one item takes
 // writes partial sums (zfix_kernel adds them in order).
-template <typename TA, typename TX, typename TACC>
+template <typename TA, typename TACC>
 __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
-                                                    int nitems, TX* __restrict__ zpart, TX* in, int64_t ld_in) {
+                                                    int nitems, typename IO<TACC>::TY* __restrict__ zpart,
+                                                    typename IO<TACC>::TI* in, int64_t ld_in) {
+  using TX = typename IO<TACC>::TI;
   constexpr int CPL = 16 / int(sizeof(TA));
   using VT = typename Vec16<TA>::type;
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
@@ -183,23 +227,24 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
     for (int q = 0; q < CPL; q++) {
       const int c = p * CPL + q;
       if (it.part < 0) {
-        if (it.k0 + c < Z.r) z[it.k0 + c] = TX(AC::value(acc[q]));
+        if (it.k0 + c < Z.r) z[it.k0 + c] = to_input<TACC>(acc[q]);
       } else {
-        zpart[it.part + c] = TX(AC::value(acc[q]));
+        zpart[it.part + c] = typename IO<TACC>::TY(AC::value(acc[q]));
       }
     }
   }
 }
 
-template <typename TX>
-__global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const TX* __restrict__ zpart, TX* in,
-                            int64_t ld_in) {
+template <typename TACC>
+__global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const typename IO<TACC>::TY* __restrict__ zpart,
+                            typename IO<TACC>::TI* in, int64_t ld_in) {
+  using TY = typename IO<TACC>::TY;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= nfix) return;
   const ZFix F = fix[f];
-  TX acc = TX(0);
+  TY acc = TY(0);
   for (int q = 0; q < F.count; q++) acc += zpart[F.part + q * kZPart];
-  in[blockIdx.y * ld_in + F.zpos] = acc;
+  in[blockIdx.y * ld_in + F.zpos] = IO<TACC>::from_double(double(acc));
 }
 
 // Phase 2, panels of at most 32 rows (leaves): lanes form 32 / mpad slices of
@@ -207,11 +252,13 @@ __global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const TX* __
 // walks segments sl, sl + slices, ... of the item on its own, four columns
 // per step, so a warp has several small tiles in flight at once.  The slices
 // are added by shuffles at the end.
-template <typename TA, typename TX, typename TACC>
+template <typename TA, typename TACC>
 __global__ void __launch_bounds__(256)
     panel_small_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
-                       int nitems, const TX* __restrict__ in, int64_t ld_in, TX* __restrict__ y, int64_t ld_y,
-                       int nslots) {
+                       int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
+                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
+  using TX = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (w >= nitems) return;
@@ -219,7 +266,7 @@ __global__ void __launch_bounds__(256)
   const Panel P = panels[it.panel];
   const int m = P.m;
   const TX* inc = in + blockIdx.y * ld_in;
-  TX* yo = y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin;
+  TY* yo = y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin;
   int mpad = 1;
   while (mpad < m) mpad <<= 1;
   const int slices = 32 / mpad;
@@ -246,18 +293,21 @@ __global__ void __launch_bounds__(256)
   }
   typename AC::A acc = AC::add(a0, a1);
   for (int o = mpad; o < 32; o <<= 1) acc = AC::add(acc, AC::shfl_xor(acc, o));
-  if (sl == 0 && i < m) yo[i] = TX(AC::value(acc));
+  if (sl == 0 && i < m) yo[i] = TY(AC::value(acc));
 }
 
 // Phase 2, panels of more than 32 rows: item chunk = row tile t of the
 // panel; every segment's tile is streamed column by column, 16 bytes per
 // lane (rows t*T + lane*RPL ..).  Input values come 32 at a time from one
 // coalesced load and are broadcast by shuffle.
-template <typename TA, typename TX, typename TACC>
+template <typename TA, typename TACC>
 __global__ void __launch_bounds__(256)
     panel_tile_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
-                      int nitems, TX* __restrict__ ypart, const TX* __restrict__ in, int64_t ld_in,
-                      TX* __restrict__ y, int64_t ld_y, int nslots) {
+                      int nitems, typename IO<TACC>::TY* __restrict__ ypart,
+                      const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
+                      typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
+  using TX = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
   constexpr int RPL = 16 / int(sizeof(TA));
   constexpr int T = 32 * RPL;
   using VT = typename Vec16<TA>::type;
@@ -282,7 +332,7 @@ __global__ void __launch_bounds__(256)
     const TX* x = inc + S.in_off;
     for (int j0 = 0; j0 < S.K; j0 += 32) {
       const int jn = min(32, S.K - j0);
-      const typename AC::X xl = AC::in(lane < jn ? x[j0 + lane] : TX(0));
+      const typename AC::X xl = AC::in(lane < jn ? x[j0 + lane] : TX{});
       const TA* Aj = A + int64_t(j0) * h;
       int jj = 0;
       for (; jj + 3 < jn; jj += 4) {
@@ -303,11 +353,11 @@ __global__ void __launch_bounds__(256)
   }
   if (act) {
     const int i = t * T + lane * RPL;
-    TX* dst = it.part < 0 ? y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin + i
+    TY* dst = it.part < 0 ? y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin + i
                           : ypart + int64_t(it.part) * T + lane * RPL;
 #pragma unroll
     for (int q = 0; q < RPL; q++)
-      if (i + q < m) dst[q] = TX(AC::value(AC::add(a0[q], a1[q])));
+      if (i + q < m) dst[q] = TY(AC::value(AC::add(a0[q], a1[q])));
   }
 }
 
@@ -411,14 +461,16 @@ unsigned vec_grid(int64_t n) {
 
 }  // namespace
 
-template <typename TA, typename TX, typename TACC>
+template <typename TA, typename TACC>
 static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix, void* zpart, void* in,
                     int64_t ld_in, int nrhs, cudaStream_t st) {
+  using TI = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
   dim3 g(warps_grid(nitems), unsigned(nrhs));
-  zgemv_kernel<TA, TX, TACC><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<TX*>(zpart), static_cast<TX*>(in), ld_in);
+  zgemv_kernel<TA, TACC><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<TY*>(zpart), static_cast<TI*>(in), ld_in);
   if (nfix > 0) {
     dim3 gf(unsigned((nfix + 255) / 256), unsigned(nrhs));
-    zfix_kernel<TX><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const TX*>(zpart), static_cast<TX*>(in), ld_in);
+    zfix_kernel<TACC><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const TY*>(zpart), static_cast<TI*>(in), ld_in);
   }
 }
 
@@ -427,38 +479,37 @@ cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, i
   if (nitems <= 0) return cudaSuccess;
   count_launches(nfix > 0 ? 2 : 1);
   if (a == Prec::kD && x == Prec::kD)
-    zgemv_t<double, double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+    zgemv_t<double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else if (a == Prec::kF && x == Prec::kD && df)
-    zgemv_t<float, double, DF>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
-  else if (a == Prec::kF && x == Prec::kD)
-    zgemv_t<float, double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+    zgemv_t<float, DF>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else if (a == Prec::kF && x == Prec::kF)
-    zgemv_t<float, float, float>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+    zgemv_t<float, float>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
-template <typename TA, typename TX, typename TACC>
+template <typename TA, typename TACC>
 static void panels_t(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big, int nbig,
                      const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y, int64_t ld_y,
                      int nslots, int nrhs, cudaStream_t st) {
+  using TI = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
   if (nbig > 0) {
     dim3 g(warps_grid(nbig), unsigned(nrhs));
-    panel_tile_kernel<TA, TX, TACC><<<g, 256, 0, st>>>(panels, segs, big, nbig, static_cast<TX*>(ypart),
-                                                       static_cast<const TX*>(in), ld_in, static_cast<TX*>(y), ld_y,
-                                                       nslots);
+    panel_tile_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, big, nbig, static_cast<TY*>(ypart),
+                                                   static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots);
   }
   if (nsmall > 0) {
     dim3 g(warps_grid(nsmall), unsigned(nrhs));
-    panel_small_kernel<TA, TX, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TX*>(in), ld_in,
-                                                        static_cast<TX*>(y), ld_y, nslots);
+    panel_small_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in,
+                                                    static_cast<TY*>(y), ld_y, nslots);
   }
   if (nfix > 0) {
     const int rows = int(tile_rows(int(sizeof(TA))));
     dim3 gf(unsigned((int64_t(nfix) * rows + 255) / 256), unsigned(nrhs));
-    panel_fix_kernel<TX><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const TX*>(ypart),
-                                             static_cast<TX*>(y), ld_y, nslots);
+    panel_fix_kernel<TY><<<gf, 256, 0, st>>>(panels, fix, nfix, rows, static_cast<const TY*>(ypart),
+                                             static_cast<TY*>(y), ld_y, nslots);
   }
 }
 
@@ -468,19 +519,30 @@ cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, 
   if (nsmall + nbig <= 0) return cudaSuccess;
   count_launches(uint64_t(nbig > 0) + uint64_t(nsmall > 0) + uint64_t(nfix > 0));
   if (a == Prec::kD && x == Prec::kD)
-    panels_t<double, double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y,
-                                     nslots, nrhs, st);
+    panels_t<double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots,
+                             nrhs, st);
   else if (a == Prec::kF && x == Prec::kD && df)
-    panels_t<float, double, DF>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots,
-                                nrhs, st);
-  else if (a == Prec::kF && x == Prec::kD)
-    panels_t<float, double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y,
-                                    nslots, nrhs, st);
+    panels_t<float, DF>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
+                        st);
   else if (a == Prec::kF && x == Prec::kF)
-    panels_t<float, float, float>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots,
-                                  nrhs, st);
+    panels_t<float, float>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
+                           st);
   else
     return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+__global__ void split_kernel(const double* __restrict__ x, float2* __restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const double v = x[i];
+    const float h = __double2float_rn(v);
+    out[i] = make_float2(h, __double2float_rn(v - double(h)));
+  }
+}
+
+cudaError_t launch_split(const double* x, void* out, int64_t n, cudaStream_t st) {
+  count_launches(1);
+  split_kernel<<<vec_grid(n), 256, 0, st>>>(x, static_cast<float2*>(out), n);
   return cudaGetLastError();
 }
 

@@ -119,8 +119,10 @@ enum class Prec { kD, kF };  // double, float
 // in:   input buffer [x (ld_in rows of x) | z], nrhs columns with leading dimension ld_in
 // y:    output slots, slot s of column c at y + (c * nslots + s) * ld_y
 // zpart / ypart: scratch of the vector precision (one column of partials).
-// df: FP32 matrices with FP64 vectors accumulated in compensated FP32
-// (FP64-level accuracy on the FP32 pipe) instead of FP64 arithmetic.
+// df: FP32 matrices with FP64 vectors, accumulated in compensated FP32
+// (FP64-level accuracy on the FP32 pipe); the input buffer `in` then holds
+// each FP64 value split into an (hi, lo) FP32 pair (launch_split), and z is
+// written in the same form.  Outputs and partial sums stay FP64.
 cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
                          void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st, bool df = false);
 // `small` items belong to panels of at most 32 rows, `big` ones to larger panels.
@@ -128,6 +130,8 @@ cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, 
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
                           int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st,
                           bool df = false);
+// out[i] = (hi, lo) FP32 pair of x[i] (hi = x rounded to FP32, lo = the rest)
+cudaError_t launch_split(const double* x, void* out, int64_t n, cudaStream_t st);
 // rows handled by one big-panel item for stored element size `a`
 inline int rows_per_item(Prec a) { return a == Prec::kD ? 64 : 128; }
 // out[perm[i] + c*ld_out] (or out[i + c*ld_out] when perm == NULL) =
