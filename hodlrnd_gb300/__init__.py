@@ -4,3 +4,4 @@ the C ABI of include/hodlrnd.h."""
 from ._lib import HodlrError, lib  # noqa: F401
 from .kernels import Kernel, kernel_2d_test, kernel_3d_test, kernel_4d_test  # noqa: F401
 from .matrix import HODLRdD_matrix  # noqa: F401
+from .storedata import load_vec, save_vec  # noqa: F401

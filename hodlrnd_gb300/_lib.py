@@ -18,6 +18,7 @@ HODLR_ERR_NOT_CONVERGED = 5
 HODLR_ERR_TREE = 6
 HODLR_ERR_STATE = 7
 HODLR_ERR_DEVICE = 8
+HODLR_ERR_IO = 9
 
 HODLR_KERNEL_INV_R = 1
 HODLR_KERNEL_INV_R2 = 2
@@ -61,8 +62,10 @@ class HodlrStats(ctypes.Structure):
 
 
 TRACE_KINDS = 16
-TRACE_NAMES = {0: "zgemv_fp64", 1: "near_fp64", 2: "far_fp64", 3: "combine_fp64", 4: "zgemv_fp32", 5: "near_fp32",
-               6: "far_fp32", 7: "combine_fp32"}
+# kinds 0-3: launches with FP64 vectors (FP64 factors, or FP32 factors with
+# compensated accumulation); 4-7: FP32 vectors (inner solve of iterative refinement)
+TRACE_NAMES = {0: "zgemv_x64", 1: "near_x64", 2: "far_x64", 3: "combine_x64", 4: "zgemv_x32", 5: "near_x32",
+               6: "far_x32", 7: "combine_x32"}
 
 
 class HodlrTrace(ctypes.Structure):
@@ -114,7 +117,9 @@ def lib():
     L.hodlr_tree_sizes.argtypes = [P, I64]
     L.hodlr_tree_get.argtypes = [P, I64, I64, I64, I64, I64, I64, I64]
     L.hodlr_tree_destroy.argtypes = [P]
-    for f in ("hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
+    L.hodlr_vec_load.argtypes = [ctypes.c_char_p, D, ctypes.c_int64, I64]
+    L.hodlr_vec_save.argtypes = [ctypes.c_char_p, D, ctypes.c_int64]
+    for f in ("hodlr_vec_load", "hodlr_vec_save", "hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
               "hodlr_matvec_device", "hodlr_solve", "hodlr_solve_device", "hodlr_stats_get",
               "hodlr_get_permutation", "hodlr_get_blocks", "hodlr_tree_build", "hodlr_tree_sizes",
               "hodlr_tree_get", "hodlr_tree_destroy", "hodlr_get_block", "hodlr_trace_enable", "hodlr_trace_get", "hodlr_set_solver"):

@@ -40,6 +40,7 @@ extern "C" {
 #define HODLR_ERR_TREE 6          /* tree would exceed the node limit (degenerate input) */
 #define HODLR_ERR_STATE 7         /* call out of order (e.g. matvec before build) */
 #define HODLR_ERR_DEVICE 8        /* a device-side check failed (index or size out of range) */
+#define HODLR_ERR_IO 9            /* a file could not be read or written, or is malformed */
 
 /* ---- kernels --------------------------------------------------------- */
 /* Entry A_ij for i != j with r = |x_i - x_j| (Euclidean, include/points_dt.hpp:31-39);
@@ -184,11 +185,12 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
  * move.  No counterpart in the reference, which only times whole phases with
  * omp_get_wtime (include/HDD_tree.hpp:77-81,95-99). */
 #define HODLR_TRACE_KINDS 16
-#define HODLR_TRACE_ZGEMV_FP64 0   /* z = V^T x, FP64 vectors */
+#define HODLR_TRACE_ZGEMV_FP64 0   /* z = V^T x, FP64 vectors (FP64 factors, or FP32 factors with
+                                      compensated accumulation) */
 #define HODLR_TRACE_NEAR_FP64 1    /* near-field leaf panels, FP64 vectors */
 #define HODLR_TRACE_FAR_FP64 2     /* far-field panels (U z and dense far blocks), FP64 vectors */
 #define HODLR_TRACE_COMBINE_FP64 3 /* sum of the per-level output slots */
-#define HODLR_TRACE_ZGEMV_FP32 4   /* the same four for FP32 vectors (mixed-precision inner solve) */
+#define HODLR_TRACE_ZGEMV_FP32 4   /* the same four for FP32 vectors (inner solve of HODLR_PREC_MIXED) */
 #define HODLR_TRACE_NEAR_FP32 5
 #define HODLR_TRACE_FAR_FP32 6
 #define HODLR_TRACE_COMBINE_FP32 7
@@ -238,6 +240,17 @@ int hodlr_aca_block_noalloc(const double* d_points, int64_t ld, int32_t ndim, co
                             const int32_t* d_cols, int32_t n, const hodlr_kernel_desc* kernel, double eps_aca,
                             uint64_t seed, int32_t cap, double* d_factors, int32_t* rank, int32_t* flags,
                             void* stream);
+
+/* ---- vector files (host only) ------------------------------------------ */
+/* storedata::load_vec / save_vec (include/myHeaders.hpp:146-170): a cereal
+ * PortableBinary archive of one std::vector<double> -- a 1-byte endianness tag
+ * (1 = little endian), a u64 element count, the float64 values -- read and
+ * written without cereal.  hodlr_vec_load with x == NULL only stores the count
+ * in *n; otherwise it fails with HODLR_ERR_INVALID when the file holds more
+ * than cap values.  Both byte orders are read; files are written little endian.
+ * Malformed files give HODLR_ERR_IO.  Errors: hodlr_last_error(NULL). */
+int hodlr_vec_load(const char* path, double* x, int64_t cap, int64_t* n);
+int hodlr_vec_save(const char* path, const double* x, int64_t n);
 
 /* ---- host-only tree planning (no device needed) ------------------------ */
 typedef struct hodlr_tree hodlr_tree;

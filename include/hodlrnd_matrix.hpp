@@ -126,4 +126,19 @@ class HODLRdD_matrix {
   hodlr_solve_info info_{};
 };
 
+// storedata::load_vec / save_vec (include/myHeaders.hpp:146-170) on
+// std::vector<double>, through hodlr_vec_load / hodlr_vec_save (no cereal).
+namespace storedata {
+inline std::vector<double> load_vec(const std::string& fname) {
+  int64_t n = 0;
+  check(hodlr_vec_load(fname.c_str(), nullptr, 0, &n), nullptr);
+  std::vector<double> x(size_t(n));
+  check(hodlr_vec_load(fname.c_str(), x.data(), n, &n), nullptr);
+  return x;
+}
+inline void save_vec(const std::string& fname, const std::vector<double>& x) {
+  check(hodlr_vec_save(fname.c_str(), x.data(), int64_t(x.size())), nullptr);
+}
+}  // namespace storedata
+
 }  // namespace hodlrnd

@@ -16,8 +16,12 @@ and the print_matrix_statistics figures.
 It also stores the reference's golden pair data/x_10000.bin / data/rhs_10000.bin
 (kernel_4d_test, numPoints = 10) with the reference's HODLR matvec of that x at
 its shipped hyper-parameters, and a dense-operator GMRES run used to pin the
-GMRES restatement bit for bit.
+GMRES restatement bit for bit, and the SHA-256 of the two vector files.
+
+    python tests/golden/make_golden.py vecfiles   # only ref_vec_files.json
 """
+import hashlib
+import json
 import os
 import subprocess
 import sys
@@ -76,6 +80,19 @@ def make_golden4d(tmp):
     print("golden4d: dense vs rhs", np.linalg.norm(R["dense"] - rhs) / np.linalg.norm(rhs))
 
 
+def make_vec_files():
+    """SHA-256 and size of the reference's own vector files, so that the
+    product's save_vec can be checked byte for byte against them."""
+    out = {}
+    for name in ("x_10000.bin", "rhs_10000.bin"):
+        with open(os.path.join(REF_DATA, name), "rb") as f:
+            buf = f.read()
+        out[name] = {"bytes": len(buf), "sha256": hashlib.sha256(buf).hexdigest()}
+    with open(os.path.join(HERE, "ref_vec_files.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print("vec files:", out)
+
+
 def make_dense_gmres(tmp):
     c = dict(ndim=2, n=300, nmax=64, dprime=0, eps=1e-12, kind=cases.INV_R, scale=1.0 / 300,
              diag=1.0, lo=-1.0, hi=1.0, seed=7)
@@ -97,6 +114,7 @@ def make_dense_gmres(tmp):
 def main():
     if not os.path.isdir(build.REF_INCLUDE):
         sys.exit(f"reference checkout not found at {build.REF_ROOT}")
+    make_vec_files()
     with tempfile.TemporaryDirectory() as tmp:
         make_golden4d(tmp)
         make_dense_gmres(tmp)
@@ -105,4 +123,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["vecfiles"]:
+        make_vec_files()
+    else:
+        main()
