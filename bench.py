@@ -3,17 +3,17 @@
 
 Workload (HODLR3D, mixed precision): NDIM=3, N=262144 points i.i.d. uniform
 in [0,1]^3 (numpy PCG64, seeded), A_ij = 1/(N^(2/3) |x_i - x_j|), A_ii = 1,
-d' = 0, Nmax = 64, eps_ACA = 1e-8; far-field U, V stored in FP32; each solve is
-FP64 iterative refinement around FP32 GMRES (restart 100) to a relative
-residual of 1e-8; right-hand sides i.i.d. N(0,1).
+d' = 0, Nmax = 64, eps_ACA = 1e-8; far-field U, V stored in FP32; solves to a
+relative residual of 1e-8; right-hand sides i.i.d. N(0,1).  Three engines:
+fp32_factors (headline: FP32 factors with compensated FP32 accumulation inside
+FP64 GMRES), mixed (FP64 iterative refinement around FP32 GMRES) and fp64.
 
 A step is one solve on the device-resident operator (the reference's
 HODLRdD_matrix::solve, include/HDD_matrix.hpp:51-62), with its right-hand side
 already in HBM; the operator build (tree, ACA, leaf blocks) happens once
 before the timed region and is reported separately.  `e2e` repeats the steps
 through the host-pointer C ABI call (hodlr_solve), the copies in and out of
-pinned host memory inside the timed region.  The FP64 engine (FP64 factors,
-FP64 GMRES with x0 = b as the reference) is timed beside it.
+pinned host memory inside the timed region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -37,6 +37,8 @@ N_POINTS = 262144
 NDIM, NMAX, DPRIME, EPS = 3, 64, 0, 1e-8
 SEED = 20261203
 CPU_SAMPLE_ITERS = 4
+METRIC = "solves/s (mixed FP32/FP64 HODLR3D solve to 1e-8 rel. residual)"
+MATVEC_REPS = 10
 
 
 def workload(n, rank):
@@ -47,7 +49,7 @@ def workload(n, rank):
 
 def config(n, impl_note):
     return {"workload": f"HODLR3D solve, N={n} uniform [0,1]^3, A_ij=1/(N^(2/3) r), A_ii=1, d'=0, Nmax=64, "
-                        f"eps_ACA=1e-8, FP32 factors + FP64 iterative refinement to 1e-8 rel. residual",
+                        f"eps_ACA=1e-8, FP32-stored far-field factors, solve to 1e-8 rel. residual",
             "n": n, "ndim": NDIM, "nmax": NMAX, "dprime": DPRIME, "eps_aca": EPS, "tol": EPS, "restart": 100,
             "rhs": "N(0,1), one per step", "l2": "inputs larger than L2 (the stored operator is several GB)",
             "impl_note": impl_note}
@@ -155,6 +157,50 @@ def cpu_baseline(pts, scale, fp64_iters):
                       f"{fp64_iters} iterations of the FP64 solve; build {t_build:.1f} s not included"}
 
 
+def timed_solves(M, B, X, ks, stream):
+    """Solves of right-hand sides B[k], k in ks, into X[k % len(X)] on the
+    device; (total ms, per-step ms, infos)."""
+    import torch
+
+    sp = stream.cuda_stream
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in ks]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    infos = []
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for (a, b), k in zip(ev, ks):
+        a.record(stream)
+        infos.append(M.solve_device(B[k].data_ptr(), X[k % X.shape[0]].data_ptr(), 1, sp))
+        b.record(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    return t0.elapsed_time(t1), np.array([a.elapsed_time(b) for a, b in ev]), infos
+
+
+def matvec_rate(M, x, y, stream):
+    """Single-RHS operator application y = A x on device vectors: ms per matvec
+    and the algorithmic HBM bytes of one application (the traced kernels' bytes:
+    every factor and leaf entry once, the vectors once per reader) over that time."""
+    import torch
+
+    sp = stream.cuda_stream
+    for _ in range(3):
+        M.matvec_device(x.data_ptr(), y.data_ptr(), 1, sp)
+    M.trace(True)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for _ in range(MATVEC_REPS):
+        M.matvec_device(x.data_ptr(), y.data_ptr(), 1, sp)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    tr = M.trace()
+    M.trace(False)
+    ms = t0.elapsed_time(t1) / MATVEC_REPS
+    nbytes = sum(v["bytes_per_launch"] * v["launches"] for v in tr.values()) / MATVEC_REPS
+    return {"ms": round(ms, 4), "bytes": nbytes, "GBps": round(nbytes / (ms / 1e3) / 1e9, 1)}
+
+
 def run_gb300(args):
     import torch
 
@@ -173,25 +219,23 @@ def run_gb300(args):
     box = ([0.0] * NDIM, [1.0] * NDIM)
     common = dict(Nmax=NMAX, eps_ACA=EPS, INTERACTION_TYPE_ALLOWED=DPRIME, tol=EPS, device=local)
     t0 = time.perf_counter()
-    M = h.HODLRdD_matrix(kern, pts, *box, precision="mixed", **common).Assemble_matrix_operators()
+    M = h.HODLRdD_matrix(kern, pts, *box, precision=args.precision, **common).Assemble_matrix_operators()
     build_s = time.perf_counter() - t0
     stats = M.statistics()
-    M64 = h.HODLRdD_matrix(kern, pts, *box, precision="fp64", **common).Assemble_matrix_operators()
-    stats64 = M64.statistics()
-    MF = h.HODLRdD_matrix(kern, pts, *box, precision="fp32_factors", **common).Assemble_matrix_operators()
+    others = {}
+    if not args.headline_only:
+        for prec in ("fp64", "mixed", "fp32_factors"):
+            if prec != args.precision:
+                others[prec] = h.HODLRdD_matrix(kern, pts, *box, precision=prec, **common).Assemble_matrix_operators()
 
     K, W = args.steps, args.warmup
     g = torch.Generator(device="cuda").manual_seed(SEED + 1000 + rank)
     B = torch.randn((K + W, n), generator=g, dtype=torch.float64, device="cuda")
     X = torch.empty_like(B)
     stream = torch.cuda.current_stream()
-    sp = stream.cuda_stream
-    for k in range(W):
-        M.solve_device(B[K + k].data_ptr(), X[K + k].data_ptr(), 1, sp)
-    torch.cuda.synchronize()
+    timed_solves(M, B, X, range(K, K + W), stream)  # warm-up
 
-    # ---- timed region: K solves, inputs resident in HBM
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    # ---- timed region: K solves, right-hand sides resident in HBM
     try:
         gpu_id = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
     except Exception:
@@ -203,56 +247,46 @@ def run_gb300(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks.start()
-    t_all0 = torch.cuda.Event(enable_timing=True)
-    t_all1 = torch.cuda.Event(enable_timing=True)
-    t_all0.record(stream)
-    infos = []
-    for k in range(K):
-        ev[k][0].record(stream)
-        infos.append(M.solve_device(B[k].data_ptr(), X[k].data_ptr(), 1, sp))
-        ev[k][1].record(stream)
-    t_all1.record(stream)
-    torch.cuda.synchronize()
+    total_ms, step_ms, infos = timed_solves(M, B, X, range(K), stream)
     if world > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
     launches = _lib.lib().hodlr_kernel_launches() - launches0
     trace = M.trace()
     M.trace(False)
-    total_ms = t_all0.elapsed_time(t_all1)
-    step_ms = np.array([a.elapsed_time(b) for a, b in ev])
     if world > 1:
         t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     value = K * world / (total_ms / 1e3)
 
-    # ---- FP64 engine on the same right-hand sides (the plain FP64 GPU path)
-    k64 = max(1, min(args.fp64_steps, K))
-    X64 = torch.empty_like(B[:k64])
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    infos64 = [M64.solve_device(B[k].data_ptr(), X64[k].data_ptr(), 1, sp) for k in range(k64)]
-    e1.record(stream)
-    torch.cuda.synchronize()
-    fp64_sps = k64 / (e0.elapsed_time(e1) / 1e3)
-    # FP32-stored factors, compensated accumulation, one FP64 GMRES
-    XF = torch.empty_like(B[:k64])
-    MF.solve_device(B[K].data_ptr(), XF[0].data_ptr(), 1, sp)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    infosF = [MF.solve_device(B[k].data_ptr(), XF[k].data_ptr(), 1, sp) for k in range(k64)]
-    e1.record(stream)
-    torch.cuda.synchronize()
-    f32f_sps = k64 / (e0.elapsed_time(e1) / 1e3)
+    # ---- the other engines on the same right-hand sides
+    k2 = max(1, min(args.other_steps, K))
+    engines = {}
+    X2 = torch.empty_like(B[:k2])
+    for prec, Mo in others.items():
+        timed_solves(Mo, B, X2, [K], stream)
+        ms, _, inf = timed_solves(Mo, B, X2, range(k2), stream)
+        engines[prec] = {"value": round(k2 / (ms / 1e3), 3), "unit": "solves/s", "steps": k2,
+                         "inner_iterations": [i["iterations"] for i in inf],
+                         "outer_iterations": [i["outer_iterations"] for i in inf],
+                         "rel_residual": max(i["rel_residual"] for i in inf)}
 
-    # ---- accuracy: residual of the mixed solution against the FP64 operator
-    x0 = X[0].cpu().numpy()
-    b0 = B[0].cpu().numpy()
-    r64 = float(np.linalg.norm(b0 - M64 * x0) / np.linalg.norm(b0))
-    x64 = X64[0].cpu().numpy()
-    mixed_vs_fp64 = float(np.linalg.norm(x0 - x64) / np.linalg.norm(x64))
+    # ---- single-RHS matvec throughput of each engine's operator
+    matvec = {p: matvec_rate(Mm, B[0], X2[0], stream)
+              for p, Mm in [(args.precision, M)] + list(others.items())}
+
+    # ---- accuracy of the headline solution against the FP64 operator
+    acc = {}
+    if "fp64" in others:
+        M64 = others["fp64"]
+        x0, b0 = X[0].cpu().numpy(), B[0].cpu().numpy()
+        acc["rel_residual_fp64_operator"] = float(np.linalg.norm(b0 - M64 * x0) / np.linalg.norm(b0))
+        x64 = torch.empty_like(B[:1])
+        M64.solve_device(B[0].data_ptr(), x64[0].data_ptr(), 1, stream.cuda_stream)
+        torch.cuda.synchronize()
+        x64 = x64[0].cpu().numpy()
+        acc["rel_diff_vs_fp64_solution"] = float(np.linalg.norm(x0 - x64) / np.linalg.norm(x64))
 
     # ---- end to end through the host-pointer C ABI (pinned host buffers)
     hb = torch.empty((K, n), dtype=torch.float64, pin_memory=True)
@@ -276,36 +310,31 @@ def run_gb300(args):
         name, d = dom
         per_launch_s = d["total_ms"] / d["launches"] / 1e3
         achieved = d["bytes_per_launch"] / per_launch_s / 1e9
-        traffic = traffic_from_profiles(name)
         roofline = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "peak_source": peak_src,
                     "bytes_per_launch": d["bytes_per_launch"], "launches": d["launches"],
                     "avg_launch_us": round(per_launch_s * 1e6, 2),
                     "share_of_traced_ms": round(d["total_ms"] / sum(v["total_ms"] for v in trace.values()), 4),
-                    "traffic": traffic}
+                    "traffic": traffic_from_profiles(name)}
 
-    iters = [i["iterations"] for i in infos]
-    out = {"metric": "solves/s (mixed FP32/FP64 HODLR3D solve to 1e-8 rel. residual)", "value": round(value, 3),
+    fp64_iters = engines.get("fp64", {}).get("inner_iterations") or [i["iterations"] for i in infos]
+    out = {"metric": METRIC, "value": round(value, 3),
            "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": round(total_ms / K, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
-           "data": "synthetic (seeded uniform points, N(0,1) right-hand sides)", "config": config(n, "GB300 engine"),
+           "data": "synthetic (seeded uniform points, N(0,1) right-hand sides)",
+           "config": config(n, ENGINE_NOTES[args.precision]),
            "latency_ms": {"p50": round(float(np.percentile(step_ms, 50)), 3),
                           "p99": round(float(np.percentile(step_ms, 99)), 3)},
-           "fp32_factor_engine": {"value": round(f32f_sps, 3), "unit": "solves/s", "steps": k64,
-                                  "iterations": [i["iterations"] for i in infosF],
-                                  "rel_residual": max(i["rel_residual"] for i in infosF)},
-           "fp64_engine": {"value": round(fp64_sps, 3), "unit": "solves/s", "steps": k64,
-                           "iterations": [i["iterations"] for i in infos64],
-                           "speedup_mixed_vs_fp64": round(value / world / fp64_sps, 3)},
-           "solve": {"inner_iterations": iters, "outer_iterations": [i["outer_iterations"] for i in infos],
-                     "rel_residual_stored_operator": max(i["rel_residual"] for i in infos),
-                     "rel_residual_fp64_operator": r64, "rel_diff_vs_fp64_solution": mixed_vs_fp64},
-           "build": {"mixed_s": round(build_s, 3), "tree_s": round(stats["t_tree_s"], 3),
+           "solve": dict({"engine": args.precision, "inner_iterations": [i["iterations"] for i in infos],
+                          "outer_iterations": [i["outer_iterations"] for i in infos],
+                          "rel_residual_stored_operator": max(i["rel_residual"] for i in infos)}, **acc),
+           "engines": engines,
+           "matvec": matvec,
+           "build": {"s": round(build_s, 3), "tree_s": round(stats["t_tree_s"], 3),
                      "aca_s": round(stats["t_aca_s"], 3), "near_s": round(stats["t_near_s"], 3),
-                     "fp64_aca_s": round(stats64["t_aca_s"], 3), "far_blocks": stats["n_far_blocks"],
-                     "dense_far_blocks": stats["n_dense_far_blocks"], "max_rank": stats["max_rank"],
-                     "far_bytes_fp32": stats["far_bytes"], "far_bytes_fp64": stats64["far_bytes"],
-                     "near_bytes_fp64": stats64["near_bytes"], "device_bytes": stats["device_bytes"],
+                     "far_blocks": stats["n_far_blocks"], "dense_far_blocks": stats["n_dense_far_blocks"],
+                     "max_rank": stats["max_rank"], "far_bytes": stats["far_bytes"],
+                     "near_bytes": stats["near_bytes"], "device_bytes": stats["device_bytes"],
                      "n_flop_reference_metric": stats["n_flop"]},
            "roofline": roofline,
            "trace": {k: {"launches": v["launches"], "ms": round(v["total_ms"], 3),
@@ -315,14 +344,22 @@ def run_gb300(args):
                    "d2h_bytes_per_step": 8 * n},
            "gpu_launches": int(launches), "clocks": clk}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(pts, scale, int(np.median([i["iterations"] for i in infos64])))
+        out["cpu_baseline"] = cpu_baseline(pts, scale, int(np.median(fp64_iters)))
     if rank == 0:
         print(json.dumps(out), flush=True)
     M.close()
-    M64.close()
-    MF.close()
+    for Mo in others.values():
+        Mo.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+ENGINE_NOTES = {
+    "fp32_factors": "far-field U, V stored in FP32, products accumulated in compensated FP32 (Dot2); FP64 near "
+                    "field; FP64 GMRES (restart 100, x0 = b) on the FP32-stored operator",
+    "mixed": "far-field U, V in FP32; FP64 iterative refinement around FP32 GMRES (inner tol 1e-4)",
+    "fp64": "all FP64 (the reference's arithmetic)",
+}
 
 
 def run_reference(args):
@@ -363,7 +400,7 @@ def run_reference(args):
     sample = (f"{CPU_SAMPLE_ITERS} GMRES iterations per step on the same N={n} operator, scaled to the {full_iters} "
               f"iterations of one full FP64 solve (measured once: {t_full:.1f} s, rel. residual {res:.1e}); "
               f"build {t_build:.1f} s not timed")
-    out = {"impl": "reference", "metric": "solves/s (mixed FP32/FP64 HODLR3D solve to 1e-8 rel. residual)",
+    out = {"impl": "reference", "metric": METRIC,
            "value": round(value, 5), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded uniform points, N(0,1) right-hand sides)",
@@ -381,7 +418,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=N_POINTS)
-    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--precision", choices=["fp32_factors", "mixed", "fp64"], default="fp32_factors",
+                    help="engine timed for `value`; the other two are timed beside it")
+    ap.add_argument("--other-steps", type=int, default=3)
+    ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

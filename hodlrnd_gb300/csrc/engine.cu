@@ -734,7 +734,8 @@ struct PrecOf<float> {
 
 // y = A x, tree order, nrhs = 1; x may alias nothing in the op's buffers.
 template <typename T>
-cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, T* yslots, cudaStream_t st) {
+cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, T* yslots, cudaStream_t st,
+                       const int64_t* out_perm = nullptr) {
   const int64_t n = op->n, ldin = n + op->zlen;
   cudaError_t e = cudaMemcpyAsync(in, x, sizeof(T) * size_t(n), cudaMemcpyDeviceToDevice, st);
   if (e != cudaSuccess) return e;
@@ -771,7 +772,7 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
     return e;
   if (far) tr.stop(st);
   tr.start(kb + 3, st);
-  e = launch_combine(px, yslots, n, op->nslots, n, 1, nullptr, y, px, n, st);
+  e = launch_combine(px, yslots, n, op->nslots, n, 1, out_perm, y, px, n, st);
   tr.stop(st);
   if (tr.used > 8192) tr.harvest();
   return e;
@@ -1071,26 +1072,9 @@ int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nr
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t n = op->n;
     for (int64_t c = 0; c < nrhs; c++) {
+      // gather into tree order; the combine step scatters back to the caller's order
       CK(launch_gather(d_x + c * n, Prec::kD, n, op->d_perm, n, 1, op->d_io, Prec::kD, n, st));
-      // the combine step scatters back to the caller's order
-      const int64_t ldin = n + op->zlen;
-      CK(cudaMemcpyAsync(op->d_in64, op->d_io, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, st));
-      if (op->nslots > 1) CK(cudaMemsetAsync(op->d_y64 + n, 0, sizeof(double) * size_t(n) * (op->nslots - 1), st));
-      const Plan& pl = op->plan64;
-      const bool df = pl.a_far == Prec::kF;
-      void* fin = op->d_in64;
-      if (df) {
-        fin = op->d_in2;
-        CK(launch_split(op->d_in64, fin, n, st));
-      }
-      CK(launch_zgemv(pl.a_far, Prec::kD, pl.zb, pl.zitems, pl.nzitems, pl.zfix, pl.nzfix, pl.zpart, fin, ldin, 1, st,
-                      df));
-      CK(launch_panels(pl.a_near, Prec::kD, pl.panels_near, pl.segs_near, pl.small_near, pl.nsmall_near, pl.big_near,
-                       pl.nbig_near, nullptr, 0, nullptr, op->d_in64, ldin, op->d_y64, n, op->nslots, 1, st));
-      CK(launch_panels(pl.a_far, Prec::kD, pl.panels_far, pl.segs_far, pl.small_far, pl.nsmall_far, pl.big_far,
-                       pl.nbig_far, pl.pfix_far, pl.npfix_far, pl.ypart, fin, ldin, op->d_y64, n, op->nslots, 1, st,
-                       df));
-      CK(launch_combine(Prec::kD, op->d_y64, n, op->nslots, n, 1, op->d_perm, d_y + c * n, Prec::kD, n, st));
+      CK(apply_tree<double>(op, op->plan64, op->d_io, d_y + c * n, op->d_in64, op->d_y64, st, op->d_perm));
     }
     return HODLR_OK;
   });
