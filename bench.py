@@ -39,6 +39,7 @@ SEED = 20261203
 CPU_SAMPLE_ITERS = 4
 METRIC = "solves/s (mixed FP32/FP64 HODLR3D solve to 1e-8 rel. residual)"
 MATVEC_REPS = 10
+SERVING_MAX_ITER = 400
 
 
 def workload(n, rank):
@@ -411,6 +412,103 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def serving_trace(count, seed, pool):
+    """The serving workload: Poisson arrivals (mean 200 requests/s) of solve
+    requests on geometries drawn from a pool of `pool` seeded point clouds,
+    NDIM in {2, 3}, N log-uniform in [4096, 262144], kernel in {1/r, log r
+    (2D only), exp(-r)}, A_ii = 1, off-diagonals scaled by 1/N^((d-1)/d),
+    1-16 right-hand sides N(0,1), eps_ACA = tol = 1e-8.  GMRES stops at
+    SERVING_MAX_ITER iterations: with the 1/sqrt(N) scaling, 2D 1/r systems
+    stagnate under GMRES(100); such requests count as not converged."""
+    rng = np.random.default_rng(seed)
+    geos = []
+    for g in range(pool):
+        d = int(rng.choice([2, 3]))
+        n = int(round(np.exp(rng.uniform(np.log(4096), np.log(262144)))))
+        kinds = ["inv_r", "exp_neg_r"] + (["log_r"] if d == 2 else [])
+        kind = str(rng.choice(kinds))
+        geos.append(dict(d=d, n=n, kind=kind, seed=int(rng.integers(1 << 30)), key=g + 1))
+    t = 0.0
+    reqs = []
+    for i in range(count):
+        t += rng.exponential(1.0 / 200.0)
+        g = geos[int(rng.integers(pool))]
+        reqs.append(dict(t=t, geo=g, nrhs=int(rng.integers(1, 17)), seed=int(rng.integers(1 << 30))))
+    return reqs
+
+
+def run_serving(args):
+    """Replays the serving trace twice on one GPU: through the request loop
+    (FP32 factors, concurrent slots, resident geometries, admission under a
+    150 GiB budget) and as the plain FP64 path (one request at a time, each
+    geometry built for its request).  Latency = submit -> solution on the host."""
+    import hodlrnd_gb300 as h
+    from hodlrnd_gb300.server import Server
+
+    reqs = serving_trace(args.requests, SEED + 5, args.pool)
+    pts_cache = {}
+
+    def points(g):
+        if g["key"] not in pts_cache:
+            pts_cache[g["key"]] = np.random.default_rng(g["seed"]).uniform(0.0, 1.0, (g["n"], g["d"]))
+        return pts_cache[g["key"]]
+
+    def kernel(g):
+        return h.Kernel(g["kind"], 1.0 / g["n"] ** ((g["d"] - 1) / g["d"]), 1.0)
+
+    def rhs(r):
+        return np.random.default_rng(r["seed"]).standard_normal((r["geo"]["n"], r["nrhs"]))
+
+    for r in reqs:  # inputs prepared before the clock starts
+        points(r["geo"])
+        r["b"] = rhs(r)
+
+    def replay(slots, precision, resident):
+        srv = Server(slots=slots, memory_budget_bytes=150 << 30)
+        tickets = []
+        t0 = time.perf_counter()
+        for r in reqs:
+            delay = t0 + r["t"] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            g = r["geo"]
+            box = ([0.0] * g["d"], [1.0] * g["d"])
+            key = g["key"] if resident else 0
+            tickets.append(srv.submit(points(g), r["b"], kernel(g), box=box, key=key, ndim=g["d"], Nmax=64,
+                                      eps_ACA=EPS, tol=EPS, precision=precision, max_iter=SERVING_MAX_ITER))
+        lat, res, worst, unconv = [], [], 0.0, 0
+        for tk in tickets:
+            x, info = srv.wait(tk)
+            lat.append(info["t_total_s"])
+            res.append(info)
+            if info["status"] == 0:
+                worst = max(worst, info["rel_residual"])
+            else:
+                unconv += 1
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        nrhs = sum(r["nrhs"] for r in reqs)
+        return {"solves_per_s": round(nrhs / wall, 3), "requests_per_s": round(len(reqs) / wall, 3),
+                "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 2),
+                "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 2), "wall_s": round(wall, 3),
+                "worst_rel_residual_converged": worst, "not_converged_requests": unconv, "builds": st["builds"], "resident_hits": st["resident_hits"],
+                "evictions": st["evictions"],
+                "prediction_over_actual": round(float(np.median([i["predicted_bytes"] / i["actual_bytes"]
+                                                                 for i in res if i["built"]])), 3)}
+
+    served = replay(args.slots, "fp32_factors", True)
+    plain = replay(1, "fp64", False)
+    out = {"metric": "served solves/s and p50/p99 latency (serving trace)", "value": served["solves_per_s"],
+           "unit": "solves/s", "n_gpus": 1, "higher_is_better": True, "dtype": "fp32+fp64", "data": "synthetic",
+           "config": {"workload": f"serving trace: {len(reqs)} requests, Poisson arrivals at 200/s, {args.pool} "
+                                  "geometries (NDIM 2-3, N log-uniform 4096-262144, 1/r, log r, exp(-r)), 1-16 RHS, "
+                                  "tol 1e-8, budget 150 GiB",
+                      "slots": args.slots},
+           "served": served, "plain_fp64_one_at_a_time": plain}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -423,10 +521,17 @@ def main():
     ap.add_argument("--other-steps", type=int, default=3)
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["solve", "serving"], default="solve",
+                    help="serving: replay the request trace through the request loop (its own JSON line)")
+    ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--pool", type=int, default=12)
+    ap.add_argument("--slots", type=int, default=4)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")
-    if args.impl == "reference":
+    if args.workload == "serving":
+        run_serving(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gb300(args)

@@ -19,6 +19,7 @@ HODLR_ERR_TREE = 6
 HODLR_ERR_STATE = 7
 HODLR_ERR_DEVICE = 8
 HODLR_ERR_IO = 9
+HODLR_ERR_TIMEOUT = 10
 
 HODLR_KERNEL_INV_R = 1
 HODLR_KERNEL_INV_R2 = 2
@@ -29,13 +30,21 @@ HODLR_PREC_FP64 = 0
 HODLR_PREC_MIXED = 1
 HODLR_PREC_FP32_FACTORS = 2
 
+HODLR_ORTHO_AUTO = 0
+HODLR_ORTHO_MGS = 1
+HODLR_ORTHO_CGS2 = 2
+
+HODLR_RELAX_AUTO = 0
+HODLR_RELAX_OFF = 1
+
 
 class HodlrParams(ctypes.Structure):
     _fields_ = [("ndim", ctypes.c_int32), ("nmax", ctypes.c_int32), ("dprime", ctypes.c_int32),
                 ("restart", ctypes.c_int32), ("eps_aca", ctypes.c_double), ("tol", ctypes.c_double),
                 ("max_iter", ctypes.c_int64), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("device_budget_bytes", ctypes.c_uint64), ("rank_cap", ctypes.c_int32),
-                ("max_outer", ctypes.c_int32), ("inner_tol", ctypes.c_double)]
+                ("max_outer", ctypes.c_int32), ("inner_tol", ctypes.c_double), ("ortho", ctypes.c_int32),
+                ("relax", ctypes.c_int32)]
 
 
 class HodlrKernelDesc(ctypes.Structure):

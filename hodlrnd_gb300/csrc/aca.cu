@@ -63,8 +63,11 @@ struct AcaTeam {
   double *U, *V;
   uint32_t *rb, *cb;
   int32_t *rl, *cl;
+  KernelDev K;
 
   __device__ AcaTeam(const AcaArgs& a_, const AcaBlockDesc& B_, Team tm_) : a(a_), B(B_), tm(tm_) {
+    K = a.K;
+    if (B.kscale != 0.0) K.scale = B.kscale;
     m = B.m;
     n = B.n;
     cap = B.cap;
@@ -167,7 +170,7 @@ struct AcaTeam {
     double ba = -1.0, bv = 0.0, v0 = 0.0, s = 0.0;
     int bi = 0x7fffffff;
     for (int j = tm.tid(); j < n; j += Team::kSize) {
-      double val = kernel_entry<D>(a.P, a.K, pi, a.lmap[B.s_map + j], xi);
+      double val = kernel_entry<D>(a.P, K, pi, a.lmap[B.s_map + j], xi);
       for (int k = 0; k < r; k++) val = __dsub_rn(val, __dmul_rn(U[i0 + int64_t(k) * m], V[j + int64_t(k) * n]));
       V[j + int64_t(r) * n] = val;
       s += val * val;
@@ -204,7 +207,7 @@ struct AcaTeam {
       double xi[D];
       const int64_t pi = a.lmap[B.t_map + i];
       load_point<D>(a.P, pi, xi);
-      double val = kernel_entry<D>(a.P, a.K, pi, pj, xi);
+      double val = kernel_entry<D>(a.P, K, pi, pj, xi);
       for (int k = 0; k < r; k++) val = __dsub_rn(val, __dmul_rn(V[j0 + int64_t(k) * n], U[i + int64_t(k) * m]));
       U[i + int64_t(r) * m] = val;
       s += val * val;

@@ -20,6 +20,8 @@ struct AcaBlockDesc {
   int64_t bits;              // offset (words) of the row bitmap followed by the column bitmap
   int64_t lists;             // offset (int32) of the used-row list (cap+2) then the used-column list (cap+2)
   uint64_t seed;             // restart-heuristic generator seed
+  double kscale;             // kernel scale of this block's operator; 0: AcaArgs::K.scale (batched builds
+                             // run blocks of several operators in one launch)
 };
 
 struct AcaOut {

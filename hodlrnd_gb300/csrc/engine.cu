@@ -169,9 +169,24 @@ struct Plan {
   int nzfix = 0;
   PanelFix* pfix_far = nullptr;
   int npfix_far = 0;
+  PanelFix* pfix_near = nullptr;  // near panels above 32 rows split over items (share ypart with the far ones)
+  int npfix_near = 0;
+  int64_t nypart_near = 0;
   int64_t nzpart = 0, nypart = 0;  // partial-sum scratch (elements of the vector type)
   void* zpart = nullptr;
   void* ypart = nullptr;
+  // host copies of the arrays above, kept for operators of a batch (merged
+  // into the batch's plan)
+  struct Host {
+    std::vector<Panel> panels_near, panels_far;
+    std::vector<Seg> segs_near, segs_far;
+    std::vector<Item> small_near, big_near, small_far, big_far;
+    std::vector<PanelFix> pfix_near, pfix_far;
+    std::vector<ZBlock> zb;
+    std::vector<ZItem> zitems;
+    std::vector<ZFix> zfix;
+  };
+  std::shared_ptr<Host> host;
 };
 
 }  // namespace
@@ -184,6 +199,11 @@ struct hodlr_ctx {
 
 struct hodlr_op {
   hodlr_ctx* ctx = nullptr;
+  bool keep_host_plans = false;  // set for the operators of a batch
+  bool batch_owned = false;      // freed by hodlr_batch_destroy only
+  bool relaxed = false;  // FP32 factors: matvecs use relaxed accumulation (set by the solver)
+  unsigned int* h_waits = nullptr;  // pinned: streaming-kernel wait give-ups (read_stream_timeouts)
+  unsigned int waits_seen = 0;
   hodlr_params p;
   hodlr_kernel_desc kd;
   Tree tree;
@@ -225,6 +245,7 @@ struct hodlr_op {
     gmres_free(g64);
     gmres_free(g32);
     if (h_scal) cudaFreeHost(h_scal);
+    if (h_waits) cudaFreeHost(h_waits);
     mem.release_all();
   }
 };
@@ -291,12 +312,37 @@ NearTiles near_tiles(const Tree& t, const NearList& nl, int esz) {
   return out;
 }
 
+// Columns one panel item takes before its panel chunk is split over items:
+// far panels above 32 rows are many (one per node and level), near ones are
+// few (leaves above 32 points) and get more, smaller items.
+constexpr int kPanelCols = 256;
+constexpr int kNearPanelCols = 48;
+
+// Runs of consecutive segments [begin, end) with about `max_cols` columns each.
+std::vector<std::pair<int32_t, int32_t>> column_groups(const std::vector<Seg>& segs, int64_t begin, int64_t end,
+                                                       int max_cols) {
+  std::vector<std::pair<int32_t, int32_t>> groups;
+  int32_t gb = int32_t(begin), cols = 0;
+  for (int64_t q = begin; q < end; q++) {
+    if (cols > 0 && cols + segs[size_t(q)].K > max_cols) {
+      groups.push_back({gb, int32_t(q)});
+      gb = int32_t(q);
+      cols = 0;
+    }
+    cols += segs[size_t(q)].K;
+  }
+  groups.push_back({gb, int32_t(end)});
+  return groups;
+}
+
 void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a, Plan& plan, cudaStream_t st) {
   const Tree& t = op->tree;
   const int L = t.levels - 1;
   std::vector<Panel> panels;
   std::vector<Seg> segs;
   std::vector<Item> small, big;
+  std::vector<PanelFix> pfix;
+  int64_t nypart = 0;
   const size_t esz = a == Prec::kD ? 8 : 4;
   size_t q = 0;
   for (int64_t k = 0; k + 1 < int64_t(op->near.leaf_ptr.size()); k++) {
@@ -306,6 +352,7 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
     p.row_begin = t.begin[size_t(t.gid(L, k))];
     p.m = int32_t(t.count[size_t(t.gid(L, k))]);
     p.slot = 0;
+    p.yoff = p.row_begin;
     p.seg_begin = int64_t(segs.size());
     for (int64_t z = b; z < e; z++, q++) {
       const TileDesc& d = nt.tiles[q];
@@ -322,11 +369,23 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
     if (p.m <= 32) {
       small.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
     } else {
+      // as for far panels: runs of about kPanelCols columns per item, partial
+      // row blocks added by the fix-up kernel
+      const std::vector<std::pair<int32_t, int32_t>> groups = column_groups(segs, p.seg_begin, p.seg_end, kNearPanelCols);
       const int rows = rows_per_item(a);
-      for (int c = 0; c < int((p.m + rows - 1) / rows); c++)
-        big.push_back({np, c, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+      for (int c = 0; c < int((p.m + rows - 1) / rows); c++) {
+        if (groups.size() == 1) {
+          big.push_back({np, c, groups[0].first, groups[0].second, -1});
+          continue;
+        }
+        pfix.push_back({np, c, int32_t(nypart), int32_t(groups.size())});
+        for (auto& g : groups) big.push_back({np, c, g.first, g.second, int32_t(nypart++)});
+      }
     }
   }
+  plan.pfix_near = upload(op->mem, pfix, st, "near panel fix-ups");
+  plan.npfix_near = int(pfix.size());
+  plan.nypart_near = nypart * rows_per_item(a);
   plan.a_near = a;
   plan.panels_near = upload(op->mem, panels, st, "near panels");
   plan.segs_near = upload(op->mem, segs, st, "near segments");
@@ -334,10 +393,15 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
   plan.big_near = upload(op->mem, big, st, "near items");
   plan.nsmall_near = int(small.size());
   plan.nbig_near = int(big.size());
+  if (op->keep_host_plans) {
+    if (!plan.host) plan.host = std::make_shared<Plan::Host>();
+    plan.host->panels_near = panels;
+    plan.host->segs_near = segs;
+    plan.host->small_near = small;
+    plan.host->big_near = big;
+    plan.host->pfix_near = pfix;
+  }
 }
-
-// Columns one far-panel item takes before its panel chunk is split over items.
-constexpr int kPanelCols = 256;
 
 // Far-field plan from the per-block storage pointers.
 void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const std::vector<const void*>& vptr, Prec a,
@@ -361,6 +425,7 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
     p.row_begin = t.begin[size_t(gt)];
     p.m = int32_t(t.count[size_t(gt)]);
     p.slot = l;
+    p.yoff = int64_t(l) * op->n + p.row_begin;
     p.seg_begin = int64_t(segs.size());
     for (size_t q = b; q < e; q++) {
       const int64_t gs = t.gid(l, op->far[q].s);
@@ -394,18 +459,7 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
       if (p.m <= 32) {
         small.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
       } else {
-        // runs of segments with about kPanelCols columns each bound one item's work
-        std::vector<std::pair<int32_t, int32_t>> groups;
-        int32_t gb = int32_t(p.seg_begin), cols = 0;
-        for (int64_t q = p.seg_begin; q < p.seg_end; q++) {
-          if (cols > 0 && cols + segs[size_t(q)].K > kPanelCols) {
-            groups.push_back({gb, int32_t(q)});
-            gb = int32_t(q);
-            cols = 0;
-          }
-          cols += segs[size_t(q)].K;
-        }
-        groups.push_back({gb, int32_t(p.seg_end)});
+        const std::vector<std::pair<int32_t, int32_t>> groups = column_groups(segs, p.seg_begin, p.seg_end, kPanelCols);
         const int rows = rows_per_item(a);
         const int chunks = int((p.m + rows - 1) / rows);
         for (int c = 0; c < chunks; c++) {
@@ -463,36 +517,73 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   plan.npfix_far = int(pfix.size());
   plan.nzpart = nzpart;
   plan.nypart = nypart * rows_per_item(a);
+  if (op->keep_host_plans) {
+    if (!plan.host) plan.host = std::make_shared<Plan::Host>();
+    plan.host->panels_far = panels;
+    plan.host->segs_far = segs;
+    plan.host->small_far = small;
+    plan.host->big_far = big;
+    plan.host->pfix_far = pfix;
+    plan.host->zb = zb;
+    plan.host->zitems = zit;
+    plan.host->zfix = zfix;
+  }
 }
 
-// ACA of every far block, in workspace-bounded batches; compacted factors go
-// to per-batch chunks (FP64 or FP32) and uptr/vptr record where.
-void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std::vector<const void*>& vptr) {
-  const Tree& t = op->tree;
-  const size_t nb = op->far.size();
-  op->rank.assign(nb, 0);
-  op->dense.assign(nb, 0);
-  uptr.assign(nb, nullptr);
-  vptr.assign(nb, nullptr);
-  if (nb == 0) return;
-  const Prec fp = op->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
-  const size_t esz = fp == Prec::kD ? 8 : 4;
-  const int cap0 = op->p.rank_cap > 0 ? op->p.rank_cap : 64;
-  std::vector<int32_t> cap(nb);
-  std::vector<int32_t> mm(nb), nn(nb);
-  std::vector<int64_t> tb(nb), sb(nb);
-  for (size_t b = 0; b < nb; b++) {
-    const int64_t gt = t.gid(op->far[b].level, op->far[b].t), gs = t.gid(op->far[b].level, op->far[b].s);
-    mm[b] = int32_t(t.count[size_t(gt)]);
-    nn[b] = int32_t(t.count[size_t(gs)]);
-    tb[b] = t.begin[size_t(gt)];
-    sb[b] = t.begin[size_t(gs)];
-    cap[b] = std::min({mm[b], nn[b], cap0});
+// ACA of every far block of the given operators (one, or the instances of a
+// batch: their blocks share every launch), in workspace-bounded batches;
+// compacted factors go to per-batch chunks of each operator's memory (FP64 or
+// FP32) and op->uptr / op->vptr record where.  With several operators their
+// points and reference-order maps are concatenated for the launches, and each
+// block carries its operator's kernel scale.
+void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
+  const size_t nops = ops.size();
+  hodlr_op* op0 = ops[0];
+  const bool joint = nops > 1;
+  std::vector<int64_t> pbase(nops, 0), lbase(nops, 0), boff(nops + 1, 0);
+  for (size_t j = 0; j < nops; j++) {
+    hodlr_op* op = ops[j];
+    const size_t nb = op->far.size();
+    op->rank.assign(nb, 0);
+    op->dense.assign(nb, 0);
+    op->uptr.assign(nb, nullptr);
+    op->vptr.assign(nb, nullptr);
+    boff[j + 1] = boff[j] + int64_t(nb);
+    if (j + 1 < nops) {
+      pbase[j + 1] = pbase[j] + op->n;
+      lbase[j + 1] = lbase[j] + int64_t(op->tree.levels) * op->n;
+    }
   }
-  auto ws_need = [&](size_t b) { return uint64_t(cap[b]) * uint64_t(mm[b] + nn[b]); };
+  const size_t nb = size_t(boff[nops]);
+  if (nb == 0) return;
+  const int ndim = op0->p.ndim;
+  const Prec fp = op0->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
+  const size_t esz = fp == Prec::kD ? 8 : 4;
+  const int cap0 = op0->p.rank_cap > 0 ? op0->p.rank_cap : 64;
+  // global block g = boff[j] + b: operator j, its far block b
+  std::vector<int32_t> job(nb), cap(nb), mm(nb), nn(nb);
+  std::vector<int64_t> tb(nb), sb(nb), tmap(nb), smap(nb);
+  for (size_t j = 0; j < nops; j++) {
+    const hodlr_op* op = ops[j];
+    const Tree& t = op->tree;
+    for (size_t b = 0; b < op->far.size(); b++) {
+      const size_t g = size_t(boff[j]) + b;
+      const FarBlock& f = op->far[b];
+      const int64_t gt = t.gid(f.level, f.t), gs = t.gid(f.level, f.s);
+      job[g] = int32_t(j);
+      mm[g] = int32_t(t.count[size_t(gt)]);
+      nn[g] = int32_t(t.count[size_t(gs)]);
+      tb[g] = pbase[j] + t.begin[size_t(gt)];
+      sb[g] = pbase[j] + t.begin[size_t(gs)];
+      tmap[g] = lbase[j] + int64_t(f.level) * op->n + t.begin[size_t(gt)];
+      smap[g] = lbase[j] + int64_t(f.level) * op->n + t.begin[size_t(gs)];
+      cap[g] = std::min({mm[g], nn[g], cap0});
+    }
+  }
+  auto ws_need = [&](size_t g) { return uint64_t(cap[g]) * uint64_t(mm[g] + nn[g]); };
   // Scratch of one batch: the FP64 workspace is bounded (4 GiB by default);
   // a single block that needs more grows it.  Not counted against the
-  // operator's memory: it is freed when the build returns.
+  // operators' memory: it is freed when the build returns.
   const size_t max_batch = 1 << 20;
   struct Scratch {
     void* p = nullptr;
@@ -510,7 +601,7 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
       bytes = need;
     }
   };
-  Scratch s_ws, s_bits, s_lists, s_desc, s_out, s_idx, s_cd;
+  Scratch s_ws, s_bits, s_lists, s_desc, s_out, s_idx, s_cd, s_pts, s_lmap;
   const uint64_t ws_doubles = uint64_t(1) << 29;
   const uint64_t bits_room = uint64_t(1) << 26, list_room = uint64_t(1) << 26;
   s_desc.ensure(max_batch * sizeof(AcaBlockDesc), st, "ACA descriptors");
@@ -521,15 +612,35 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
   AcaOut* d_out = static_cast<AcaOut*>(s_out.p);
   int32_t* d_lists_idx = static_cast<int32_t*>(s_idx.p);
   CompactDesc* d_cd = static_cast<CompactDesc*>(s_cd.p);
+  // points and reference-order maps of the launches
+  PointsDev P{op0->d_pts, op0->n};
+  const int32_t* d_lmap = op0->d_lmap;
+  if (joint) {
+    const int64_t ntot = pbase[nops - 1] + ops[nops - 1]->n;
+    s_pts.ensure(size_t(ntot) * size_t(ndim) * sizeof(double), st, "batch points");
+    double* jp = static_cast<double*>(s_pts.p);
+    std::vector<int32_t> jl;
+    jl.reserve(size_t(lbase[nops - 1] + int64_t(ops[nops - 1]->tree.levels) * ops[nops - 1]->n));
+    for (size_t j = 0; j < nops; j++) {
+      for (int k = 0; k < ndim; k++)
+        CK(cudaMemcpyAsync(jp + int64_t(k) * ntot + pbase[j], ops[j]->d_pts + int64_t(k) * ops[j]->n,
+                           sizeof(double) * size_t(ops[j]->n), cudaMemcpyDeviceToDevice, st));
+      for (int32_t v : reference_order_map(ops[j]->tree)) jl.push_back(int32_t(v + pbase[j]));
+    }
+    s_lmap.ensure(jl.size() * sizeof(int32_t), st, "batch reference-order maps");
+    CK(cudaMemcpyAsync(s_lmap.p, jl.data(), jl.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    P = PointsDev{jp, ntot};
+    d_lmap = static_cast<const int32_t*>(s_lmap.p);
+  }
   std::vector<size_t> todo(nb);
-  for (size_t b = 0; b < nb; b++) todo[b] = b;
+  for (size_t g = 0; g < nb; g++) todo[g] = g;
   // large blocks first keeps the CTA-team launch ahead of the warp teams
   std::stable_sort(todo.begin(), todo.end(), [&](size_t a, size_t b) {
     return std::max(mm[a], nn[a]) > std::max(mm[b], nn[b]);
   });
 
-  PointsDev P{op->d_pts, op->n};
-  KernelDev K{op->kd.kind, op->kd.scale, op->kd.diag};
+  KernelDev K{op0->kd.kind, op0->kd.scale, op0->kd.diag};
   size_t pos = 0;
   std::vector<size_t> retry;
   std::vector<AcaBlockDesc> desc;
@@ -540,13 +651,13 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
     // next batch
     std::vector<size_t> batch;
     uint64_t acc_w = 0, acc_b = 0, acc_l = 0;
-    auto take = [&](size_t b) {
-      const uint64_t w = ws_need(b), bw = uint64_t((mm[b] + 31) / 32 + (nn[b] + 31) / 32),
-                     lw = uint64_t(2 * (cap[b] + 2));
+    auto take = [&](size_t g) {
+      const uint64_t w = ws_need(g), bw = uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32),
+                     lw = uint64_t(2 * (cap[g] + 2));
       if (!batch.empty() && (acc_w + w > ws_doubles || acc_b + bw > bits_room || acc_l + lw > list_room ||
                              batch.size() >= max_batch))
         return false;
-      batch.push_back(b);
+      batch.push_back(g);
       acc_w += w;
       acc_b += bw;
       acc_l += lw;
@@ -554,8 +665,8 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
     };
     if (!retry.empty()) {
       std::vector<size_t> rest;
-      for (size_t b : retry)
-        if (!take(b)) rest.push_back(b);
+      for (size_t g : retry)
+        if (!take(g)) rest.push_back(g);
       retry.swap(rest);
     } else {
       while (pos < todo.size() && take(todo[pos])) pos++;
@@ -565,22 +676,25 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
     cta_list.clear();
     uint64_t ow = 0, ob = 0, ol = 0;
     for (size_t q = 0; q < batch.size(); q++) {
-      const size_t b = batch[q];
+      const size_t g = batch[q];
+      const hodlr_op* op = ops[size_t(job[g])];
+      const FarBlock& f = op->far[size_t(int64_t(g) - boff[size_t(job[g])])];
       AcaBlockDesc& d = desc[q];
-      d.t_map = int64_t(op->far[b].level) * op->n + tb[b];
-      d.s_map = int64_t(op->far[b].level) * op->n + sb[b];
-      d.m = mm[b];
-      d.n = nn[b];
-      d.cap = cap[b];
+      d.t_map = tmap[g];
+      d.s_map = smap[g];
+      d.m = mm[g];
+      d.n = nn[g];
+      d.cap = cap[g];
       d.pad = 0;
       d.ws = int64_t(ow);
       d.bits = int64_t(ob);
       d.lists = int64_t(ol);
-      d.seed = block_seed(op->far[b].level, op->far[b].t, op->far[b].s);
-      ow += ws_need(b);
-      ob += uint64_t((mm[b] + 31) / 32 + (nn[b] + 31) / 32);
-      ol += uint64_t(2 * (cap[b] + 2));
-      (std::max(mm[b], nn[b]) <= 256 ? warp_list : cta_list).push_back(int32_t(q));
+      d.seed = block_seed(f.level, f.t, f.s);
+      d.kscale = joint ? op->kd.scale : 0.0;
+      ow += ws_need(g);
+      ob += uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32);
+      ol += uint64_t(2 * (cap[g] + 2));
+      (std::max(mm[g], nn[g]) <= 256 ? warp_list : cta_list).push_back(int32_t(q));
     }
     std::vector<int32_t> lst(cta_list);
     lst.insert(lst.end(), warp_list.begin(), warp_list.end());
@@ -591,66 +705,74 @@ void run_aca(hodlr_op* op, cudaStream_t st, std::vector<const void*>& uptr, std:
     CK(cudaMemcpyAsync(d_desc, desc.data(), desc.size() * sizeof(AcaBlockDesc), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(d_lists_idx, lst.data(), lst.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     AcaArgs a;
-    a.lmap = op->d_lmap;
+    a.lmap = d_lmap;
     a.P = P;
     a.K = K;
-    a.tol = op->p.eps_aca;
+    a.tol = op0->p.eps_aca;
     a.blocks = d_desc;
     a.ws = ws;
     a.bits = static_cast<uint32_t*>(s_bits.p);
     a.lists = static_cast<int32_t*>(s_lists.p);
     a.out = d_out;
-    CK(launch_aca(op->p.ndim, a, d_lists_idx + cta_list.size(), int(warp_list.size()), d_lists_idx,
-                  int(cta_list.size()), st));
+    CK(launch_aca(ndim, a, d_lists_idx + cta_list.size(), int(warp_list.size()), d_lists_idx, int(cta_list.size()),
+                  st));
     out.resize(batch.size());
     CK(cudaMemcpyAsync(out.data(), d_out, out.size() * sizeof(AcaOut), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    // compaction of the finished blocks into one chunk
+    // compaction of the finished blocks: one chunk per operator and batch
     cds.clear();
-    uint64_t bytes = 0;
-    std::vector<uint64_t> off(batch.size());
+    std::vector<uint64_t> bytes(nops, 0), off(batch.size(), 0);
     for (size_t q = 0; q < batch.size(); q++) {
-      const size_t b = batch[q];
+      const size_t g = batch[q];
       if (out[q].flags & kAcaOverflow) {
-        cap[b] = std::min(std::min(mm[b], nn[b]), cap[b] * 4);
-        retry.push_back(b);
+        cap[g] = std::min(std::min(mm[g], nn[g]), cap[g] * 4);
+        retry.push_back(g);
         continue;
       }
+      hodlr_op* op = ops[size_t(job[g])];
+      const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
       op->rank[b] = out[q].rank;
       op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
-      off[q] = bytes;
+      off[q] = bytes[size_t(job[g])];
       const int64_t r = op->rank[b];
-      const uint64_t ub = (uint64_t(stored_elems(mm[b], op->dense[b] ? nn[b] : r, int(esz))) * esz + 15) / 16 * 16;
-      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(nn[b]) * uint64_t(vpad(r, int(esz))) * esz + 15) / 16 * 16;
-      bytes += ub + vb;
+      const uint64_t ub = (uint64_t(stored_elems(mm[g], op->dense[b] ? nn[g] : r, int(esz))) * esz + 15) / 16 * 16;
+      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(nn[g]) * uint64_t(vpad(r, int(esz))) * esz + 15) / 16 * 16;
+      bytes[size_t(job[g])] += ub + vb;
     }
-    if (bytes > 0) {
-      char* chunk = static_cast<char*>(op->mem.alloc(bytes, "far-field factors"));
-      CK(cudaMemsetAsync(chunk, 0, bytes, st));  // tile padding rows must read as zero
-      for (size_t q = 0; q < batch.size(); q++) {
-        const size_t b = batch[q];
-        if (out[q].flags & kAcaOverflow) continue;
-        CompactDesc c;
-        c.t_begin = tb[b];
-        c.s_begin = sb[b];
-        c.t_map = desc[q].t_map;
-        c.s_map = desc[q].s_map;
-        c.ws = desc[q].ws;
-        c.u_dst = chunk + off[q];
-        c.v_dst = chunk + off[q] +
-                  (uint64_t(stored_elems(mm[b], std::max(op->rank[b], 0), int(esz))) * esz + 15) / 16 * 16;
-        c.m = mm[b];
-        c.n = nn[b];
-        c.rank = op->rank[b];
-        c.dense = op->dense[b];
-        c.cap = desc[q].cap;
-        c.pad = 0;
-        uptr[b] = c.u_dst;
-        vptr[b] = c.v_dst;
-        if (op->dense[b] || op->rank[b] > 0) cds.push_back(c);
+    std::vector<char*> chunk(nops, nullptr);
+    for (size_t j = 0; j < nops; j++)
+      if (bytes[j] > 0) {
+        chunk[j] = static_cast<char*>(ops[j]->mem.alloc(bytes[j], "far-field factors"));
+        CK(cudaMemsetAsync(chunk[j], 0, bytes[j], st));  // tile padding rows must read as zero
       }
+    for (size_t q = 0; q < batch.size(); q++) {
+      const size_t g = batch[q];
+      if (out[q].flags & kAcaOverflow) continue;
+      hodlr_op* op = ops[size_t(job[g])];
+      const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
+      char* ch = chunk[size_t(job[g])];
+      CompactDesc c;
+      c.t_begin = tb[g];
+      c.s_begin = sb[g];
+      c.t_map = desc[q].t_map;
+      c.s_map = desc[q].s_map;
+      c.ws = desc[q].ws;
+      c.u_dst = ch + off[q];
+      c.v_dst = ch + off[q] + (uint64_t(stored_elems(mm[g], std::max(op->rank[b], 0), int(esz))) * esz + 15) / 16 * 16;
+      c.m = mm[g];
+      c.n = nn[g];
+      c.rank = op->rank[b];
+      c.dense = op->dense[b];
+      c.cap = desc[q].cap;
+      c.pad = 0;
+      c.kscale = desc[q].kscale;
+      op->uptr[b] = c.u_dst;
+      op->vptr[b] = c.v_dst;
+      if (op->dense[b] || op->rank[b] > 0) cds.push_back(c);
+    }
+    if (!cds.empty()) {
       CK(cudaMemcpyAsync(d_cd, cds.data(), cds.size() * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
-      CK(launch_compact(op->p.ndim, P, K, ws, op->d_lmap, d_cd, int(cds.size()), fp, st));
+      CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(cds.size()), fp, st));
       CK(cudaStreamSynchronize(st));
     }
   }
@@ -747,28 +869,30 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
   Tracer& tr = op->tr;
   if (plan.nzb > 0) tr.start(kb + 0, st);
-  // FP32 factors with FP64 vectors: compensated FP32 accumulation on split inputs
+  // FP32 factors with FP64 vectors: compensated (or, while the solver allows
+  // it, relaxed) FP32 accumulation on split inputs
   const bool df = plan.a_far == Prec::kF && px == Prec::kD;
+  const Accum acc = !df ? Accum::kByType : op->relaxed ? Accum::kRelaxed : Accum::kCompensated;
   void* fin = in;
   if (df) {
     fin = op->d_in2;
     if ((e = launch_split(reinterpret_cast<const double*>(in), fin, n, st)) != cudaSuccess) return e;
   }
   if ((e = launch_zgemv(plan.a_far, px, plan.zb, plan.zitems, plan.nzitems, plan.zfix, plan.nzfix, plan.zpart, fin, ldin,
-                        1, st, df)) != cudaSuccess)
+                        1, st, acc)) != cudaSuccess)
     return e;
   if (plan.nzb > 0) tr.stop(st);
   tr.start(kb + 1, st);
   if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.small_near, plan.nsmall_near,
-                         plan.big_near, plan.nbig_near, nullptr, 0, nullptr, in, ldin, yslots, n, op->nslots, 1, st)) !=
-      cudaSuccess)
+                         plan.big_near, plan.nbig_near, plan.pfix_near, plan.npfix_near, plan.ypart, in, ldin, yslots, n,
+                         op->nslots, 1, st)) != cudaSuccess)
     return e;
   tr.stop(st);
   const bool far = plan.nsmall_far + plan.nbig_far > 0;
   if (far) tr.start(kb + 2, st);
   if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.small_far, plan.nsmall_far, plan.big_far,
                          plan.nbig_far, plan.pfix_far, plan.npfix_far, plan.ypart, fin, ldin, yslots, n, op->nslots, 1,
-                         st, df)) != cudaSuccess)
+                         st, acc)) != cudaSuccess)
     return e;
   if (far) tr.stop(st);
   tr.start(kb + 3, st);
@@ -781,6 +905,12 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
 __global__ void axpy_f2d_kernel(double* x, const float* d, int64_t n) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
     x[i] = x[i] + double(d[i]);
+}
+
+Ortho ortho_of(const hodlr_params& p) {
+  if (p.ortho == HODLR_ORTHO_MGS) return Ortho::kMGS;
+  if (p.ortho == HODLR_ORTHO_CGS2) return Ortho::kCGS2;
+  return p.precision == HODLR_PREC_FP64 ? Ortho::kMGS : Ortho::kCGS2;
 }
 
 // Solve in tree order on device buffers b, x (one right-hand side).
@@ -798,12 +928,48 @@ void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr
       return apply_tree<double>(op, op->plan64, xi, yo, op->d_in64, op->d_y64, st);
     };
     GmresResult r;
-    CK(gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter, tol, st, &r));
+    // FP32 factors: relaxed accumulation once the residual estimate is below
+    // tol * 1e6 -- an inexact Krylov method may take products with relative
+    // error up to about tol / |r_k| (Simoncini and Szyld, SIAM J. Sci.
+    // Comput. 25 (2003); Bouras and Fraysse, SIAM J. Matrix Anal. Appl. 26
+    // (2005)), and relaxed products are accurate to about 1e-6 -- then the
+    // true residual with compensated products decides, and GMRES continues
+    // from x with compensated products while it is above tol.
+    const bool relax = p.precision == HODLR_PREC_FP32_FACTORS && p.relax != HODLR_RELAX_OFF;
+    const double relax_at = std::min(1.0, tol * 1e6);
+    std::function<void(double)> progress;
+    if (relax) progress = [op, relax_at](double res) { op->relaxed = res < relax_at; };
+    op->relaxed = false;
+    const cudaError_t ge = gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter, tol, st, &r, ortho_of(p),
+                                               progress);
+    op->relaxed = false;
+    CK(ge);
+    int64_t its = r.iterations;
+    int sweeps = 1;
+    double res = r.resid;
+    bool conv = r.converged;
+    if (relax && conv) {
+      for (;;) {
+        // |b - A x| / |b| with compensated products
+        CK(apply_tree<double>(op, op->plan64, x, op->d_io2, op->d_in64, op->d_y64, st));
+        CK(vec_sub_norm2<double>(b, op->d_io2, op->d_r64, op->n, op->d_part, op->d_scal + 1, st));
+        CK(vec_norm2<double>(b, op->n, op->d_part, op->d_scal + 2, st));
+        CK(cudaMemcpyAsync(op->h_scal, op->d_scal, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        res = op->h_scal[1] / (op->h_scal[2] == 0.0 ? 1.0 : op->h_scal[2]);
+        if (res <= tol || sweeps >= 4 || its >= max_iter) break;
+        GmresResult r2;
+        CK(gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter - its, tol, st, &r2, ortho_of(p)));
+        its += r2.iterations;
+        sweeps++;
+      }
+      conv = res <= tol;
+    }
     CK(cudaStreamSynchronize(st));
-    info->iterations = r.iterations;
-    info->outer_iterations = 1;
-    info->rel_residual = r.resid;
-    info->converged = r.converged ? 1 : 0;
+    info->iterations = its;
+    info->outer_iterations = sweeps;
+    info->rel_residual = res;
+    info->converged = conv ? 1 : 0;
   } else {
     // FP64 iterative refinement around FP32 GMRES on the FP32 operator
     const int max_outer = p.max_outer > 0 ? p.max_outer : 10;
@@ -831,7 +997,7 @@ void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr
       double sweep_tol = inner_tol;
       if (outer > 0) sweep_tol = std::min(inner_tol, 0.3 * tol / rel);
       CK(gmres_solve<float>(op->g32, A32, op->d_r32, op->d_d32, true, restart, max_iter - inner_total,
-                            std::max(sweep_tol, tol), st, &r));
+                            std::max(sweep_tol, tol), st, &r, ortho_of(p)));
       inner_total += r.iterations;
       axpy_f2d_kernel<<<kVecCtas, 256, 0, st>>>(x, op->d_d32, n);
       CK(cudaGetLastError());
@@ -867,6 +1033,343 @@ int guarded(hodlr_ctx* ctx, const std::function<int()>& f) {
 
 // ================================================================= C ABI
 
+
+// State carried from build_prepare to build_finish.
+struct BuildState {
+  NearTiles nt, nt32;
+  double* near64 = nullptr;
+  float* near32 = nullptr;
+  double t0 = 0.0, t2 = 0.0;
+};
+
+// Tree, lists, points and the near field of `op` (op->p, op->kd, op->n set).
+void build_prepare(hodlr_op* op, const double* points, const double* box_lo, const double* box_hi, cudaStream_t st,
+                   BuildState& bs) {
+  const int64_t n = op->n;
+  const double t0 = bs.t0 = now_s();
+  TreeParams tp;
+  tp.ndim = op->p.ndim;
+  tp.nmax = op->p.nmax;
+  tp.dprime = op->p.dprime;
+  const std::string terr = build_tree(tp, points, n, box_lo, box_hi, op->tree);
+  if (!terr.empty())
+    throw Failure{terr.find("exceeds") != std::string::npos ? HODLR_ERR_TREE : HODLR_ERR_INVALID,
+                  "hodlr_build: " + terr};
+  op->far = far_blocks(op->tree);
+  op->near = near_blocks(op->tree);
+  op->nslots = op->tree.levels;
+  const double t1 = now_s();
+  op->st.t_tree_s = t1 - t0;
+  // points in tree order, structure of arrays
+  const int d = op->p.ndim;
+  std::vector<double> soa(size_t(n) * size_t(d));
+  for (int64_t i = 0; i < n; i++)
+    for (int k = 0; k < d; k++) soa[size_t(k) * size_t(n) + size_t(i)] = points[size_t(op->tree.perm[size_t(i)]) * d + k];
+  op->d_pts = upload(op->mem, soa, st, "points");
+  op->d_perm = upload(op->mem, op->tree.perm, st, "permutation");
+  op->d_lmap = upload(op->mem, reference_order_map(op->tree), st, "reference-order map");
+  // near field
+  bs.nt = near_tiles(op->tree, op->near, 8);
+  const NearTiles& nt = bs.nt;
+  PointsDev P{op->d_pts, n};
+  KernelDev K{op->kd.kind, op->kd.scale, op->kd.diag};
+  TileDesc* d_tiles = upload(op->mem, nt.tiles, st, "near tile descriptors");
+  double* near64 = bs.near64 = op->mem.alloc_n<double>(size_t(std::max<int64_t>(nt.total, 1)), "near field (FP64)");
+  CK(cudaMemsetAsync(near64, 0, sizeof(double) * size_t(std::max<int64_t>(nt.total, 1)), st));
+  CK(launch_assemble(d, P, K, d_tiles, int(nt.tiles.size()), near64, Prec::kD, st));
+  if (op->p.precision == HODLR_PREC_MIXED) {
+    bs.nt32 = near_tiles(op->tree, op->near, 4);
+    const NearTiles& nt32 = bs.nt32;
+    TileDesc* d_tiles32 = upload(op->mem, nt32.tiles, st, "near tile descriptors");
+    float* near32 = bs.near32 = op->mem.alloc_n<float>(size_t(std::max<int64_t>(nt32.total, 1)), "near field (FP32)");
+    CK(cudaMemsetAsync(near32, 0, sizeof(float) * size_t(std::max<int64_t>(nt32.total, 1)), st));
+    CK(launch_assemble(d, P, K, d_tiles32, int(nt32.tiles.size()), near32, Prec::kF, st));
+    CK(cudaStreamSynchronize(st));
+    op->mem.release(d_tiles32);
+  }
+  CK(cudaStreamSynchronize(st));
+  op->mem.release(d_tiles);
+  bs.t2 = now_s();
+  const double t2 = bs.t2;
+  op->st.t_near_s = t2 - t1;
+}
+
+// Plans, work vectors and statistics, once the far blocks are compressed.
+void build_finish(hodlr_op* op, BuildState& bs, cudaStream_t st) {
+  const int64_t n = op->n;
+  const std::vector<const void*>& uptr = op->uptr;
+  const std::vector<const void*>& vptr = op->vptr;
+  // plans
+  const Prec fp = op->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
+  build_near_plan(op, bs.nt, bs.near64, Prec::kD, op->plan64, st);
+  build_far_plan(op, uptr, vptr, fp, op->plan64, st);
+  if (op->p.precision == HODLR_PREC_MIXED) {
+    build_near_plan(op, bs.nt32, bs.near32, Prec::kF, op->plan32, st);
+    op->plan32.a_far = Prec::kF;
+    op->plan32.panels_far = op->plan64.panels_far;
+    op->plan32.segs_far = op->plan64.segs_far;
+    op->plan32.small_far = op->plan64.small_far;
+    op->plan32.big_far = op->plan64.big_far;
+    op->plan32.nsmall_far = op->plan64.nsmall_far;
+    op->plan32.nbig_far = op->plan64.nbig_far;
+    op->plan32.zb = op->plan64.zb;
+    op->plan32.nzb = op->plan64.nzb;
+    op->plan32.zitems = op->plan64.zitems;
+    op->plan32.nzitems = op->plan64.nzitems;
+    op->plan32.zfix = op->plan64.zfix;
+    op->plan32.nzfix = op->plan64.nzfix;
+    op->plan32.pfix_far = op->plan64.pfix_far;
+    op->plan32.npfix_far = op->plan64.npfix_far;
+    op->plan32.nzpart = op->plan64.nzpart;
+    op->plan32.nypart = std::max(op->plan64.nypart, op->plan32.nypart_near);
+    op->plan32.zpart = op->mem.alloc(size_t(std::max<int64_t>(op->plan32.nzpart, 1)) * 4, "z partial sums (FP32)");
+    op->plan32.ypart = op->mem.alloc(size_t(std::max<int64_t>(op->plan32.nypart, 1)) * 4, "row partial sums (FP32)");
+  }
+  op->plan64.nypart = std::max(op->plan64.nypart, op->plan64.nypart_near);
+  op->plan64.zpart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nzpart, 1)) * 8, "z partial sums");
+  op->plan64.ypart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nypart, 1)) * 8, "row partial sums");
+  // work vectors; the input buffers [x | z] end in 16 bytes of padding,
+  // which the streaming V^T x stage copies may read (a run of inputs is
+  // copied from the 16-byte boundary below it to the one above it)
+  const int64_t ldin = n + op->zlen;
+  op->d_in64 = static_cast<double*>(op->mem.alloc(size_t(ldin) * 8 + 16, "matvec input"));
+  if (op->p.precision != HODLR_PREC_FP64)
+    op->d_in2 = op->mem.alloc(size_t(ldin) * 8 + 16, "matvec input (FP32 pairs)");
+  op->d_y64 = op->mem.alloc_n<double>(size_t(n) * size_t(op->nslots), "matvec slots");
+  op->d_b64 = op->mem.alloc_n<double>(size_t(n), "rhs");
+  op->d_x64 = op->mem.alloc_n<double>(size_t(n), "solution");
+  op->d_r64 = op->mem.alloc_n<double>(size_t(n), "residual");
+  op->d_io = op->mem.alloc_n<double>(size_t(n), "staging");
+  op->d_io2 = op->mem.alloc_n<double>(size_t(n), "staging");
+  op->d_hb = op->mem.alloc_n<double>(size_t(n), "host staging");
+  op->d_hx = op->mem.alloc_n<double>(size_t(n), "host staging");
+  op->d_part = op->mem.alloc_n<double>(size_t(kVecCtas), "partials");
+  op->d_scal = op->mem.alloc_n<double>(8, "scalars");
+  CK(cudaMallocHost(&op->h_scal, sizeof(double) * 8));
+  CK(cudaMallocHost(&op->h_waits, sizeof(unsigned int)));
+  CK(read_stream_timeouts(op->h_waits, st));
+  CK(cudaStreamSynchronize(st));
+  op->waits_seen = *op->h_waits;
+  const int restart = op->p.restart > 0 ? op->p.restart : 100;
+  if (op->p.precision == HODLR_PREC_MIXED) {
+    op->d_in32 = static_cast<float*>(op->mem.alloc(size_t(ldin) * 4 + 16, "matvec input (FP32)"));
+    op->d_y32 = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots), "matvec slots (FP32)");
+    op->d_r32 = op->mem.alloc_n<float>(size_t(n), "residual (FP32)");
+    op->d_d32 = op->mem.alloc_n<float>(size_t(n), "correction (FP32)");
+    CK(gmres_alloc<float>(op->g32, n, restart));
+  } else {
+    CK(gmres_alloc<double>(op->g64, n, restart));
+  }
+  CK(cudaStreamSynchronize(st));
+  op->st.t_build_s = now_s() - bs.t0;
+  compute_stats(op);
+}
+
+
+// ---- batches ---------------------------------------------------------------
+// The operators of a batch are built together (their far blocks share the ACA
+// launches) and keep their own storage; the batch adds one merged plan over
+// all of them, so that a matvec of every instance is one launch per phase,
+// and a CUDA graph of that launch sequence per (x, y, nrhs).
+struct hodlr_batch {
+  hodlr_ctx* ctx = nullptr;
+  std::vector<hodlr_op*> ops;
+  Prec vec = Prec::kD;  // vector type of hodlr_batch_matvec_device
+  bool df = false;      // FP32 factors with FP64 vectors (compensated accumulation)
+  DevMem mem;
+  Plan plan;
+  int64_t ld_in = 0, ycol = 0, total_n = 0, max_n = 0;
+  std::vector<int64_t> offsets;  // instance i: rows offsets[i] .. offsets[i+1] of the caller's vectors
+  BatchInst* d_inst = nullptr;
+  void* d_in = nullptr;   // [x | z] of every instance, vector type
+  void* d_in2 = nullptr;  // the same as (hi, lo) FP32 pairs (df)
+  void* d_y = nullptr;    // output slots of every instance
+  struct Graph {
+    const void* x;
+    void* y;
+    int64_t nrhs;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    uint64_t kernels;
+  };
+  std::vector<Graph> graphs;
+  ~hodlr_batch() {
+    for (Graph& g : graphs) {
+      cudaGraphExecDestroy(g.exec);
+      cudaGraphDestroy(g.graph);
+    }
+    for (hodlr_op* op : ops) delete op;
+    mem.release_all();
+  }
+};
+
+namespace {
+
+// The merged plan of the batch (vector type b.vec): every instance's items,
+// segments and panels with their offsets moved to the instance's place in the
+// batch's input buffer, output slots and partial-sum scratch.
+void build_batch_plan(hodlr_batch& b, cudaStream_t st) {
+  Plan::Host h;
+  const bool f32 = b.vec == Prec::kF;
+  int64_t in_base = 0, y_base = 0, x_base = 0, zpart = 0;
+  int64_t near_parts = 0, far_parts = 0;
+  std::vector<BatchInst> inst;
+  b.offsets.assign(1, 0);
+  for (hodlr_op* op : b.ops) {
+    const Plan& pn = f32 ? op->plan32 : op->plan64;  // near field and scratch sizes
+    const Plan::Host& hn = *pn.host;
+    const Plan::Host& hf = *op->plan64.host;  // far field (shared by both vector types)
+    BatchInst I;
+    I.n = op->n;
+    I.x_base = x_base;
+    I.in_base = in_base;
+    I.y_base = y_base;
+    I.perm = op->d_perm;
+    I.nslots = op->nslots;
+    I.pad = 0;
+    inst.push_back(I);
+    // near field
+    const int rows_near = rows_per_item(pn.a_near);
+    const int32_t pb = int32_t(h.panels_near.size()), sbase = int32_t(h.segs_near.size());
+    for (Panel p : hn.panels_near) {
+      p.seg_begin += sbase;
+      p.seg_end += sbase;
+      p.yoff += y_base;
+      h.panels_near.push_back(p);
+    }
+    for (Seg s : hn.segs_near) {
+      s.in_off += in_base;
+      h.segs_near.push_back(s);
+    }
+    auto shift_item = [&](Item it, int32_t panel_base, int32_t seg_base, int64_t part_base) {
+      it.panel += panel_base;
+      it.seg_b += seg_base;
+      it.seg_e += seg_base;
+      if (it.part >= 0) it.part += int32_t(part_base);
+      return it;
+    };
+    for (const Item& it : hn.small_near) h.small_near.push_back(shift_item(it, pb, sbase, near_parts));
+    for (const Item& it : hn.big_near) h.big_near.push_back(shift_item(it, pb, sbase, near_parts));
+    for (PanelFix f : hn.pfix_near) {
+      f.panel += pb;
+      f.part += int32_t(near_parts);
+      h.pfix_near.push_back(f);
+    }
+    near_parts += pn.nypart_near / rows_near;
+    // far field
+    const int rows_far = rows_per_item(op->plan64.a_far);
+    const int32_t fpb = int32_t(h.panels_far.size()), fsb = int32_t(h.segs_far.size());
+    for (Panel p : hf.panels_far) {
+      p.seg_begin += fsb;
+      p.seg_end += fsb;
+      p.yoff += y_base;
+      h.panels_far.push_back(p);
+    }
+    for (Seg s : hf.segs_far) {
+      s.in_off += in_base;
+      h.segs_far.push_back(s);
+    }
+    for (const Item& it : hf.small_far) h.small_far.push_back(shift_item(it, fpb, fsb, far_parts));
+    for (const Item& it : hf.big_far) h.big_far.push_back(shift_item(it, fpb, fsb, far_parts));
+    int64_t op_far_parts = 0;
+    for (PanelFix f : hf.pfix_far) {
+      op_far_parts += f.count;
+      f.panel += fpb;
+      f.part += int32_t(far_parts);
+      h.pfix_far.push_back(f);
+    }
+    far_parts += op_far_parts;
+    // V^T x
+    const int32_t zbb = int32_t(h.zb.size());
+    for (ZBlock z : hf.zb) {
+      z.x_off += in_base;
+      z.z_off += in_base;
+      h.zb.push_back(z);
+    }
+    for (ZItem it : hf.zitems) {
+      it.zb += zbb;
+      if (it.part >= 0) it.part += int32_t(zpart);
+      h.zitems.push_back(it);
+    }
+    for (ZFix f : hf.zfix) {
+      f.zpos += in_base;
+      f.part += int32_t(zpart);
+      h.zfix.push_back(f);
+    }
+    zpart += op->plan64.nzpart;
+    (void)rows_far;
+    in_base += op->n + op->zlen;
+    y_base += int64_t(op->nslots) * op->n;
+    x_base += op->n;
+    b.offsets.push_back(x_base);
+    b.max_n = std::max(b.max_n, op->n);
+  }
+  if (in_base > (int64_t(1) << 31) || zpart > (int64_t(1) << 31))
+    throw Failure{HODLR_ERR_INVALID, "hodlr_build_batch: the batch is too large for one merged plan"};
+  b.ld_in = in_base;
+  b.ycol = y_base;
+  b.total_n = x_base;
+  Plan& p = b.plan;
+  const Plan& p0 = f32 ? b.ops[0]->plan32 : b.ops[0]->plan64;
+  p.a_near = p0.a_near;
+  p.a_far = b.ops[0]->plan64.a_far;
+  p.panels_near = upload(b.mem, h.panels_near, st, "batch near panels");
+  p.segs_near = upload(b.mem, h.segs_near, st, "batch near segments");
+  p.small_near = upload(b.mem, h.small_near, st, "batch near items");
+  p.big_near = upload(b.mem, h.big_near, st, "batch near items");
+  p.nsmall_near = int(h.small_near.size());
+  p.nbig_near = int(h.big_near.size());
+  p.pfix_near = upload(b.mem, h.pfix_near, st, "batch near fix-ups");
+  p.npfix_near = int(h.pfix_near.size());
+  p.panels_far = upload(b.mem, h.panels_far, st, "batch far panels");
+  p.segs_far = upload(b.mem, h.segs_far, st, "batch far segments");
+  p.small_far = upload(b.mem, h.small_far, st, "batch far items");
+  p.big_far = upload(b.mem, h.big_far, st, "batch far items");
+  p.nsmall_far = int(h.small_far.size());
+  p.nbig_far = int(h.big_far.size());
+  p.pfix_far = upload(b.mem, h.pfix_far, st, "batch far fix-ups");
+  p.npfix_far = int(h.pfix_far.size());
+  p.zb = upload(b.mem, h.zb, st, "batch z blocks");
+  p.nzb = int(h.zb.size());
+  p.zitems = upload(b.mem, h.zitems, st, "batch z items");
+  p.nzitems = int(h.zitems.size());
+  p.zfix = upload(b.mem, h.zfix, st, "batch z fix-ups");
+  p.nzfix = int(h.zfix.size());
+  const size_t vsz = f32 ? 4 : 8;
+  p.nzpart = zpart;
+  p.nypart = std::max(near_parts * rows_per_item(p.a_near), far_parts * rows_per_item(p.a_far));
+  p.zpart = b.mem.alloc(size_t(std::max<int64_t>(p.nzpart, 1)) * vsz, "batch z partial sums");
+  p.ypart = b.mem.alloc(size_t(std::max<int64_t>(p.nypart, 1)) * vsz, "batch row partial sums");
+  b.d_inst = upload(b.mem, inst, st, "batch instances");
+  b.d_in = b.mem.alloc(size_t(b.ld_in) * vsz + 16, "batch matvec input");
+  if (b.df) b.d_in2 = b.mem.alloc(size_t(b.ld_in) * 8 + 16, "batch matvec input (FP32 pairs)");
+  b.d_y = b.mem.alloc(size_t(b.ycol) * vsz, "batch matvec slots");
+  CK(cudaStreamSynchronize(st));
+}
+
+// One column: x (caller order, all instances) -> y.
+void batch_apply(hodlr_batch& b, const void* x, void* y, cudaStream_t st) {
+  const Plan& p = b.plan;
+  const size_t vsz = b.vec == Prec::kF ? 4 : 8;
+  CK(launch_batch_gather(b.vec, b.d_inst, int(b.ops.size()), b.max_n, x, b.d_in, st));
+  CK(cudaMemsetAsync(b.d_y, 0, size_t(b.ycol) * vsz, st));
+  void* fin = b.d_in;
+  Accum acc = Accum::kByType;
+  if (b.df) {
+    fin = b.d_in2;
+    acc = Accum::kCompensated;
+    CK(launch_split(static_cast<const double*>(b.d_in), fin, b.ld_in, st));
+  }
+  CK(launch_zgemv(p.a_far, b.vec, p.zb, p.zitems, p.nzitems, p.zfix, p.nzfix, p.zpart, fin, b.ld_in, 1, st, acc));
+  CK(launch_panels(p.a_near, b.vec, p.panels_near, p.segs_near, p.small_near, p.nsmall_near, p.big_near, p.nbig_near,
+                   p.pfix_near, p.npfix_near, p.ypart, b.d_in, b.ld_in, b.d_y, b.ycol, 1, 1, st));
+  CK(launch_panels(p.a_far, b.vec, p.panels_far, p.segs_far, p.small_far, p.nsmall_far, p.big_far, p.nbig_far,
+                   p.pfix_far, p.npfix_far, p.ypart, fin, b.ld_in, b.d_y, b.ycol, 1, 1, st, acc));
+  CK(launch_batch_combine(b.vec, b.d_inst, int(b.ops.size()), b.max_n, b.d_y, y, st));
+}
+
+}  // namespace
+
 extern "C" {
 
 void hodlr_params_default(hodlr_params* p) {
@@ -901,6 +1404,10 @@ int hodlr_ctx_create(const hodlr_params* params, hodlr_ctx** out) {
   if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED && p.precision != HODLR_PREC_FP32_FACTORS)
     return fail(nullptr, HODLR_ERR_INVALID, "unknown precision");
   if (p.restart < 0 || p.restart > 1000) return fail(nullptr, HODLR_ERR_INVALID, "restart must be in 0..1000");
+  if (p.ortho < HODLR_ORTHO_AUTO || p.ortho > HODLR_ORTHO_CGS2)
+    return fail(nullptr, HODLR_ERR_INVALID, "unknown orthogonalisation");
+  if (p.relax != HODLR_RELAX_AUTO && p.relax != HODLR_RELAX_OFF)
+    return fail(nullptr, HODLR_ERR_INVALID, "relax must be HODLR_RELAX_AUTO or HODLR_RELAX_OFF");
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev == 0)
@@ -945,112 +1452,12 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
   return guarded(ctx, [&]() -> int {
     CK(cudaSetDevice(ctx->p.device));
     cudaStream_t st = ctx->stream;
-    const double t0 = now_s();
-    TreeParams tp;
-    tp.ndim = op->p.ndim;
-    tp.nmax = op->p.nmax;
-    tp.dprime = op->p.dprime;
-    const std::string terr = build_tree(tp, points, n, box_lo, box_hi, op->tree);
-    if (!terr.empty()) return fail(ctx, terr.find("exceeds") != std::string::npos ? HODLR_ERR_TREE : HODLR_ERR_INVALID,
-                                   "hodlr_build: " + terr);
-    op->far = far_blocks(op->tree);
-    op->near = near_blocks(op->tree);
-    op->nslots = op->tree.levels;
-    const double t1 = now_s();
-    op->st.t_tree_s = t1 - t0;
-    // points in tree order, structure of arrays
-    const int d = op->p.ndim;
-    std::vector<double> soa(size_t(n) * size_t(d));
-    for (int64_t i = 0; i < n; i++)
-      for (int k = 0; k < d; k++) soa[size_t(k) * size_t(n) + size_t(i)] = points[size_t(op->tree.perm[size_t(i)]) * d + k];
-    op->d_pts = upload(op->mem, soa, st, "points");
-    op->d_perm = upload(op->mem, op->tree.perm, st, "permutation");
-    op->d_lmap = upload(op->mem, reference_order_map(op->tree), st, "reference-order map");
-    // near field
-    const NearTiles nt = near_tiles(op->tree, op->near, 8);
-    PointsDev P{op->d_pts, n};
-    KernelDev K{kernel->kind, kernel->scale, kernel->diag};
-    TileDesc* d_tiles = upload(op->mem, nt.tiles, st, "near tile descriptors");
-    double* near64 = op->mem.alloc_n<double>(size_t(std::max<int64_t>(nt.total, 1)), "near field (FP64)");
-    CK(cudaMemsetAsync(near64, 0, sizeof(double) * size_t(std::max<int64_t>(nt.total, 1)), st));
-    CK(launch_assemble(d, P, K, d_tiles, int(nt.tiles.size()), near64, Prec::kD, st));
-    float* near32 = nullptr;
-    NearTiles nt32;
-    if (op->p.precision == HODLR_PREC_MIXED) {
-      nt32 = near_tiles(op->tree, op->near, 4);
-      TileDesc* d_tiles32 = upload(op->mem, nt32.tiles, st, "near tile descriptors");
-      near32 = op->mem.alloc_n<float>(size_t(std::max<int64_t>(nt32.total, 1)), "near field (FP32)");
-      CK(cudaMemsetAsync(near32, 0, sizeof(float) * size_t(std::max<int64_t>(nt32.total, 1)), st));
-      CK(launch_assemble(d, P, K, d_tiles32, int(nt32.tiles.size()), near32, Prec::kF, st));
-      CK(cudaStreamSynchronize(st));
-      op->mem.release(d_tiles32);
-    }
-    CK(cudaStreamSynchronize(st));
-    op->mem.release(d_tiles);
-    const double t2 = now_s();
-    op->st.t_near_s = t2 - t1;
-    // far field
-    std::vector<const void*>& uptr = op->uptr;
-    std::vector<const void*>& vptr = op->vptr;
-    run_aca(op.get(), st, uptr, vptr);
-    const double t3 = now_s();
-    op->st.t_aca_s = t3 - t2;
-    // plans
-    const Prec fp = op->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
-    build_near_plan(op.get(), nt, near64, Prec::kD, op->plan64, st);
-    build_far_plan(op.get(), uptr, vptr, fp, op->plan64, st);
-    if (op->p.precision == HODLR_PREC_MIXED) {
-      build_near_plan(op.get(), nt32, near32, Prec::kF, op->plan32, st);
-      op->plan32.a_far = Prec::kF;
-      op->plan32.panels_far = op->plan64.panels_far;
-      op->plan32.segs_far = op->plan64.segs_far;
-      op->plan32.small_far = op->plan64.small_far;
-      op->plan32.big_far = op->plan64.big_far;
-      op->plan32.nsmall_far = op->plan64.nsmall_far;
-      op->plan32.nbig_far = op->plan64.nbig_far;
-      op->plan32.zb = op->plan64.zb;
-      op->plan32.nzb = op->plan64.nzb;
-      op->plan32.zitems = op->plan64.zitems;
-      op->plan32.nzitems = op->plan64.nzitems;
-      op->plan32.zfix = op->plan64.zfix;
-      op->plan32.nzfix = op->plan64.nzfix;
-      op->plan32.pfix_far = op->plan64.pfix_far;
-      op->plan32.npfix_far = op->plan64.npfix_far;
-      op->plan32.nzpart = op->plan64.nzpart;
-      op->plan32.nypart = op->plan64.nypart;
-      op->plan32.zpart = op->mem.alloc(size_t(std::max<int64_t>(op->plan32.nzpart, 1)) * 4, "z partial sums (FP32)");
-      op->plan32.ypart = op->mem.alloc(size_t(std::max<int64_t>(op->plan32.nypart, 1)) * 4, "row partial sums (FP32)");
-    }
-    op->plan64.zpart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nzpart, 1)) * 8, "z partial sums");
-    op->plan64.ypart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nypart, 1)) * 8, "row partial sums");
-    // work vectors
-    const int64_t ldin = n + op->zlen;
-    op->d_in64 = op->mem.alloc_n<double>(size_t(ldin), "matvec input");
-    if (op->p.precision != HODLR_PREC_FP64) op->d_in2 = op->mem.alloc(size_t(ldin) * 8, "matvec input (FP32 pairs)");
-    op->d_y64 = op->mem.alloc_n<double>(size_t(n) * size_t(op->nslots), "matvec slots");
-    op->d_b64 = op->mem.alloc_n<double>(size_t(n), "rhs");
-    op->d_x64 = op->mem.alloc_n<double>(size_t(n), "solution");
-    op->d_r64 = op->mem.alloc_n<double>(size_t(n), "residual");
-    op->d_io = op->mem.alloc_n<double>(size_t(n), "staging");
-    op->d_io2 = op->mem.alloc_n<double>(size_t(n), "staging");
-    op->d_hb = op->mem.alloc_n<double>(size_t(n), "host staging");
-    op->d_hx = op->mem.alloc_n<double>(size_t(n), "host staging");
-    op->d_part = op->mem.alloc_n<double>(size_t(kVecCtas), "partials");
-    op->d_scal = op->mem.alloc_n<double>(8, "scalars");
-    CK(cudaMallocHost(&op->h_scal, sizeof(double) * 8));
-    const int restart = op->p.restart > 0 ? op->p.restart : 100;
-    if (op->p.precision == HODLR_PREC_MIXED) {
-      op->d_in32 = op->mem.alloc_n<float>(size_t(ldin), "matvec input (FP32)");
-      op->d_y32 = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots), "matvec slots (FP32)");
-      op->d_r32 = op->mem.alloc_n<float>(size_t(n), "residual (FP32)");
-      op->d_d32 = op->mem.alloc_n<float>(size_t(n), "correction (FP32)");
-      CK(gmres_alloc<float>(op->g32, n, restart));
-    } else {
-      CK(gmres_alloc<double>(op->g64, n, restart));
-    }
-    CK(cudaStreamSynchronize(st));
-    op->st.t_build_s = now_s() - t0;
-    compute_stats(op.get());
+    BuildState bs;
+    build_prepare(op.get(), points, box_lo, box_hi, st, bs);
+    std::vector<hodlr_op*> one{op.get()};
+    run_aca(one, st);
+    op->st.t_aca_s = now_s() - bs.t2;
+    build_finish(op.get(), bs, st);
     *out = op.release();
     return HODLR_OK;
   });
@@ -1058,10 +1465,23 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
 
 int hodlr_op_destroy(hodlr_op* op) {
   if (!op) return HODLR_OK;
+  if (op->batch_owned)
+    return fail(op->ctx, HODLR_ERR_STATE, "hodlr_op_destroy: the operator belongs to a batch (hodlr_batch_destroy)");
   cudaSetDevice(op->p.device);
   cudaStreamSynchronize(op->ctx->stream);
   delete op;
   return HODLR_OK;
+}
+
+// After a synchronised matvec or solve on `st`: a streaming kernel that gave
+// up waiting for its copies left results that must not be used.
+void check_stream_waits(hodlr_op* op, cudaStream_t st) {
+  CK(read_stream_timeouts(op->h_waits, st));
+  CK(cudaStreamSynchronize(st));
+  if (*op->h_waits != op->waits_seen) {
+    op->waits_seen = *op->h_waits;
+    throw Failure{HODLR_ERR_DEVICE, "a matvec kernel gave up waiting for its bulk copies; the results are invalid"};
+  }
 }
 
 int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nrhs, void* stream) {
@@ -1096,6 +1516,7 @@ int hodlr_matvec(hodlr_op* op, const double* x, double* y, int64_t nrhs) {
     }
     CK(cudaStreamSynchronize(st));
     op->st.t_matvec_s = (now_s() - t0) / double(nrhs);
+    check_stream_waits(op, st);
     return HODLR_OK;
   });
 }
@@ -1128,6 +1549,7 @@ int hodlr_solve_device(hodlr_op* op, const double* d_b, double* d_x, int64_t nrh
       all_conv = all_conv && one.converged;
     }
     CK(cudaStreamSynchronize(st));
+    check_stream_waits(op, st);
     info->rel_residual = worst;
     info->converged = all_conv ? 1 : 0;
     return all_conv ? HODLR_OK : fail(op->ctx, HODLR_ERR_NOT_CONVERGED, "GMRES did not reach the tolerance");
@@ -1343,6 +1765,118 @@ int hodlr_tree_get(const hodlr_tree* tr, int64_t* level_sizes, int64_t* node_cou
 
 int hodlr_tree_destroy(hodlr_tree* tr) {
   delete tr;
+  return HODLR_OK;
+}
+
+
+int hodlr_build_batch(hodlr_ctx* ctx, int32_t count, const double* const* points, const int64_t* n,
+                      const double* box_lo, const double* box_hi, const hodlr_kernel_desc* kernels,
+                      hodlr_batch** out) {
+  if (!ctx || !points || !n || !box_lo || !box_hi || !kernels || !out)
+    return fail(ctx, HODLR_ERR_INVALID, "hodlr_build_batch: null argument");
+  *out = nullptr;
+  if (count < 1) return fail(ctx, HODLR_ERR_INVALID, "hodlr_build_batch: count must be positive");
+  for (int32_t i = 0; i < count; i++) {
+    if (!points[i] || n[i] < 1 || n[i] > (int64_t(1) << 31) - 1)
+      return fail(ctx, HODLR_ERR_INVALID, "hodlr_build_batch: instance " + std::to_string(i) + ": bad points or n");
+    if (kernels[i].kind != kernels[0].kind || kernels[i].diag != kernels[0].diag || kernels[i].scale == 0.0)
+      return fail(ctx, HODLR_ERR_INVALID,
+                  "hodlr_build_batch: instances must share the kernel kind and diagonal and have nonzero scales");
+  }
+  if (kernels[0].kind < HODLR_KERNEL_INV_R || kernels[0].kind > HODLR_KERNEL_EXP_NEG_R)
+    return fail(ctx, HODLR_ERR_INVALID, "hodlr_build_batch: unknown kernel kind");
+  std::unique_ptr<hodlr_batch> b(new hodlr_batch());
+  b->ctx = ctx;
+  b->vec = ctx->p.precision == HODLR_PREC_MIXED ? Prec::kF : Prec::kD;
+  b->df = ctx->p.precision == HODLR_PREC_FP32_FACTORS;
+  return guarded(ctx, [&]() -> int {
+    CK(cudaSetDevice(ctx->p.device));
+    cudaStream_t st = ctx->stream;
+    const int d = ctx->p.ndim;
+    std::vector<BuildState> bs(static_cast<size_t>(count));
+    for (int32_t i = 0; i < count; i++) {
+      hodlr_op* op = new hodlr_op();
+      b->ops.push_back(op);
+      op->ctx = ctx;
+      op->p = ctx->p;
+      op->kd = kernels[i];
+      op->n = n[i];
+      op->keep_host_plans = true;
+      op->batch_owned = true;
+      std::memset(&op->st, 0, sizeof(op->st));
+      build_prepare(op, points[i], box_lo + size_t(i) * d, box_hi + size_t(i) * d, st, bs[size_t(i)]);
+    }
+    const double ta = now_s();
+    run_aca(b->ops, st);
+    const double t_aca = now_s() - ta;
+    for (int32_t i = 0; i < count; i++) {
+      b->ops[size_t(i)]->st.t_aca_s = t_aca;
+      build_finish(b->ops[size_t(i)], bs[size_t(i)], st);
+    }
+    build_batch_plan(*b, st);
+    *out = b.release();
+    return HODLR_OK;
+  });
+}
+
+int hodlr_batch_offsets(const hodlr_batch* b, int64_t* offsets) {
+  if (!b || !offsets) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_batch_offsets: null argument");
+  std::copy(b->offsets.begin(), b->offsets.end(), offsets);
+  return HODLR_OK;
+}
+
+int hodlr_batch_op(hodlr_batch* b, int32_t i, hodlr_op** op) {
+  if (!b || !op) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_batch_op: null argument");
+  if (i < 0 || i >= int32_t(b->ops.size())) return fail(b->ctx, HODLR_ERR_INVALID, "hodlr_batch_op: index out of range");
+  *op = b->ops[size_t(i)];
+  return HODLR_OK;
+}
+
+int hodlr_batch_matvec_device(hodlr_batch* b, const void* d_x, void* d_y, int64_t nrhs, void* stream) {
+  if (!b || !d_x || !d_y) return fail(b ? b->ctx : nullptr, HODLR_ERR_INVALID, "hodlr_batch_matvec_device: null argument");
+  if (nrhs < 1) return fail(b->ctx, HODLR_ERR_INVALID, "hodlr_batch_matvec_device: nrhs must be positive");
+  return guarded(b->ctx, [&]() -> int {
+    CK(cudaSetDevice(b->ctx->p.device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    hodlr_batch::Graph* g = nullptr;
+    for (hodlr_batch::Graph& q : b->graphs)
+      if (q.x == d_x && q.y == d_y && q.nrhs == nrhs) g = &q;
+    if (!g) {
+      // capture every column's launch sequence once on the batch's own stream
+      const size_t vsz = b->vec == Prec::kF ? 4 : 8;
+      cudaStream_t cs = b->ctx->stream;
+      CK(cudaStreamSynchronize(cs));
+      const uint64_t k0 = g_kernel_launches.load();
+      hodlr_batch::Graph ng{d_x, d_y, nrhs, nullptr, nullptr, 0};
+      CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      try {
+        for (int64_t c = 0; c < nrhs; c++)
+          batch_apply(*b, static_cast<const char*>(d_x) + size_t(c * b->total_n) * vsz,
+                      static_cast<char*>(d_y) + size_t(c * b->total_n) * vsz, cs);
+      } catch (...) {
+        cudaGraph_t dead = nullptr;
+        cudaStreamEndCapture(cs, &dead);
+        if (dead) cudaGraphDestroy(dead);
+        throw;
+      }
+      CK(cudaStreamEndCapture(cs, &ng.graph));
+      ng.kernels = g_kernel_launches.load() - k0;
+      CK(cudaGraphInstantiate(&ng.exec, ng.graph, 0));
+      b->graphs.push_back(ng);
+      g = &b->graphs.back();
+    } else {
+      count_launches(g->kernels);
+    }
+    CK(cudaGraphLaunch(g->exec, st));
+    return HODLR_OK;
+  });
+}
+
+int hodlr_batch_destroy(hodlr_batch* b) {
+  if (!b) return HODLR_OK;
+  cudaSetDevice(b->ctx->p.device);
+  cudaStreamSynchronize(b->ctx->stream);
+  delete b;
   return HODLR_OK;
 }
 

@@ -68,6 +68,75 @@ __global__ void __launch_bounds__(kThreads)
   if (threadIdx.x == 0) part_out[blockIdx.x] = acc;
 }
 
+// Classical Gram-Schmidt, one pass (applied twice per Arnoldi step: CGS2).
+// cgs_dots: part[j * kVecCtas + cta] = this CTA's share of <w, v_j> for
+// j < nv, eight vectors at a time so each thread keeps eight loads in flight.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    cgs_dots_kernel(const T* __restrict__ w, const T* __restrict__ V, int64_t n, int nv, double* __restrict__ part) {
+  constexpr int U = 8;
+  __shared__ double sh[U][kThreads / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < nv; j0 += U) {
+    const int jn = min(U, nv - j0);
+    double acc[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) acc[u] = 0.0;
+    for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads) {
+      const double wi = to_d(w[i]);
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (u < jn) acc[u] += to_d(V[int64_t(j0 + u) * n + i]) * wi;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+      if (lane == 0) sh[u][wid] = acc[u];
+    }
+    __syncthreads();
+    if (threadIdx.x < jn) {
+      double v = 0.0;
+      for (int q = 0; q < kThreads / 32; q++) v += sh[threadIdx.x][q];
+      part[int64_t(j0 + threadIdx.x) * kVecCtas + blockIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// One CTA per basis vector j: hc[j] = <w, v_j> from the partial sums (fixed
+// order); the Hessenberg column gets hc (first pass) or hc added (second).
+__global__ void __launch_bounds__(kThreads)
+    cgs_reduce_kernel(const double* __restrict__ part, double* __restrict__ hc, double* __restrict__ hcol, int second) {
+  const int j = blockIdx.x;
+  const double v = reduce_parts(part + int64_t(j) * kVecCtas);
+  if (threadIdx.x == 0) {
+    hc[j] = v;
+    hcol[j] = second ? __dadd_rn(hcol[j], v) : v;
+  }
+}
+
+// w -= sum_j hc[j] v_j (in FP64, j in order, rounded to T once); with part,
+// also the partial sums of |w|^2 for the normalisation.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) cgs_update_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t n,
+                                                              int nv, const double* __restrict__ hc,
+                                                              double* __restrict__ part) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads) {
+    double wi = to_d(w[i]);
+#pragma unroll 8
+    for (int j = 0; j < nv; j++) wi = axmy(wi, hc[j], to_d(V[int64_t(j) * n + i]));
+    const T t = T(wi);
+    w[i] = t;
+    acc += to_d(t) * to_d(t);
+  }
+  if (part) {
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+  }
+}
+
 // h = sqrt(<w, w>) from part; v_next = (1 / h) * w (GMRES.hpp:241-242).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -193,6 +262,8 @@ cudaError_t gmres_alloc(GmresWork<T>& W, int64_t n, int restart) {
   HODLR_TRY(cudaMalloc(&W.rot, sizeof(double) * 4 * size_t(restart + 1)));
   HODLR_TRY(cudaMemset(W.rot, 0, sizeof(double) * 4 * size_t(restart + 1)));
   HODLR_TRY(cudaMalloc(&W.part, sizeof(double) * 2 * kVecCtas));
+  HODLR_TRY(cudaMalloc(&W.partk, sizeof(double) * kVecCtas * size_t(restart + 1)));
+  HODLR_TRY(cudaMalloc(&W.hc, sizeof(double) * size_t(restart + 1)));
   HODLR_TRY(cudaMalloc(&W.scal, sizeof(double) * 8));
   HODLR_TRY(cudaMallocHost(&W.hscal, sizeof(double) * 8));
   return cudaSuccess;
@@ -207,6 +278,8 @@ void gmres_free(GmresWork<T>& W) {
   cudaFree(W.H);
   cudaFree(W.rot);
   cudaFree(W.part);
+  cudaFree(W.partk);
+  cudaFree(W.hc);
   cudaFree(W.scal);
   if (W.hscal) cudaFreeHost(W.hscal);
   W = GmresWork<T>();
@@ -232,7 +305,8 @@ cudaError_t vec_norm2(const T* a, int64_t n, double* part, double* dst, cudaStre
 
 template <typename T>
 cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* x, bool x0_zero, int restart,
-                        int64_t max_iter, double tol, cudaStream_t st, GmresResult* res) {
+                        int64_t max_iter, double tol, cudaStream_t st, GmresResult* res, Ortho ortho,
+                        const std::function<void(double)>& progress) {
   const int64_t n = W.n;
   if (restart > W.restart || restart < 1) return cudaErrorInvalidValue;
   const int m = restart, ldh = W.restart + 1;
@@ -272,17 +346,29 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
     for (int i = 0; i < m && j <= max_iter; i++, j++) {
       T* vi = W.V + int64_t(i) * n;
       HODLR_TRY(A(vi, W.w));
-      count_launches(1);
-      dot_partial_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, part0);
-      for (int k = 0; k <= i; k++) {
-        const T* next = k < i ? W.V + int64_t(k + 1) * n : nullptr;
-        double* pin = (k & 1) ? part1 : part0;
-        double* pout = (k & 1) ? part0 : part1;
+      double* plast;
+      if (ortho == Ortho::kMGS) {
         count_launches(1);
-        mgs_step_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V + int64_t(k) * n, next, n, pin, pout,
-                                                           W.H + k + int64_t(i) * ldh);
+        dot_partial_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, part0);
+        for (int k = 0; k <= i; k++) {
+          const T* next = k < i ? W.V + int64_t(k + 1) * n : nullptr;
+          double* pin = (k & 1) ? part1 : part0;
+          double* pout = (k & 1) ? part0 : part1;
+          count_launches(1);
+          mgs_step_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V + int64_t(k) * n, next, n, pin, pout,
+                                                             W.H + k + int64_t(i) * ldh);
+        }
+        plast = (i & 1) ? part0 : part1;
+      } else {
+        // CGS2: two classical passes against v_0 .. v_i, |w|^2 from the second
+        for (int pass = 0; pass < 2; pass++) {
+          count_launches(3);
+          cgs_dots_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, i + 1, W.partk);
+          cgs_reduce_kernel<<<i + 1, kThreads, 0, st>>>(W.partk, W.hc, W.H + int64_t(i) * ldh, pass);
+          cgs_update_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, i + 1, W.hc, pass == 1 ? part0 : nullptr);
+        }
+        plast = part0;
       }
-      double* plast = (i & 1) ? part0 : part1;
       count_launches(1);
       normalize_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V + int64_t(i + 1) * n, n, plast,
                                                           W.H + (i + 1) + int64_t(i) * ldh);
@@ -291,6 +377,7 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
       HODLR_TRY(cudaGetLastError());
       HODLR_TRY(host_scal(1));
       resid = W.hscal[0];
+      if (progress) progress(resid);
       if (resid < tol) {
         count_launches(1);
         backsolve_kernel<<<1, 1, 0, st>>>(W.H, ldh, W.rot, W.restart, i);
@@ -307,6 +394,7 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
     backsolve_kernel<<<1, 1, 0, st>>>(W.H, ldh, W.rot, W.restart, m - 1);
     count_launches(1);
     update_x_kernel<T><<<kVecCtas, kThreads, 0, st>>>(x, W.V, n, W.rot, W.restart, m - 1, n);
+    if (progress) progress(1.0);  // the restart's true residual
     HODLR_TRY(A(x, W.tmp));
     HODLR_TRY(vec_sub_norm2<T>(b, W.tmp, W.r, n, part0, W.scal + 1, st));
     HODLR_TRY(host_scal(2));
@@ -328,9 +416,11 @@ template cudaError_t gmres_alloc<float>(GmresWork<float>&, int64_t, int);
 template void gmres_free<double>(GmresWork<double>&);
 template void gmres_free<float>(GmresWork<float>&);
 template cudaError_t gmres_solve<double>(GmresWork<double>&, const TreeMatvec<double>&, const double*, double*, bool,
-                                         int, int64_t, double, cudaStream_t, GmresResult*);
+                                         int, int64_t, double, cudaStream_t, GmresResult*, Ortho,
+                                         const std::function<void(double)>&);
 template cudaError_t gmres_solve<float>(GmresWork<float>&, const TreeMatvec<float>&, const float*, float*, bool, int,
-                                        int64_t, double, cudaStream_t, GmresResult*);
+                                        int64_t, double, cudaStream_t, GmresResult*, Ortho,
+                                        const std::function<void(double)>&);
 template cudaError_t vec_sub_norm2<double>(const double*, const double*, double*, int64_t, double*, double*,
                                            cudaStream_t);
 template cudaError_t vec_sub_norm2<float>(const float*, const float*, float*, int64_t, double*, double*, cudaStream_t);

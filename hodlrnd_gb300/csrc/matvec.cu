@@ -1,8 +1,15 @@
 // HODLR matvec kernels (see matvec.h).
+#include "bulk.cuh"
 #include "device.cuh"
 #include "matvec.h"
 
 namespace hodlr {
+
+__device__ unsigned int g_stream_timeouts = 0;
+
+cudaError_t read_stream_timeouts(unsigned int* host, cudaStream_t st) {
+  return cudaMemcpyFromSymbolAsync(host, g_stream_timeouts, sizeof(unsigned int), 0, cudaMemcpyDeviceToHost, st);
+}
 
 namespace {
 
@@ -137,6 +144,34 @@ struct IO<DF> {
   }
 };
 
+// Relaxed accumulation (Accum::kRelaxed): the inputs and outputs of DF
+// (split FP64 inputs, FP64 outputs) with plain FP32 sums of the products of
+// the FP32 factors with the inputs' high parts.  Cheaper, and accurate to
+// about 1e-6 relative: what an inexact Krylov method may use once its
+// residual has dropped far enough.
+struct FH {};
+
+template <>
+struct Acc<FH> {
+  using A = float;
+  using X = float;
+  static __device__ __forceinline__ X in(float2 v) { return v.x; }
+  static __device__ __forceinline__ X in(float v) { return v; }
+  static __device__ __forceinline__ A zero() { return 0.f; }
+  static __device__ __forceinline__ void fma(A& a, float v, X x) { a = __fmaf_rn(v, x, a); }
+  static __device__ __forceinline__ A add(A a, A b) { return a + b; }
+  static __device__ __forceinline__ A shfl_xor(A a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+  static __device__ __forceinline__ X shfl(X x, int src) { return __shfl_sync(0xffffffffu, x, src); }
+  static __device__ __forceinline__ double value(A a) { return double(a); }
+};
+
+template <>
+struct IO<FH> {
+  using TI = float2;
+  using TY = double;
+  static __device__ __forceinline__ TI from_double(double v) { return IO<DF>::from_double(v); }
+};
+
 // acc[q] += a[q] * x for the components of a 16-byte vector
 template <typename TACC, typename X>
 __device__ __forceinline__ void axpy16(const float4& a, X x, typename Acc<TACC>::A* acc) {
@@ -170,16 +205,446 @@ template <>
 __device__ __forceinline__ float2 to_input<DF>(DF a) {
   return Acc<DF>::to_pair(a);
 }
+template <>
+__device__ __forceinline__ float2 to_input<FH>(float a) {
+  return make_float2(a, 0.f);
+}
 
 // Phase 1: z_b = V_b^T x_s with V_b stored row major (n x vpad(r)).  The
 // CPL = 16 / sizeof(TA) columns of a 16-byte load belong to one lane; P lanes
 // cover a row's nk columns and the warp's G = 32 / P lane groups take
-// consecutive rows, so each load instruction of the warp reads G whole rows,
-// one contiguous run.  Each lane keeps CPL running sums; the groups are added
-// by shuffles once at the end.  A block with more rows than one item takes
-// writes partial sums (zfix_kernel adds them in order).
+// consecutive rows, so each 16-byte read of the warp covers G whole rows.
+// Each lane keeps CPL running sums, over rows g, g + G, g + 2G, ... of the
+// item in that order; the groups are added by shuffles once at the end.  A
+// block with more rows than one item takes writes partial sums (zfix_kernel
+// adds them in order).
+//
+// An item that covers whole rows (k0 == 0, nk == vpad(r)) reads one
+// contiguous run of V, and its inputs x[j0 .. j1) are contiguous too: both
+// are staged through a per-warp ring of kZStages shared-memory stages by bulk
+// copies, R rows per stage (R a multiple of G, so every lane's row order is
+// the one above).  Other items (blocks of more than 128 FP32 or 64 FP64
+// columns) load V directly.
+constexpr int kZWarps = 4;            // warps per CTA of zgemv_kernel
+constexpr int kZStages = 3;           // ring stages per warp
+constexpr int kZStageBytes = 2048;    // V bytes per stage
+constexpr int kZXBytes = 1056;        // input bytes per stage: <= 128 rows x 8 bytes + 2 x 15 alignment slack, rounded to 16
+constexpr int kZWarpSmem = 64 + kZStages * (kZStageBytes + kZXBytes);
+static_assert(kZWarpSmem % 16 == 0 && kZXBytes % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
+
 template <typename TA, typename TACC>
-__global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
+__global__ void __launch_bounds__(kZWarps * 32) zgemv_kernel(const ZBlock* __restrict__ zb,
+                                                           const ZItem* __restrict__ items, int nitems,
+                                                           typename IO<TACC>::TY* __restrict__ zpart,
+                                                           typename IO<TACC>::TI* in, int64_t ld_in) {
+  using TX = typename IO<TACC>::TI;
+  constexpr int CPL = 16 / int(sizeof(TA));
+  using VT = typename Vec16<TA>::type;
+  using AC = Acc<TACC>;
+  extern __shared__ __align__(16) unsigned char zsm[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kZWarps + wid;
+  if (w >= nitems) return;
+  const ZItem it = items[w];
+  const ZBlock Z = zb[it.zb];
+  const int64_t rp = vpad(Z.r, int(sizeof(TA)));
+  const TX* x = in + blockIdx.y * ld_in + Z.x_off;
+  TX* z = in + blockIdx.y * ld_in + Z.z_off;
+  const int lanes = (it.nk + CPL - 1) / CPL;
+  int P = 1;
+  while (P < lanes) P <<= 1;
+  const int G = 32 / P, g = lane / P, p = lane % P;
+  const bool cact = p < lanes;
+  typename AC::A acc[CPL];
+#pragma unroll
+  for (int q = 0; q < CPL; q++) acc[q] = AC::zero();
+  if (it.k0 == 0 && it.nk == rp) {
+    // rows of rowb = rp * sizeof(TA) bytes (16 .. 512, a multiple of 16); V
+    // is 16-byte aligned (factor chunks are, and every block's V starts on a
+    // 16-byte boundary), so every stage's source and size are too.  The input
+    // run is copied from its 16-byte boundary below to the one above; the
+    // input buffers carry 16 bytes of padding at their end for that.
+    unsigned char* base = zsm + wid * kZWarpSmem;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+    unsigned char* vbuf = base + 64;
+    unsigned char* xbuf = vbuf + kZStages * kZStageBytes;
+    const int rowb = int(rp) * int(sizeof(TA));
+    const int R = (kZStageBytes / rowb) / G * G;  // >= G since 4 P >= lanes
+    const int nrows = it.j1 - it.j0;
+    const int nst = (nrows + R - 1) / R;
+    const TA* V = static_cast<const TA*>(Z.V) + int64_t(it.j0) * rp;
+    const TX* xr = x + it.j0;
+    if (lane == 0) {
+#pragma unroll
+      for (int s = 0; s < kZStages; s++) mbar_init(bar + s, 1);
+      fence_mbar_init();
+    }
+    __syncwarp();
+    auto issue = [&](int q) {  // lane 0
+      const int s = q % kZStages;
+      const int r0 = q * R, nr = min(R, nrows - r0);
+      const uint32_t vb = uint32_t(nr) * uint32_t(rowb);
+      const unsigned char* xs = reinterpret_cast<const unsigned char*>(xr + r0);
+      const unsigned char* xa = static_cast<const unsigned char*>(align_down16(xs));
+      const uint32_t xb = uint32_t((xs + size_t(nr) * sizeof(TX) - xa + 15) & ~size_t(15));
+      fence_proxy_async();
+      mbar_expect_tx(bar + s, vb + xb);
+      bulk_g2s(vbuf + s * kZStageBytes, V + int64_t(r0) * rp, vb, bar + s);
+      bulk_g2s(xbuf + s * kZXBytes, xa, xb, bar + s);
+    };
+    if (lane == 0)
+      for (int q = 0; q < min(kZStages, nst); q++) issue(q);
+    for (int q = 0; q < nst; q++) {
+      const int s = q % kZStages;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(bar + s, uint32_t(q / kZStages) & 1u));
+      if (!ok) {
+        // give up: count it, let the copies still in flight land, return
+        if (lane == 0) atomicAdd(&g_stream_timeouts, 1u);
+        for (int t = q; t < min(q + kZStages, nst); t++) mbar_wait(bar + t % kZStages, uint32_t(t / kZStages) & 1u);
+        return;
+      }
+      const int r0 = q * R, nr = min(R, nrows - r0);
+      const int xo = int((reinterpret_cast<uintptr_t>(xr + r0) & 15u) / sizeof(TX));
+      const TX* xsm = reinterpret_cast<const TX*>(xbuf + s * kZXBytes) + xo;
+      const unsigned char* vs = vbuf + s * kZStageBytes + p * 16;
+      for (int i = g; i < nr; i += G) {
+        const VT v = cact ? *reinterpret_cast<const VT*>(vs + i * rowb) : vzero<VT>();
+        axpy16<TACC>(v, AC::in(xsm[i]), acc);
+      }
+      __syncwarp();
+      if (lane == 0 && q + kZStages < nst) issue(q + kZStages);
+    }
+  } else {
+    const TA* Vc = static_cast<const TA*>(Z.V) + it.k0 + p * CPL;
+    int j = it.j0 + g;
+    for (; j + 3 * G < it.j1; j += 4 * G) {
+      VT v[4];
+      typename AC::X xs[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        v[u] = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j + u * G) * rp)) : vzero<VT>();
+        xs[u] = AC::in(x[j + u * G]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) axpy16<TACC>(v[u], xs[u], acc);
+    }
+    for (; j < it.j1; j += G) {
+      const VT v = cact ? __ldg(reinterpret_cast<const VT*>(Vc + int64_t(j) * rp)) : vzero<VT>();
+      axpy16<TACC>(v, AC::in(x[j]), acc);
+    }
+  }
+  for (int o = P; o < 32; o <<= 1)
+#pragma unroll
+    for (int q = 0; q < CPL; q++) acc[q] = AC::add(acc[q], AC::shfl_xor(acc[q], o));
+  if (g == 0 && cact) {
+#pragma unroll
+    for (int q = 0; q < CPL; q++) {
+      const int c = p * CPL + q;
+      if (it.part < 0) {
+        if (it.k0 + c < Z.r) z[it.k0 + c] = to_input<TACC>(acc[q]);
+      } else {
+        zpart[it.part + c] = typename IO<TACC>::TY(AC::value(acc[q]));
+      }
+    }
+  }
+}
+
+template <typename TACC>
+__global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const typename IO<TACC>::TY* __restrict__ zpart,
+                            typename IO<TACC>::TI* in, int64_t ld_in) {
+  using TY = typename IO<TACC>::TY;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nfix) return;
+  const ZFix F = fix[f];
+  TY acc = TY(0);
+  for (int q = 0; q < F.count; q++) acc += zpart[F.part + q * kZPart];
+  in[blockIdx.y * ld_in + F.zpos] = IO<TACC>::from_double(double(acc));
+}
+
+// Phase 2, panels of at most 32 rows (leaves): lanes form 32 / mpad slices of
+// mpad lanes (mpad = next power of two >= m), one lane per row; slice sl
+// takes segments sl, sl + slices, ... of the item, each cut into pieces of at
+// most cmax columns (a multiple of 16 bytes' worth of elements, so that every
+// piece starts on a 16-byte boundary).  The warp runs in rounds: in round q
+// every slice processes its q-th piece.  A piece (its m x c column-major
+// block, rounded up to 16 bytes, and its input run, from the 16-byte boundary
+// below to the one above) is staged in shared memory by bulk copies that the
+// slice's first lane starts, kSStages rounds ahead; each round's mbarrier
+// expects one arrival per slice.  Column j of a piece goes to accumulator
+// j & 1; the slices are added by shuffles at the end.
+constexpr int kSWarps = 4;         // warps per CTA of panel_small_kernel
+constexpr int kSStages = 3;
+constexpr int kSUBytes = 2048;     // segment bytes per round (all slices)
+constexpr int kSXBytes = 2048;     // input bytes per round (all slices)
+constexpr int kSWarpSmem = 64 + kSStages * (kSUBytes + kSXBytes);
+static_assert(kSWarpSmem % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+template <typename TA, typename TACC>
+__global__ void __launch_bounds__(kSWarps * 32, 4)
+    panel_small_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
+                       int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
+                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
+  using TX = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
+  using AC = Acc<TACC>;
+  constexpr int esz = int(sizeof(TA));
+  constexpr int Q = 16 / esz;  // piece columns are a multiple of Q
+  extern __shared__ __align__(16) unsigned char ssm[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kSWarps + wid;
+  if (w >= nitems) return;
+  const Item it = items[w];
+  const Panel P = panels[it.panel];
+  const int m = P.m;
+  const TX* inc = in + blockIdx.y * ld_in;
+  TY* yo = y + int64_t(blockIdx.y) * nslots * ld_y + P.yoff;
+  int mpad = 1;
+  while (mpad < m) mpad <<= 1;
+  const int slices = 32 / mpad;
+  const int i = lane & (mpad - 1), sl = lane / mpad;
+  // per slice and round: ub bytes of segment, xb bytes of inputs; a piece of
+  // c columns needs c*m*esz + 15 and c*sizeof(TX) + 32 bytes at most
+  const int ub = kSUBytes / slices, xb = kSXBytes / slices;
+  const int cmax = min((ub - 15) / (m * esz), (xb - 32) / int(sizeof(TX))) / Q * Q;  // >= Q: ub, xb >= 64 mpad
+  unsigned char* base = ssm + wid * kSWarpSmem;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  unsigned char* stage0 = base + 64;
+  // rounds = the largest piece count over the slices
+  int npieces = 0;
+  for (int64_t q = it.seg_b + sl; q < it.seg_e; q += slices) npieces += (segs[q].K + cmax - 1) / cmax;
+  int rounds = npieces;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rounds = max(rounds, __shfl_xor_sync(0xffffffffu, rounds, o));
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < kSStages; s++) mbar_init(bar + s, uint32_t(slices));
+    fence_mbar_init();
+  }
+  __syncwarp();
+
+  int64_t ps = it.seg_b + sl;  // producer cursor of this slice (used by its first lane)
+  int pc = 0;
+#define HODLR_SMALL_ISSUE(q_)                                                                                   \
+  do {                                                                                                          \
+    if (i != 0) break;                                                                                          \
+    const int st_ = (q_) % kSStages;                                                                            \
+    if (ps >= it.seg_e) {                                                                                       \
+      mbar_arrive(bar + st_);                                                                                   \
+      break;                                                                                                    \
+    }                                                                                                           \
+    const Seg S_ = segs[ps];                                                                                    \
+    const int c_ = min(cmax, S_.K - pc);                                                                        \
+    unsigned char* su_ = stage0 + st_ * (kSUBytes + kSXBytes) + sl * ub;                                        \
+    unsigned char* sx_ = stage0 + st_ * (kSUBytes + kSXBytes) + kSUBytes + sl * xb;                             \
+    /* pc is a multiple of Q, so the piece starts 16-byte aligned; the rounded                                 \
+       size stays inside the block's storage (padded to 16 bytes) */                                            \
+    const TA* A_ = static_cast<const TA*>(S_.A) + int64_t(pc) * m;                                              \
+    const uint32_t bu_ = uint32_t((c_ * m * esz + 15) & ~15);                                                   \
+    const unsigned char* xs_ = reinterpret_cast<const unsigned char*>(inc + S_.in_off + pc);                    \
+    const unsigned char* xa_ = static_cast<const unsigned char*>(align_down16(xs_));                            \
+    const uint32_t bx_ = uint32_t((xs_ + size_t(c_) * sizeof(TX) - xa_ + 15) & ~size_t(15));                    \
+    fence_proxy_async();                                                                                        \
+    mbar_expect_tx(bar + st_, bu_ + bx_);                                                                       \
+    bulk_g2s(su_, A_, bu_, bar + st_);                                                                          \
+    bulk_g2s(sx_, xa_, bx_, bar + st_);                                                                         \
+    pc += c_;                                                                                                   \
+    if (pc >= S_.K) {                                                                                           \
+      ps += slices;                                                                                             \
+      pc = 0;                                                                                                   \
+    }                                                                                                           \
+  } while (0)
+  for (int q = 0; q < min(kSStages, rounds); q++) HODLR_SMALL_ISSUE(q);
+  typename AC::A a0 = AC::zero(), a1 = AC::zero();
+  int64_t cs = it.seg_b + sl;  // consumer cursor
+  int cc = 0;
+  for (int q = 0; q < rounds; q++) {
+    const int st = q % kSStages;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(bar + st, uint32_t(q / kSStages) & 1u));
+    if (!ok) {
+      if (lane == 0) atomicAdd(&g_stream_timeouts, 1u);
+      for (int t = q; t < min(q + kSStages, rounds); t++) mbar_wait(bar + t % kSStages, uint32_t(t / kSStages) & 1u);
+      return;
+    }
+    if (cs < it.seg_e) {
+      const Seg S = segs[cs];
+      const int c = min(cmax, S.K - cc);
+      const TA* su = reinterpret_cast<const TA*>(stage0 + st * (kSUBytes + kSXBytes) + sl * ub);
+      const int xo = int((reinterpret_cast<uintptr_t>(inc + S.in_off + cc) & 15u) / sizeof(TX));
+      const TX* sx = reinterpret_cast<const TX*>(stage0 + st * (kSUBytes + kSXBytes) + kSUBytes + sl * xb) + xo;
+      if (i < m) {
+        int j = 0;
+        for (; j + 1 < c; j += 2) {
+          AC::fma(a0, su[j * m + i], AC::in(sx[j]));
+          AC::fma(a1, su[(j + 1) * m + i], AC::in(sx[j + 1]));
+        }
+        if (j < c) AC::fma(a0, su[j * m + i], AC::in(sx[j]));
+      }
+      cc += c;
+      if (cc >= S.K) {
+        cs += slices;
+        cc = 0;
+      }
+    }
+    __syncwarp();  // round q's stage is refilled for round q + kSStages
+    if (q + kSStages < rounds) HODLR_SMALL_ISSUE(q + kSStages);
+  }
+#undef HODLR_SMALL_ISSUE
+  typename AC::A acc = AC::add(a0, a1);
+  for (int o = mpad; o < 32; o <<= 1) acc = AC::add(acc, AC::shfl_xor(acc, o));
+  if (sl == 0 && i < m) yo[i] = TY(AC::value(acc));
+}
+
+// Phase 2, panels of more than 32 rows: item chunk = row tile t of the
+// panel (T = 512 / sizeof(TA) rows, lane l owns rows t*T + l*RPL ..).  Every
+// segment's tile is h x K, column major with column stride h (h = the tile's
+// row count rounded up to 4), so a run of its columns is one contiguous byte
+// range, and so is the run of their input values.  Both are staged through a
+// per-warp ring of kPStages shared-memory stages by bulk copies, at most
+// kPStageBytes of tile and kPCols columns per stage.  Column j of a segment
+// goes to accumulator set j & 1.
+constexpr int kPWarps = 4;           // warps per CTA of panel_tile_kernel
+constexpr int kPStages = 3;
+constexpr int kPStageBytes = 4096;
+constexpr int kPCols = 64;           // columns per stage at most
+constexpr int kPXBytes = kPCols * 8 + 32;
+constexpr int kPWarpSmem = 64 + kPStages * (kPStageBytes + kPXBytes);
+static_assert(kPWarpSmem % 16 == 0 && kPXBytes % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
+
+template <typename TA, typename TACC>
+__global__ void __launch_bounds__(kPWarps * 32, 4)
+    panel_tile_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
+                      int nitems, typename IO<TACC>::TY* __restrict__ ypart,
+                      const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
+                      typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
+  using TX = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
+  constexpr int RPL = 16 / int(sizeof(TA));
+  constexpr int T = 32 * RPL;
+  using VT = typename Vec16<TA>::type;
+  using AC = Acc<TACC>;
+  extern __shared__ __align__(16) unsigned char psm[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kPWarps + wid;
+  if (w >= nitems) return;
+  const Item it = items[w];
+  const Panel P = panels[it.panel];
+  const int m = P.m;
+  const TX* inc = in + blockIdx.y * ld_in;
+  const int t = it.chunk;
+  const int rows = min(T, m - t * T);
+  const int64_t h = tile_height(m, t, int(sizeof(TA)));
+  const int colb = int(h) * int(sizeof(TA));  // bytes per tile column: 16 .. 512, a multiple of 16
+  const int cps = min(kPCols, kPStageBytes / colb);
+  const bool act = lane * RPL < rows;
+  typename AC::A a0[RPL], a1[RPL];
+#pragma unroll
+  for (int q = 0; q < RPL; q++) a0[q] = a1[q] = AC::zero();
+
+  unsigned char* base = psm + wid * kPWarpSmem;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  unsigned char* ubuf = base + 64;
+  unsigned char* xbuf = ubuf + kPStages * kPStageBytes;
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < kPStages; s++) mbar_init(bar + s, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  // producer cursor (segment, first column); every lane keeps it, lane 0 issues
+  int64_t ps = it.seg_b;
+  int pc = 0, issued = 0;
+#define HODLR_PANEL_ISSUE_NEXT()                                                                                  \
+  do {                                                                                                            \
+    while (ps < it.seg_e && pc >= segs[ps].K) {                                                                   \
+      ps++;                                                                                                       \
+      pc = 0;                                                                                                     \
+    }                                                                                                             \
+    if (ps >= it.seg_e) break;                                                                                    \
+    const Seg S_ = segs[ps];                                                                                      \
+    const int nc_ = min(cps, S_.K - pc);                                                                          \
+    if (lane == 0) {                                                                                              \
+      const int st_ = issued % kPStages;                                                                          \
+      /* U tile t starts at element t*T*K: 16-byte aligned since T * sizeof(TA) = 512 */                          \
+      const TA* src_ = static_cast<const TA*>(S_.A) + int64_t(t) * T * S_.K + int64_t(pc) * h;                    \
+      const uint32_t ub_ = uint32_t(nc_) * uint32_t(colb);                                                        \
+      const unsigned char* xs_ = reinterpret_cast<const unsigned char*>(inc + S_.in_off + pc);                    \
+      const unsigned char* xa_ = static_cast<const unsigned char*>(align_down16(xs_));                            \
+      const uint32_t xb_ = uint32_t((xs_ + size_t(nc_) * sizeof(TX) - xa_ + 15) & ~size_t(15));                   \
+      fence_proxy_async();                                                                                        \
+      mbar_expect_tx(bar + st_, ub_ + xb_);                                                                       \
+      bulk_g2s(ubuf + st_ * kPStageBytes, src_, ub_, bar + st_);                                                  \
+      bulk_g2s(xbuf + st_ * kPXBytes, xa_, xb_, bar + st_);                                                       \
+    }                                                                                                             \
+    pc += nc_;                                                                                                    \
+    issued++;                                                                                                     \
+  } while (0)
+  for (int q = 0; q < kPStages; q++) HODLR_PANEL_ISSUE_NEXT();
+  // consumer cursor
+  int64_t cs = it.seg_b;
+  int cc = 0;
+  for (int q = 0; q < issued; q++) {
+    while (cc >= segs[cs].K) {
+      cs++;
+      cc = 0;
+    }
+    const Seg S = segs[cs];
+    const int nc = min(cps, S.K - cc);
+    const int st = q % kPStages;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(bar + st, uint32_t(q / kPStages) & 1u));
+    if (!ok) {
+      if (lane == 0) atomicAdd(&g_stream_timeouts, 1u);
+      for (int u = q; u < issued; u++) mbar_wait(bar + u % kPStages, uint32_t(u / kPStages) & 1u);
+      return;
+    }
+    const int xo = int((reinterpret_cast<uintptr_t>(inc + S.in_off + cc) & 15u) / sizeof(TX));
+    const TX* xsm = reinterpret_cast<const TX*>(xbuf + st * kPXBytes) + xo;
+    const unsigned char* us = ubuf + st * kPStageBytes + lane * 16;
+    int j = 0;
+    for (; j + 1 < nc; j += 2) {
+      const VT v0 = act ? *reinterpret_cast<const VT*>(us + j * colb) : vzero<VT>();
+      const VT v1 = act ? *reinterpret_cast<const VT*>(us + (j + 1) * colb) : vzero<VT>();
+      // column cc + j has the parity of cc + j
+      if (((cc + j) & 1) == 0) {
+        axpy16<TACC>(v0, AC::in(xsm[j]), a0);
+        axpy16<TACC>(v1, AC::in(xsm[j + 1]), a1);
+      } else {
+        axpy16<TACC>(v0, AC::in(xsm[j]), a1);
+        axpy16<TACC>(v1, AC::in(xsm[j + 1]), a0);
+      }
+    }
+    if (j < nc) {
+      const VT v0 = act ? *reinterpret_cast<const VT*>(us + j * colb) : vzero<VT>();
+      if (((cc + j) & 1) == 0)
+        axpy16<TACC>(v0, AC::in(xsm[j]), a0);
+      else
+        axpy16<TACC>(v0, AC::in(xsm[j]), a1);
+    }
+    cc += nc;
+    __syncwarp();
+    HODLR_PANEL_ISSUE_NEXT();  // the next run, if any, into the stage just consumed
+  }
+#undef HODLR_PANEL_ISSUE_NEXT
+  if (act) {
+    const int i = t * T + lane * RPL;
+    TY* dst = it.part < 0 ? y + int64_t(blockIdx.y) * nslots * ld_y + P.yoff + i
+                          : ypart + int64_t(it.part) * T + lane * RPL;
+#pragma unroll
+    for (int q = 0; q < RPL; q++)
+      if (i + q < m) dst[q] = TY(AC::value(AC::add(a0[q], a1[q])));
+  }
+}
+
+// ---- direct-load variants, used for FP64 factors ----------------------------
+// FP64 products run on GB300's FP64 pipe, whose rate (not the bytes in
+// flight) bounds these kernels; plain loads with eight warps per CTA keep
+// that pipe busier than the shared-memory staged versions above.  Same lane
+// layouts and summation orders as described above for each phase.
+template <typename TA, typename TACC>
+__global__ void __launch_bounds__(256) zgemv_direct_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
                                                     int nitems, typename IO<TACC>::TY* __restrict__ zpart,
                                                     typename IO<TACC>::TI* in, int64_t ld_in) {
   using TX = typename IO<TACC>::TI;
@@ -235,26 +700,9 @@ __global__ void __launch_bounds__(256) zgemv_kernel(const ZBlock* __restrict__ z
   }
 }
 
-template <typename TACC>
-__global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const typename IO<TACC>::TY* __restrict__ zpart,
-                            typename IO<TACC>::TI* in, int64_t ld_in) {
-  using TY = typename IO<TACC>::TY;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= nfix) return;
-  const ZFix F = fix[f];
-  TY acc = TY(0);
-  for (int q = 0; q < F.count; q++) acc += zpart[F.part + q * kZPart];
-  in[blockIdx.y * ld_in + F.zpos] = IO<TACC>::from_double(double(acc));
-}
-
-// Phase 2, panels of at most 32 rows (leaves): lanes form 32 / mpad slices of
-// mpad lanes (mpad = next power of two >= m), one lane per row; slice sl
-// walks segments sl, sl + slices, ... of the item on its own, four columns
-// per step, so a warp has several small tiles in flight at once.  The slices
-// are added by shuffles at the end.
 template <typename TA, typename TACC>
 __global__ void __launch_bounds__(256)
-    panel_small_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
+    panel_small_direct_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
                        int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
                        typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
   using TX = typename IO<TACC>::TI;
@@ -266,7 +714,7 @@ __global__ void __launch_bounds__(256)
   const Panel P = panels[it.panel];
   const int m = P.m;
   const TX* inc = in + blockIdx.y * ld_in;
-  TY* yo = y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin;
+  TY* yo = y + int64_t(blockIdx.y) * nslots * ld_y + P.yoff;
   int mpad = 1;
   while (mpad < m) mpad <<= 1;
   const int slices = 32 / mpad;
@@ -296,13 +744,9 @@ __global__ void __launch_bounds__(256)
   if (sl == 0 && i < m) yo[i] = TY(AC::value(acc));
 }
 
-// Phase 2, panels of more than 32 rows: item chunk = row tile t of the
-// panel; every segment's tile is streamed column by column, 16 bytes per
-// lane (rows t*T + lane*RPL ..).  Input values come 32 at a time from one
-// coalesced load and are broadcast by shuffle.
 template <typename TA, typename TACC>
 __global__ void __launch_bounds__(256)
-    panel_tile_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
+    panel_tile_direct_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
                       int nitems, typename IO<TACC>::TY* __restrict__ ypart,
                       const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
@@ -353,7 +797,7 @@ __global__ void __launch_bounds__(256)
   }
   if (act) {
     const int i = t * T + lane * RPL;
-    TY* dst = it.part < 0 ? y + (int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin + i
+    TY* dst = it.part < 0 ? y + int64_t(blockIdx.y) * nslots * ld_y + P.yoff + i
                           : ypart + int64_t(it.part) * T + lane * RPL;
 #pragma unroll
     for (int q = 0; q < RPL; q++)
@@ -376,7 +820,7 @@ __global__ void __launch_bounds__(256) panel_fix_kernel(const Panel* __restrict_
   if (i >= P.m) return;
   TX acc = TX(0);
   for (int g = 0; g < F.count; g++) acc += ypart[int64_t(F.part + g) * rows + q];
-  y[(int64_t(blockIdx.y) * nslots + P.slot) * ld_y + P.row_begin + i] = acc;
+  y[int64_t(blockIdx.y) * nslots * ld_y + P.yoff + i] = acc;
 }
 
 template <typename TX, typename TO>
@@ -423,6 +867,7 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
   const CompactDesc B = blocks[blockIdx.x];
   TO* u = static_cast<TO*>(B.u_dst);
   constexpr int esz = int(sizeof(TO));
+  if (B.kscale != 0.0) K.scale = B.kscale;
   if (B.dense) {
     const int64_t total = int64_t(B.m) * B.n;
     for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
@@ -466,8 +911,15 @@ static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix
                     int64_t ld_in, int nrhs, cudaStream_t st) {
   using TI = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
-  dim3 g(warps_grid(nitems), unsigned(nrhs));
-  zgemv_kernel<TA, TACC><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<TY*>(zpart), static_cast<TI*>(in), ld_in);
+  if (sizeof(TA) == 8) {
+    dim3 g(warps_grid(nitems), unsigned(nrhs));
+    zgemv_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<TY*>(zpart),
+                                                     static_cast<TI*>(in), ld_in);
+  } else {
+    dim3 g(unsigned((nitems + kZWarps - 1) / kZWarps), unsigned(nrhs));
+    zgemv_kernel<TA, TACC><<<g, kZWarps * 32, kZWarps * kZWarpSmem, st>>>(zb, items, nitems, static_cast<TY*>(zpart),
+                                                                           static_cast<TI*>(in), ld_in);
+  }
   if (nfix > 0) {
     dim3 gf(unsigned((nfix + 255) / 256), unsigned(nrhs));
     zfix_kernel<TACC><<<gf, 256, 0, st>>>(fix, nfix, static_cast<const TY*>(zpart), static_cast<TI*>(in), ld_in);
@@ -475,13 +927,15 @@ static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix
 }
 
 cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
-                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st, bool df) {
+                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st, Accum acc) {
   if (nitems <= 0) return cudaSuccess;
   count_launches(nfix > 0 ? 2 : 1);
   if (a == Prec::kD && x == Prec::kD)
     zgemv_t<double, double>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
-  else if (a == Prec::kF && x == Prec::kD && df)
+  else if (a == Prec::kF && x == Prec::kD && acc == Accum::kCompensated)
     zgemv_t<float, DF>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+  else if (a == Prec::kF && x == Prec::kD && acc == Accum::kRelaxed)
+    zgemv_t<float, FH>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else if (a == Prec::kF && x == Prec::kF)
     zgemv_t<float, float>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else
@@ -495,15 +949,31 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
                      int nslots, int nrhs, cudaStream_t st) {
   using TI = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
-  if (nbig > 0) {
+  if (nbig > 0 && sizeof(TA) == 8) {
     dim3 g(warps_grid(nbig), unsigned(nrhs));
-    panel_tile_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, big, nbig, static_cast<TY*>(ypart),
-                                                   static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots);
+    panel_tile_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, big, nbig, static_cast<TY*>(ypart),
+                                                          static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y,
+                                                          nslots);
+  } else if (nbig > 0) {
+    dim3 g(unsigned((nbig + kPWarps - 1) / kPWarps), unsigned(nrhs));
+    // above the default 48 KB of dynamic shared memory; set on every launch
+    // (the attribute is per device and cheap to set)
+    cudaFuncSetAttribute(panel_tile_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kPWarps * kPWarpSmem);
+    panel_tile_kernel<TA, TACC><<<g, kPWarps * 32, kPWarps * kPWarpSmem, st>>>(
+        panels, segs, big, nbig, static_cast<TY*>(ypart), static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y,
+        nslots);
   }
-  if (nsmall > 0) {
+  if (nsmall > 0 && sizeof(TA) == 8) {
     dim3 g(warps_grid(nsmall), unsigned(nrhs));
-    panel_small_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in,
-                                                    static_cast<TY*>(y), ld_y, nslots);
+    panel_small_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TI*>(in),
+                                                           ld_in, static_cast<TY*>(y), ld_y, nslots);
+  } else if (nsmall > 0) {
+    dim3 g(unsigned((nsmall + kSWarps - 1) / kSWarps), unsigned(nrhs));
+    cudaFuncSetAttribute(panel_small_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kSWarps * kSWarpSmem);
+    panel_small_kernel<TA, TACC><<<g, kSWarps * 32, kSWarps * kSWarpSmem, st>>>(
+        panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots);
   }
   if (nfix > 0) {
     const int rows = int(tile_rows(int(sizeof(TA))));
@@ -515,20 +985,78 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
 
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
-                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st, bool df) {
+                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st, Accum acc) {
   if (nsmall + nbig <= 0) return cudaSuccess;
   count_launches(uint64_t(nbig > 0) + uint64_t(nsmall > 0) + uint64_t(nfix > 0));
   if (a == Prec::kD && x == Prec::kD)
     panels_t<double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots,
                              nrhs, st);
-  else if (a == Prec::kF && x == Prec::kD && df)
+  else if (a == Prec::kF && x == Prec::kD && acc == Accum::kCompensated)
     panels_t<float, DF>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
+                        st);
+  else if (a == Prec::kF && x == Prec::kD && acc == Accum::kRelaxed)
+    panels_t<float, FH>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
                         st);
   else if (a == Prec::kF && x == Prec::kF)
     panels_t<float, float>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
                            st);
   else
     return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) batch_gather_kernel(const BatchInst* __restrict__ inst, const T* __restrict__ x,
+                                                           T* __restrict__ in) {
+  const BatchInst I = inst[blockIdx.y];
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < I.n; r += int64_t(gridDim.x) * blockDim.x)
+    in[I.in_base + r] = x[I.x_base + I.perm[r]];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) batch_combine_kernel(const BatchInst* __restrict__ inst, const T* __restrict__ y,
+                                                            T* __restrict__ out) {
+  const BatchInst I = inst[blockIdx.y];
+  for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < I.n; r += int64_t(gridDim.x) * blockDim.x) {
+    const T* yc = y + I.y_base + r;
+    double acc = double(yc[0]);
+    for (int s = 1; s < I.nslots; s++) acc += double(yc[int64_t(s) * I.n]);
+    out[I.x_base + I.perm[r]] = T(acc);
+  }
+}
+
+namespace {
+dim3 batch_grid(int count, int64_t max_n) {
+  int64_t g = (max_n + 255) / 256;
+  if (g > 64) g = 64;
+  if (g < 1) g = 1;
+  return dim3(unsigned(g), unsigned(count));
+}
+}  // namespace
+
+cudaError_t launch_batch_gather(Prec x, const BatchInst* inst, int count, int64_t max_n, const void* src, void* in,
+                                cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  count_launches(1);
+  if (x == Prec::kD)
+    batch_gather_kernel<double><<<batch_grid(count, max_n), 256, 0, st>>>(inst, static_cast<const double*>(src),
+                                                                           static_cast<double*>(in));
+  else
+    batch_gather_kernel<float><<<batch_grid(count, max_n), 256, 0, st>>>(inst, static_cast<const float*>(src),
+                                                                          static_cast<float*>(in));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_combine(Prec x, const BatchInst* inst, int count, int64_t max_n, const void* y, void* out,
+                                 cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  count_launches(1);
+  if (x == Prec::kD)
+    batch_combine_kernel<double><<<batch_grid(count, max_n), 256, 0, st>>>(inst, static_cast<const double*>(y),
+                                                                            static_cast<double*>(out));
+  else
+    batch_combine_kernel<float><<<batch_grid(count, max_n), 256, 0, st>>>(inst, static_cast<const float*>(y),
+                                                                           static_cast<float*>(out));
   return cudaGetLastError();
 }
 

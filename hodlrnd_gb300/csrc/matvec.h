@@ -26,6 +26,8 @@ struct Panel {
   int64_t seg_begin, seg_end;
   int32_t m;          // rows
   int32_t slot;       // output slot
+  int64_t yoff;       // offset of the first row's output in a column of the slots (slot * ld_y + row_begin
+                      // for one operator; the instance's base added in a batch plan)
 };
 
 // Storage of an m x K matrix (near tiles, dense far blocks, factors U and V).
@@ -119,19 +121,43 @@ enum class Prec { kD, kF };  // double, float
 // in:   input buffer [x (ld_in rows of x) | z], nrhs columns with leading dimension ld_in
 // y:    output slots, slot s of column c at y + (c * nslots + s) * ld_y
 // zpart / ypart: scratch of the vector precision (one column of partials).
-// df: FP32 matrices with FP64 vectors, accumulated in compensated FP32
-// (FP64-level accuracy on the FP32 pipe); the input buffer `in` then holds
-// each FP64 value split into an (hi, lo) FP32 pair (launch_split), and z is
-// written in the same form.  Outputs and partial sums stay FP64.
+// acc, for FP32 matrices with FP64 vectors: the input buffer `in` holds each
+// FP64 value split into an (hi, lo) FP32 pair (launch_split), z is written in
+// the same form, outputs and partial sums stay FP64, and products are summed
+// * kCompensated: in compensated FP32 (FP64-level accuracy on the FP32 pipe);
+// * kRelaxed: in plain FP32 from the high parts (about 1e-6 relative).
+// Other type pairs ignore it.
+enum class Accum { kByType, kCompensated, kRelaxed };
 cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix,
-                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st, bool df = false);
+                         void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st,
+                         Accum acc = Accum::kByType);
 // `small` items belong to panels of at most 32 rows, `big` ones to larger panels.
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
                           int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st,
-                          bool df = false);
+                          Accum acc = Accum::kByType);
+// One instance of a batch of operators: its n rows sit at x_base in the
+// caller's concatenated vectors, at in_base in the batch's input buffer and
+// at y_base in the batch's output slots (nslots slots of n rows each).
+struct BatchInst {
+  int64_t n, x_base, in_base, y_base;
+  const int64_t* perm;  // tree position -> caller index within the instance
+  int32_t nslots, pad;
+};
+// in[in_base + r] = x[x_base + perm[r]] for every instance (vectors of type x)
+cudaError_t launch_batch_gather(Prec x, const BatchInst* inst, int count, int64_t max_n, const void* src, void* in,
+                                cudaStream_t st);
+// out[x_base + perm[r]] = sum over the instance's slots s of y[y_base + s n + r]
+cudaError_t launch_batch_combine(Prec x, const BatchInst* inst, int count, int64_t max_n, const void* y, void* out,
+                                 cudaStream_t st);
+
 // out[i] = (hi, lo) FP32 pair of x[i] (hi = x rounded to FP32, lo = the rest)
 cudaError_t launch_split(const double* x, void* out, int64_t n, cudaStream_t st);
+
+// Copies to `host` (pinned) the number of times a streaming kernel on this
+// device gave up waiting for its bulk copies since the library was loaded
+// (every wait is bounded); the value is valid once `st` has synchronised.
+cudaError_t read_stream_timeouts(unsigned int* host, cudaStream_t st);
 // rows handled by one big-panel item for stored element size `a`
 inline int rows_per_item(Prec a) { return a == Prec::kD ? 64 : 128; }
 // out[perm[i] + c*ld_out] (or out[i + c*ld_out] when perm == NULL) =
@@ -165,6 +191,7 @@ struct CompactDesc {
   int32_t m, n, rank, dense;
   int32_t cap;        // workspace columns (V starts after m * cap doubles)
   int32_t pad;
+  double kscale;      // kernel scale for a dense block's entries; 0: the launch's K.scale
 };
 // U row i (reference order) lands on tree row lmap[t_map + i] - t_begin; V likewise.
 cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,

@@ -27,7 +27,7 @@ def _dp(a):
 class HODLRdD_matrix:
     def __init__(self, userkernel, gridPoints, x1, x2, *, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0,
                  precision="fp64", restart=100, tol=None, max_iter=0, device=0, device_budget_bytes=0, rank_cap=0,
-                 inner_tol=0.0, max_outer=0):
+                 inner_tol=0.0, max_outer=0, ortho="auto", relax=True):
         self.kernel = userkernel
         self.points = np.ascontiguousarray(gridPoints, dtype=np.float64)
         if self.points.ndim != 2:
@@ -54,6 +54,8 @@ class HODLRdD_matrix:
         p.rank_cap = int(rank_cap)
         p.inner_tol = float(inner_tol)
         p.max_outer = int(max_outer)
+        p.ortho = {"auto": _lib.HODLR_ORTHO_AUTO, "mgs": _lib.HODLR_ORTHO_MGS, "cgs2": _lib.HODLR_ORTHO_CGS2}[ortho]
+        p.relax = _lib.HODLR_RELAX_AUTO if relax else _lib.HODLR_RELAX_OFF
         self.params = p
         self._ctx = None
         self._op = None

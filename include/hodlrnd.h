@@ -41,6 +41,7 @@ extern "C" {
 #define HODLR_ERR_STATE 7         /* call out of order (e.g. matvec before build) */
 #define HODLR_ERR_DEVICE 8        /* a device-side check failed (index or size out of range) */
 #define HODLR_ERR_IO 9            /* a file could not be read or written, or is malformed */
+#define HODLR_ERR_TIMEOUT 10      /* hodlr_server_wait: the request has not finished within the timeout */
 
 /* ---- kernels --------------------------------------------------------- */
 /* Entry A_ij for i != j with r = |x_i - x_j| (Euclidean, include/points_dt.hpp:31-39);
@@ -81,7 +82,25 @@ typedef struct hodlr_params {
   int32_t rank_cap;  /* initial ACA workspace columns per block (0 = default); grown on demand */
   int32_t max_outer; /* MIXED: iterative-refinement sweeps (0 = default 10) */
   double inner_tol;  /* MIXED: relative-residual target of each FP32 inner GMRES (<= 0: default 1e-4) */
+  int32_t ortho;     /* GMRES orthogonalisation, HODLR_ORTHO_* */
+  int32_t relax;     /* FP32_FACTORS: HODLR_RELAX_AUTO (relaxed products once the residual allows) or _OFF */
 } hodlr_params;
+
+/* FP32_FACTORS solves: once GMRES's residual estimate is below tol * 1e6, the
+ * matvecs sum the FP32 products in plain FP32 (about 1e-6 relative, which an
+ * inexact Krylov method tolerates at that residual) instead of compensated
+ * FP32; the solve ends only when the true residual, with compensated
+ * products, is at most tol (GMRES continues from x otherwise). */
+#define HODLR_RELAX_AUTO 0
+#define HODLR_RELAX_OFF 1
+
+/* GMRES orthogonalisation.  MGS is the reference's (include/GMRES.hpp:236-240)
+ * and needs i + 2 kernel launches at Arnoldi step i; CGS2 (classical
+ * Gram-Schmidt applied twice) needs six at any step and is as orthogonal.
+ * AUTO: MGS for HODLR_PREC_FP64 (the reference's arithmetic), CGS2 otherwise. */
+#define HODLR_ORTHO_AUTO 0
+#define HODLR_ORTHO_MGS 1
+#define HODLR_ORTHO_CGS2 2
 
 /* Fill p with the reference's defaults: ndim 2, Nmax 64, d' 0, eps 1e-10,
  * restart 100, tol = eps, max_iter = N, FP64.  No counterpart in the
@@ -240,6 +259,113 @@ int hodlr_aca_block_noalloc(const double* d_points, int64_t ld, int32_t ndim, co
                             const int32_t* d_cols, int32_t n, const hodlr_kernel_desc* kernel, double eps_aca,
                             uint64_t seed, int32_t cap, double* d_factors, int32_t* rank, int32_t* flags,
                             void* stream);
+
+/* ---- batches of independent operators ---------------------------------- */
+/* No counterpart in the reference (one HODLRdD_matrix per caller,
+ * include/HDD_matrix.hpp:20-62).  count operators built on ctx's parameters,
+ * instance i from points[i] (n[i] x ndim, row major), box box_lo/hi +
+ * i*ndim and kernels[i] (one kind and diagonal for all, scales may differ).
+ * The far blocks of every instance are compressed together (they share each
+ * ACA launch); each instance keeps its own storage and is an ordinary
+ * operator (hodlr_batch_op: solve, matvec, statistics; owned by the batch).
+ * The batch also holds one merged plan over all instances. */
+typedef struct hodlr_batch hodlr_batch;
+int hodlr_build_batch(hodlr_ctx* ctx, int32_t count, const double* const* points, const int64_t* n,
+                      const double* box_lo, const double* box_hi, const hodlr_kernel_desc* kernels,
+                      hodlr_batch** out);
+/* offsets[0..count]: instance i occupies rows offsets[i] .. offsets[i+1]-1 of a batch vector. */
+int hodlr_batch_offsets(const hodlr_batch* batch, int64_t* offsets);
+int hodlr_batch_op(hodlr_batch* batch, int32_t i, hodlr_op** op);
+/* Y = A X for every instance at once: X and Y are device arrays of
+ * offsets[count] x nrhs (column major, each instance's rows in its caller's
+ * order) of FP32 for HODLR_PREC_MIXED, FP64 otherwise.  Every column of every
+ * instance is one launch per phase of the merged plan; the whole sequence is
+ * captured as a CUDA graph on the first call with these (X, Y, nrhs) and
+ * replayed on `stream` afterwards.  Asynchronous. */
+int hodlr_batch_matvec_device(hodlr_batch* batch, const void* d_x, void* d_y, int64_t nrhs, void* stream);
+int hodlr_batch_destroy(hodlr_batch* batch);
+
+/* ---- request loop (serving) --------------------------------------------- */
+/* No counterpart in the reference, which builds and solves one
+ * HODLRdD_matrix at a time in its caller (include/HDD_matrix.hpp:20-62).
+ *
+ * A server owns `slots` worker threads.  Requests (a geometry -- points, box,
+ * kernel, parameters -- and nrhs right-hand sides) are queued by
+ * hodlr_server_submit, which copies every input and returns at once.  A
+ * worker admits the first queued request whose predicted device bytes
+ * (hodlr_predict_bytes, corrected by what earlier builds measured) fit in
+ * memory_budget_bytes next to the resident geometries and the other running
+ * requests, evicting idle resident geometries least recently used first.
+ * Each geometry has its own CUDA stream, so running requests overlap on the
+ * device.  A request with a nonzero geometry_key keeps its operator resident
+ * after it finishes; a later request with the same key may pass points =
+ * NULL and is solved on the resident operator (requests on one operator run
+ * one at a time).  Results are bit-identical to solving the same request
+ * alone: every kernel is deterministic and no work is shared between
+ * requests.
+ *
+ * simulate = 1 runs the same admission and scheduling without a GPU (builds
+ * and solves take a nominal time, x = b); it exists for capacity planning and
+ * for testing the scheduler. */
+typedef struct hodlr_server hodlr_server;
+
+typedef struct hodlr_server_params {
+  int32_t device;               /* CUDA device of every geometry */
+  int32_t slots;                /* requests running at once (worker threads); 0 = 4 */
+  uint64_t memory_budget_bytes; /* device bytes for resident and running geometries; 0 = 150 GiB */
+  int32_t simulate;             /* 1: no GPU work (see above) */
+  int32_t reserved;
+} hodlr_server_params;
+
+typedef struct hodlr_request {
+  uint64_t geometry_key;     /* 0: do not keep the operator resident */
+  hodlr_params params;       /* per-request parameters (params.device is ignored) */
+  hodlr_kernel_desc kernel;
+  const double* points;      /* n x ndim, row major; NULL to reuse the resident geometry_key */
+  const double* box_lo;      /* ndim each; may be NULL with points == NULL */
+  const double* box_hi;
+  int64_t n;
+  const double* b;           /* n x nrhs, column major, caller's point order */
+  int64_t nrhs;
+} hodlr_request;
+
+typedef struct hodlr_result {
+  int32_t status;            /* HODLR_OK, HODLR_ERR_NOT_CONVERGED, or the failure */
+  int32_t built;             /* 1: this request built its operator; 0: it was resident */
+  int64_t iterations;        /* GMRES iterations summed over the right-hand sides */
+  double rel_residual;       /* worst over the right-hand sides */
+  double t_queue_s;          /* submit -> admission */
+  double t_build_s;          /* operator build (0 when resident) */
+  double t_solve_s;          /* all right-hand sides, host copies included */
+  double t_total_s;          /* submit -> completion */
+  uint64_t predicted_bytes;  /* reserved at admission for a build */
+  uint64_t actual_bytes;     /* the operator's device footprint */
+  char message[128];         /* failure message, empty on success */
+} hodlr_result;
+
+typedef struct hodlr_server_stats {
+  uint64_t submitted, completed, rejected, builds, resident_hits, evictions, rhs_solved;
+  int64_t queued, running, resident;
+  uint64_t used_bytes;
+} hodlr_server_stats;
+
+int hodlr_server_create(const hodlr_server_params* params, hodlr_server** out);
+int hodlr_server_submit(hodlr_server* server, const hodlr_request* request, uint64_t* ticket);
+/* Waits up to timeout_s (< 0: no limit) for the request; on completion writes
+ * x (n x nrhs, caller's order; may be NULL) and *result (may be NULL), forgets
+ * the ticket and returns result->status.  HODLR_ERR_TIMEOUT if still running. */
+int hodlr_server_wait(hodlr_server* server, uint64_t ticket, double timeout_s, double* x, hodlr_result* result);
+int hodlr_server_stats_get(hodlr_server* server, hodlr_server_stats* out);
+/* Finishes every submitted request, then frees the resident geometries. */
+int hodlr_server_destroy(hodlr_server* server);
+
+/* Predicted device bytes of hodlr_build + solves for these inputs: tree,
+ * lists and near field exactly; far-block ranks from a prior model of rank
+ * versus eps_aca, ndim and block size; plus the build's ACA workspace.  Host
+ * only.  No counterpart in the reference (its print_matrix_statistics reports
+ * the memory after the build, include/HDD_matrix.hpp:69-85). */
+int hodlr_predict_bytes(const hodlr_params* params, const double* points, int64_t n, const double* box_lo,
+                        const double* box_hi, uint64_t* bytes);
 
 /* ---- vector files (host only) ------------------------------------------ */
 /* storedata::load_vec / save_vec (include/myHeaders.hpp:146-170): a cereal

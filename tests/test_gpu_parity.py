@@ -215,3 +215,40 @@ def test_budget_is_enforced():
     with pytest.raises(_lib.HodlrError) as e:
         build(c, f["points"], device_budget_bytes=1 << 16)
     assert e.value.code == _lib.HODLR_ERR_BUDGET
+
+
+def test_cgs2_orthogonalisation_matches_mgs():
+    """CGS2 (six launches per Arnoldi step) against the reference's MGS on the
+    FP64 operator: same iteration count within 2, same solution within 1e-10."""
+    c = cases.REF_CASES["hodlr3d_n4096"]
+    f = dict(np.load(os.path.join(GOLDEN, "ref_hodlr3d_n4096.npz")))
+    Mm = build(c, f["points"], ortho="mgs")
+    Mc = build(c, f["points"], ortho="cgs2")
+    xm = Mm.solve(f["b"])
+    xc = Mc.solve(f["b"])
+    im, ic = Mm.last_solve, Mc.last_solve
+    assert ic["converged"] == 1 and ic["rel_residual"] <= c["eps"]
+    assert abs(im["iterations"] - ic["iterations"]) <= 2
+    assert rel(xc, xm) < 1e-10
+    Mm.close()
+    Mc.close()
+
+
+def test_relaxed_products_keep_the_true_residual():
+    """FP32 factors: plain-FP32 products once the residual estimate allows it
+    (inexact GMRES), compensated products for the final true residual."""
+    c = cases.REF_CASES["hodlr3d_n4096"]
+    f = dict(np.load(os.path.join(GOLDEN, "ref_hodlr3d_n4096.npz")))
+    Mr = build(c, f["points"], precision="fp32_factors")
+    Mc = build(c, f["points"], precision="fp32_factors", relax=False)
+    xr = Mr.solve(f["b"])
+    xc = Mc.solve(f["b"])
+    ir, ic = Mr.last_solve, Mc.last_solve
+    assert ir["converged"] == 1 and ir["rel_residual"] <= c["eps"]
+    assert ic["converged"] == 1 and ic["rel_residual"] <= c["eps"]
+    # the true residual with compensated products, recomputed here
+    r = f["b"] - Mc * xr
+    assert np.linalg.norm(r) / np.linalg.norm(f["b"]) <= c["eps"]
+    assert rel(xr, xc) < 1e-6
+    Mr.close()
+    Mc.close()
