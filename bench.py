@@ -509,6 +509,88 @@ def run_serving(args):
     print(json.dumps(out), flush=True)
 
 
+def run_batch(args):
+    """The batching workload: args.instances independent 3D operators, N
+    log-uniform in [2048, 65536], seeded uniform points in [0,1]^3, A_ij =
+    1/(N^(2/3) r), A_ii = 1, d' = 0, Nmax = 64, eps_ACA = 1e-6, FP32 factors
+    and vectors; 32 right-hand sides N(0,1) per instance.  Times the batched
+    build (shared ACA launches) against building the instances one by one, and
+    the batch matvec of all instances and right-hand sides (one CUDA graph)
+    against the instances' own matvecs."""
+    import torch
+
+    import hodlrnd_gb300 as h
+    from hodlrnd_gb300.batch import HODLRdD_batch
+
+    rng = np.random.default_rng(SEED + 3)
+    ns = [int(round(np.exp(rng.uniform(np.log(2048), np.log(65536))))) for _ in range(args.instances)]
+    pts = [rng.uniform(0.0, 1.0, (n, 3)) for n in ns]
+    kern = [h.Kernel("inv_r", 1.0 / n ** (2.0 / 3.0), 1.0) for n in ns]
+    box = ([0.0] * 3, [1.0] * 3)
+    params = dict(Nmax=64, eps_ACA=1e-6, tol=1e-6, precision="mixed")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    B = HODLRdD_batch(kern, pts, [box] * len(ns), **params)
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sample = list(range(0, len(ns), max(1, len(ns) // 16)))  # one-by-one builds of a sample, scaled
+    alone = []
+    for i in sample:
+        alone.append(h.HODLRdD_matrix(kern[i], pts[i], *box, **params).Assemble_matrix_operators())
+    t_alone = (time.perf_counter() - t0) * len(ns) / len(sample)
+    nrhs = 32
+    off = B.offsets
+    X = torch.randn((nrhs, int(off[-1])), dtype=torch.float32, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(SEED + 4))
+    Y = torch.empty_like(X)
+    st = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        B.matvec_device(X.data_ptr(), Y.data_ptr(), nrhs, st.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(args.steps):
+        B.matvec_device(X.data_ptr(), Y.data_ptr(), nrhs, st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # bytes of one single-RHS batch matvec: every instance's factors and near tiles (FP32) once
+    from hodlrnd_gb300 import _lib
+    import ctypes
+
+    tot_bytes = 0
+    for i in range(len(ns)):
+        sv = _lib.HodlrStats()
+        _lib.check(_lib.lib().hodlr_stats_get(B.op(i), ctypes.byref(sv)))
+        tot_bytes += sv.far_bytes + sv.near_bytes // 3  # the FP32 near copy is a third of near_bytes
+    # instances' own matvecs (FP64 vectors) of the sample, per right-hand side
+    x1 = torch.randn(int(max(ns)), dtype=torch.float64, device="cuda")
+    y1 = torch.empty_like(x1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for M in alone:
+        for _ in range(4):
+            M.matvec_device(x1.data_ptr(), y1.data_ptr(), 1, st.cuda_stream)
+    torch.cuda.synchronize()
+    t_one = (time.perf_counter() - t0) / 4 * len(ns) / len(sample)
+    for M in alone:
+        M.close()
+    out = {"metric": "batched matvecs/s (instances x right-hand sides)", "value": round(len(ns) * nrhs / (ms / 1e3), 1),
+           "unit": "instance-matvecs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(ms, 3), "higher_is_better": True, "dtype": "fp32", "data": "synthetic",
+           "config": {"workload": f"{len(ns)} 3D instances, N log-uniform 2048-65536 (total {int(off[-1])}), "
+                                  "1/(N^(2/3) r), eps_ACA 1e-6, FP32 factors and vectors, 32 RHS each",
+                      "instances": len(ns), "total_points": int(off[-1])},
+           "graph_step": "one CUDA graph: every instance and right-hand side, one launch per phase per column",
+           "hbm_GBps_per_rhs_pass": round(tot_bytes * nrhs / (ms / 1e3) / 1e9, 1),
+           "build": {"batched_s": round(t_batch, 3), "one_by_one_s_estimated": round(t_alone, 3),
+                     "one_by_one_sample": len(sample)},
+           "one_by_one_fp64_matvec_s_per_rhs_all_instances": round(t_one, 4),
+           "batched_s_per_rhs_all_instances": round(ms / 1e3 / nrhs, 5)}
+    print(json.dumps(out), flush=True)
+    B.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -521,7 +603,8 @@ def main():
     ap.add_argument("--other-steps", type=int, default=3)
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["solve", "serving"], default="solve",
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--workload", choices=["solve", "serving", "batch"], default="solve",
                     help="serving: replay the request trace through the request loop (its own JSON line)")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--pool", type=int, default=12)
@@ -531,6 +614,8 @@ def main():
         ap.error("--warmup must be at least 3")
     if args.workload == "serving":
         run_serving(args)
+    elif args.workload == "batch":
+        run_batch(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

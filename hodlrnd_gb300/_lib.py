@@ -44,7 +44,7 @@ class HodlrParams(ctypes.Structure):
                 ("max_iter", ctypes.c_int64), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("device_budget_bytes", ctypes.c_uint64), ("rank_cap", ctypes.c_int32),
                 ("max_outer", ctypes.c_int32), ("inner_tol", ctypes.c_double), ("ortho", ctypes.c_int32),
-                ("relax", ctypes.c_int32)]
+                ("relax", ctypes.c_int32), ("relax_below", ctypes.c_double)]
 
 
 class HodlrKernelDesc(ctypes.Structure):
@@ -126,9 +126,10 @@ def lib():
     L.hodlr_tree_sizes.argtypes = [P, I64]
     L.hodlr_tree_get.argtypes = [P, I64, I64, I64, I64, I64, I64, I64]
     L.hodlr_tree_destroy.argtypes = [P]
+    L.hodlr_set_relax.argtypes = [P, ctypes.c_int32, ctypes.c_double]
     L.hodlr_vec_load.argtypes = [ctypes.c_char_p, D, ctypes.c_int64, I64]
     L.hodlr_vec_save.argtypes = [ctypes.c_char_p, D, ctypes.c_int64]
-    for f in ("hodlr_vec_load", "hodlr_vec_save", "hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
+    for f in ("hodlr_set_relax", "hodlr_vec_load", "hodlr_vec_save", "hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
               "hodlr_matvec_device", "hodlr_solve", "hodlr_solve_device", "hodlr_stats_get",
               "hodlr_get_permutation", "hodlr_get_blocks", "hodlr_tree_build", "hodlr_tree_sizes",
               "hodlr_tree_get", "hodlr_tree_destroy", "hodlr_get_block", "hodlr_trace_enable", "hodlr_trace_get", "hodlr_set_solver"):

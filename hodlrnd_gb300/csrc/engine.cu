@@ -907,6 +907,9 @@ __global__ void axpy_f2d_kernel(double* x, const float* d, int64_t n) {
     x[i] = x[i] + double(d[i]);
 }
 
+// Default threshold of relaxed products: residual estimate below tol times this.
+constexpr double kRelaxFactor = 1e5;
+
 Ortho ortho_of(const hodlr_params& p) {
   if (p.ortho == HODLR_ORTHO_MGS) return Ortho::kMGS;
   if (p.ortho == HODLR_ORTHO_CGS2) return Ortho::kCGS2;
@@ -929,14 +932,14 @@ void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr
     };
     GmresResult r;
     // FP32 factors: relaxed accumulation once the residual estimate is below
-    // tol * 1e6 -- an inexact Krylov method may take products with relative
+    // relax_below (tol * 1e5) -- an inexact Krylov method may take products with relative
     // error up to about tol / |r_k| (Simoncini and Szyld, SIAM J. Sci.
     // Comput. 25 (2003); Bouras and Fraysse, SIAM J. Matrix Anal. Appl. 26
     // (2005)), and relaxed products are accurate to about 1e-6 -- then the
     // true residual with compensated products decides, and GMRES continues
     // from x with compensated products while it is above tol.
     const bool relax = p.precision == HODLR_PREC_FP32_FACTORS && p.relax != HODLR_RELAX_OFF;
-    const double relax_at = std::min(1.0, tol * 1e6);
+    const double relax_at = p.relax_below > 0 ? p.relax_below : std::min(1.0, tol * kRelaxFactor);
     std::function<void(double)> progress;
     if (relax) progress = [op, relax_at](double res) { op->relaxed = res < relax_at; };
     op->relaxed = false;
@@ -1184,6 +1187,9 @@ struct hodlr_batch {
   void* d_in = nullptr;   // [x | z] of every instance, vector type
   void* d_in2 = nullptr;  // the same as (hi, lo) FP32 pairs (df)
   void* d_y = nullptr;    // output slots of every instance
+  // several right-hand sides (FP32 vectors): nchunks_mr chunks of kMR columns
+  int nchunks_mr = 0;
+  float *d_in_mr = nullptr, *d_y_mr = nullptr, *d_zpart_mr = nullptr, *d_ypart_mr = nullptr;
   struct Graph {
     const void* x;
     void* y;
@@ -1366,6 +1372,42 @@ void batch_apply(hodlr_batch& b, const void* x, void* y, cudaStream_t st) {
   CK(launch_panels(p.a_far, b.vec, p.panels_far, p.segs_far, p.small_far, p.nsmall_far, p.big_far, p.nbig_far,
                    p.pfix_far, p.npfix_far, p.ypart, fin, b.ld_in, b.d_y, b.ycol, 1, 1, st, acc));
   CK(launch_batch_combine(b.vec, b.d_inst, int(b.ops.size()), b.max_n, b.d_y, y, st));
+}
+
+// All columns at once with FP32 vectors: chunks of kMR right-hand sides, each
+// factor byte read once per chunk (kernels of the multi-RHS family).
+// Work buffers of nch chunks (allocated outside any stream capture).
+void ensure_mr_buffers(hodlr_batch& b, int nch) {
+  const Plan& p = b.plan;
+  if (nch > b.nchunks_mr) {
+    for (void* q : {static_cast<void*>(b.d_in_mr), static_cast<void*>(b.d_y_mr), static_cast<void*>(b.d_zpart_mr),
+                    static_cast<void*>(b.d_ypart_mr)})
+      if (q) b.mem.release(q);
+    const size_t c = size_t(nch) * kMR * sizeof(float);
+    b.d_in_mr = static_cast<float*>(b.mem.alloc(size_t(b.ld_in) * c, "batch multi-RHS input"));
+    b.d_y_mr = static_cast<float*>(b.mem.alloc(size_t(b.ycol) * c, "batch multi-RHS slots"));
+    b.d_zpart_mr =
+        static_cast<float*>(b.mem.alloc(size_t(std::max<int64_t>(p.nzpart, 1)) * c, "batch multi-RHS z partial sums"));
+    b.d_ypart_mr = static_cast<float*>(
+        b.mem.alloc(size_t(std::max<int64_t>(p.nypart, 1)) * c, "batch multi-RHS row partial sums"));
+    b.nchunks_mr = nch;
+  }
+}
+
+void batch_apply_mr(hodlr_batch& b, const float* x, float* y, int64_t nrhs, cudaStream_t st) {
+  const Plan& p = b.plan;
+  const int nch = int((nrhs + kMR - 1) / kMR);
+  if (nch > b.nchunks_mr) throw Failure{HODLR_ERR_STATE, "batch multi-RHS buffers were not allocated"};
+  const int count = int(b.ops.size());
+  CK(launch_batch_gather_mr(b.d_inst, count, b.max_n, x, b.total_n, int(nrhs), b.d_in_mr, b.ld_in, nch, st));
+  CK(cudaMemsetAsync(b.d_y_mr, 0, size_t(b.ycol) * size_t(nch) * kMR * sizeof(float), st));
+  const int64_t zld = std::max<int64_t>(p.nzpart, 1), yld = std::max<int64_t>(p.nypart, 1);
+  CK(launch_zgemv_mr(p.zb, p.zitems, p.nzitems, p.zfix, p.nzfix, b.d_zpart_mr, zld, b.d_in_mr, b.ld_in, nch, st));
+  CK(launch_panels_mr(p.panels_near, p.segs_near, p.small_near, p.nsmall_near, p.big_near, p.nbig_near, p.pfix_near,
+                      p.npfix_near, b.d_ypart_mr, yld, b.d_in_mr, b.ld_in, b.d_y_mr, b.ycol, nch, st));
+  CK(launch_panels_mr(p.panels_far, p.segs_far, p.small_far, p.nsmall_far, p.big_far, p.nbig_far, p.pfix_far,
+                      p.npfix_far, b.d_ypart_mr, yld, b.d_in_mr, b.ld_in, b.d_y_mr, b.ycol, nch, st));
+  CK(launch_batch_combine_mr(b.d_inst, count, b.max_n, b.d_y_mr, b.ycol, y, b.total_n, int(nrhs), nch, st));
 }
 
 }  // namespace
@@ -1579,6 +1621,15 @@ int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_so
     }
     return rc;
   });
+}
+
+int hodlr_set_relax(hodlr_op* op, int32_t relax, double relax_below) {
+  if (!op) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_set_relax: null argument");
+  if (relax != HODLR_RELAX_AUTO && relax != HODLR_RELAX_OFF)
+    return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_set_relax: relax must be HODLR_RELAX_AUTO or HODLR_RELAX_OFF");
+  op->p.relax = relax;
+  op->p.relax_below = relax_below;
+  return HODLR_OK;
 }
 
 int hodlr_set_solver(hodlr_op* op, int32_t restart, double tol, int64_t max_iter, double inner_tol,
@@ -1845,14 +1896,19 @@ int hodlr_batch_matvec_device(hodlr_batch* b, const void* d_x, void* d_y, int64_
       // capture every column's launch sequence once on the batch's own stream
       const size_t vsz = b->vec == Prec::kF ? 4 : 8;
       cudaStream_t cs = b->ctx->stream;
+      if (b->vec == Prec::kF) ensure_mr_buffers(*b, int((nrhs + kMR - 1) / kMR));
       CK(cudaStreamSynchronize(cs));
       const uint64_t k0 = g_kernel_launches.load();
       hodlr_batch::Graph ng{d_x, d_y, nrhs, nullptr, nullptr, 0};
       CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
       try {
-        for (int64_t c = 0; c < nrhs; c++)
-          batch_apply(*b, static_cast<const char*>(d_x) + size_t(c * b->total_n) * vsz,
-                      static_cast<char*>(d_y) + size_t(c * b->total_n) * vsz, cs);
+        if (b->vec == Prec::kF) {
+          batch_apply_mr(*b, static_cast<const float*>(d_x), static_cast<float*>(d_y), nrhs, cs);
+        } else {
+          for (int64_t c = 0; c < nrhs; c++)
+            batch_apply(*b, static_cast<const char*>(d_x) + size_t(c * b->total_n) * vsz,
+                        static_cast<char*>(d_y) + size_t(c * b->total_n) * vsz, cs);
+        }
       } catch (...) {
         cudaGraph_t dead = nullptr;
         cudaStreamEndCapture(cs, &dead);

@@ -1165,4 +1165,563 @@ cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, con
   return cudaGetLastError();
 }
 
+
+// ============================================================================
+// Several right-hand sides at once: FP32 factors, FP32 vectors, FP32 sums.
+// A chunk of kMR right-hand sides is interleaved: entry e of a vector buffer
+// holds its kMR values contiguously (byte offset e * 4 kMR), so one input row
+// or z row is one 128-byte run that the bulk-copy engine stages next to the
+// factor bytes, and every factor entry read from HBM feeds kMR FMAs.  The
+// lane layouts are those of the single-vector kernels, each lane keeping kMR
+// sums per matrix row or column it owns; grid.y runs over chunks.
+// ============================================================================
+namespace {
+
+constexpr int kMWarps = 4;
+constexpr int kMStages = 3;
+constexpr int kMVBytes = 4096;                 // factor bytes per stage
+constexpr int kMXBytes = 4096;                 // input bytes per stage (32 rows of kMR floats)
+constexpr int kMRowBytes = kMR * 4;            // one interleaved entry
+constexpr int kMWarpSmem = 64 + kMStages * (kMVBytes + kMXBytes);
+static_assert(kMWarpSmem % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
+
+__device__ __forceinline__ void fma4x(float a, const float4& x, float* acc) {
+  acc[0] = __fmaf_rn(a, x.x, acc[0]);
+  acc[1] = __fmaf_rn(a, x.y, acc[1]);
+  acc[2] = __fmaf_rn(a, x.z, acc[2]);
+  acc[3] = __fmaf_rn(a, x.w, acc[3]);
+}
+
+// Lane c of a warp owns right-hand side c of the chunk (kMR = 32 = warp
+// width): it reads its input value of a row with one conflict-free shared
+// load, the row's factor values with broadcast 16-byte loads, and keeps one
+// sum per output row or column it produces -- no cross-lane reductions, and
+// every output row is one coalesced 128-byte store.
+
+// z_b = V_b^T X_s: item = rows [j0, j1) of block zb (all columns); passes of
+// kMCols columns (one pass unless r > kMCols); runs of whole V rows and their
+// input rows staged by bulk copies in a ring of kMStages.
+constexpr int kMCols = 64;
+
+// acc[c] += V[i][c] x[i] over the stage's rows, NC4 groups of 4 columns
+template <int NC4>
+__device__ __forceinline__ void mr_rows(const unsigned char* vs, int rowb, const float* xs, int nr, int lane,
+                                        float (&acc)[kMCols]) {
+  for (int i = 0; i < nr; i++) {
+    const float x = xs[i * kMR + lane];
+    const float4* v4 = reinterpret_cast<const float4*>(vs + i * rowb);
+#pragma unroll
+    for (int c = 0; c < NC4; c++) {
+      const float4 v = v4[c];
+      acc[4 * c] = __fmaf_rn(v.x, x, acc[4 * c]);
+      acc[4 * c + 1] = __fmaf_rn(v.y, x, acc[4 * c + 1]);
+      acc[4 * c + 2] = __fmaf_rn(v.z, x, acc[4 * c + 2]);
+      acc[4 * c + 3] = __fmaf_rn(v.w, x, acc[4 * c + 3]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kMWarps * 32, 3)
+    zgemv_mr_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items, int nitems,
+                    float* __restrict__ zpart, int64_t zpart_ld, float* in, int64_t ld_in) {
+  extern __shared__ __align__(16) unsigned char msm[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kMWarps + wid;
+  if (w >= nitems) return;
+  const ZItem it = items[w];
+  const ZBlock Z = zb[it.zb];
+  const int64_t rp = vpad(Z.r, 4);
+  float* inc = in + int64_t(blockIdx.y) * ld_in * kMR;
+  float* zp = zpart + int64_t(blockIdx.y) * zpart_ld * kMR;
+  unsigned char* base = msm + wid * kMWarpSmem;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  unsigned char* stage0 = base + 64;
+  const int rowb = int(rp) * 4;  // 16 .. 512 bytes, a multiple of 16
+  const int R = min(kMVBytes / rowb, kMXBytes / kMRowBytes);  // 0 only for rows above 4096 bytes
+  const int nrows = it.j1 - it.j0;
+  const int nst = (nrows + R - 1) / R;
+  const float* V = static_cast<const float*>(Z.V) + int64_t(it.j0) * rp;
+  const float* xr = inc + (Z.x_off + it.j0) * kMR;
+  const int npass = (it.nk + kMCols - 1) / kMCols;
+  float acc[kMCols];
+  if (R == 0) {
+    // rows wider than a stage (rank above 1024): direct loads
+    for (int pass = 0; pass < npass; pass++) {
+      const int c0 = it.k0 + pass * kMCols, ncol = min(kMCols, it.k0 + it.nk - c0);
+#pragma unroll
+      for (int c = 0; c < kMCols; c++) acc[c] = 0.f;
+      for (int j = 0; j < nrows; j++) {
+        const float x = xr[int64_t(j) * kMR + lane];
+        const float* vj = V + int64_t(j) * rp + c0;
+#pragma unroll
+        for (int c = 0; c < kMCols; c++)
+          if (c < ncol) acc[c] = __fmaf_rn(__ldg(vj + c), x, acc[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < kMCols; c++)
+        if (c < ncol) {
+          const int col = c0 + c;
+          if (it.part < 0) {
+            if (col < Z.r) inc[(Z.z_off + col) * kMR + lane] = acc[c];
+          } else {
+            zp[(int64_t(it.part) + col - it.k0) * kMR + lane] = acc[c];
+          }
+        }
+    }
+    return;
+  }
+  const int total = nst * npass;  // stages over all passes
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < kMStages; s++) mbar_init(bar + s, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  // stage q: pass q / nst, rows (q % nst) * R ..
+#define HODLR_MR_ISSUE(q_)                                                                     \
+  do {                                                                                         \
+    const int s_ = (q_) % kMStages;                                                            \
+    const int r0_ = ((q_) % nst) * R, nr_ = min(R, nrows - r0_);                               \
+    unsigned char* st_ = stage0 + s_ * (kMVBytes + kMXBytes);                                  \
+    fence_proxy_async();                                                                       \
+    mbar_expect_tx(bar + s_, uint32_t(nr_) * uint32_t(rowb + kMRowBytes));                     \
+    bulk_g2s(st_, V + int64_t(r0_) * rp, uint32_t(nr_ * rowb), bar + s_);                      \
+    bulk_g2s(st_ + kMVBytes, xr + int64_t(r0_) * kMR, uint32_t(nr_ * kMRowBytes), bar + s_);    \
+  } while (0)
+  if (lane == 0)
+    for (int q = 0; q < min(kMStages, total); q++) HODLR_MR_ISSUE(q);
+  for (int q = 0; q < total; q++) {
+    const int pass = q / nst, c0 = it.k0 + pass * kMCols;
+    const int ncol4 = min(kMCols, it.k0 + it.nk - c0) / 4;
+    if (q % nst == 0) {
+#pragma unroll
+      for (int c = 0; c < kMCols; c++) acc[c] = 0.f;
+    }
+    const int s = q % kMStages;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(bar + s, uint32_t(q / kMStages) & 1u));
+    if (!ok) {
+      if (lane == 0) atomicAdd(&g_stream_timeouts, 1u);
+      for (int t = q; t < min(q + kMStages, total); t++) mbar_wait(bar + t % kMStages, uint32_t(t / kMStages) & 1u);
+      return;
+    }
+    const int nr = min(R, nrows - (q % nst) * R);
+    const unsigned char* vs = stage0 + s * (kMVBytes + kMXBytes) + c0 * 4;
+    const float* xs = reinterpret_cast<const float*>(stage0 + s * (kMVBytes + kMXBytes) + kMVBytes);
+    switch (ncol4) {  // column count known at compile time: no per-row guards
+#define HODLR_MR_CASE(k_) \
+  case k_:                \
+    mr_rows<k_>(vs, rowb, xs, nr, lane, acc); \
+    break;
+      HODLR_MR_CASE(1) HODLR_MR_CASE(2) HODLR_MR_CASE(3) HODLR_MR_CASE(4) HODLR_MR_CASE(5) HODLR_MR_CASE(6)
+      HODLR_MR_CASE(7) HODLR_MR_CASE(8) HODLR_MR_CASE(9) HODLR_MR_CASE(10) HODLR_MR_CASE(11) HODLR_MR_CASE(12)
+      HODLR_MR_CASE(13) HODLR_MR_CASE(14) HODLR_MR_CASE(15) HODLR_MR_CASE(16)
+#undef HODLR_MR_CASE
+      default:
+        break;
+    }
+    __syncwarp();
+    if (lane == 0 && q + kMStages < total) HODLR_MR_ISSUE(q + kMStages);
+    if (q % nst == nst - 1) {  // end of a pass: columns c0 .. c0 + 4 ncol4
+#pragma unroll
+      for (int c = 0; c < kMCols; c++)
+        if (c < 4 * ncol4) {
+          const int col = c0 + c;
+          if (it.part < 0) {
+            if (col < Z.r) inc[(Z.z_off + col) * kMR + lane] = acc[c];
+          } else {
+            zp[(int64_t(it.part) + col - it.k0) * kMR + lane] = acc[c];
+          }
+        }
+    }
+  }
+#undef HODLR_MR_ISSUE
+}
+
+// z row zpos (all kMR values) = sum of the item partials, in order.
+__global__ void __launch_bounds__(256) zfix_mr_kernel(const ZFix* __restrict__ fix, int nfix,
+                                                     const float* __restrict__ zpart, int64_t zpart_ld,
+                                                     float* __restrict__ in, int64_t ld_in) {
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const int f = int(t / kMR), c = int(t % kMR);
+  if (f >= nfix) return;
+  const ZFix F = fix[f];
+  const float* zp = zpart + int64_t(blockIdx.y) * zpart_ld * kMR;
+  float acc = 0.f;
+  for (int q = 0; q < F.count; q++) acc += zp[(int64_t(F.part) + int64_t(q) * kZPart) * kMR + c];
+  in[int64_t(blockIdx.y) * ld_in * kMR + F.zpos * kMR + c] = acc;
+}
+
+// Leaf panels (m <= 32): one warp per item; lane c keeps m sums.  The item's
+// segments are cut into pieces that are packed, in order, into stages of at
+// most kMSUBytes of factor bytes (each piece 16-byte aligned, a multiple of 4
+// columns unless it ends its segment) and kMSRows input rows; one lane issues
+// the bulk copies of a stage, every lane replays the same packing to find the
+// pieces.
+constexpr int kMSUBytes = 4096;
+constexpr int kMSRows = 32;
+constexpr int kMSXBytes = kMSRows * kMRowBytes;
+constexpr int kMSWarpSmem = 64 + kMStages * (kMSUBytes + kMSXBytes);
+static_assert(kMSWarpSmem % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
+
+// acc[i] += U[i][j] x[j] over a piece's columns, rows 0 .. MP-1
+template <int MP>
+__device__ __forceinline__ void mr_cols(const float* ua, int m, const float* xr, int nc, float (&acc)[32]) {
+  for (int j = 0; j < nc; j++) {
+    const float x = xr[j * kMR];
+#pragma unroll
+    for (int i = 0; i < MP; i++) acc[i] = __fmaf_rn(ua[j * m + i], x, acc[i]);
+  }
+}
+
+struct MrCursor {
+  int64_t s;  // segment
+  int c;      // first column of the next piece
+};
+
+// Next piece of a stage holding `used` factor bytes and `rows` input rows;
+// false when the stage is full or the segments are done.
+__device__ __forceinline__ bool mr_next_piece(const Seg* segs, int64_t seg_e, int m, MrCursor& cur, int used, int rows,
+                                              int64_t& s, int& c0, int& nc, int& bytes) {
+  if (cur.s >= seg_e) return false;
+  const int K = segs[cur.s].K;
+  int room_c = min((kMSUBytes - used) / (m * 4), kMSRows - rows);
+  int c = min(K - cur.c, room_c);
+  if (c < K - cur.c) c = c / 4 * 4;  // a piece that does not end its segment keeps 16-byte alignment
+  if (c <= 0) return false;
+  nc = c;
+  bytes = (c * m * 4 + 15) & ~15;
+  if (used + bytes > kMSUBytes) return false;
+  s = cur.s;
+  c0 = cur.c;
+  cur.c += c;
+  if (cur.c >= K) {
+    cur.s++;
+    cur.c = 0;
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(kMWarps * 32, 3)
+    panel_small_mr_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs,
+                          const Item* __restrict__ items, int nitems, const float* __restrict__ in, int64_t ld_in,
+                          float* __restrict__ y, int64_t ld_y) {
+  extern __shared__ __align__(16) unsigned char msm[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kMWarps + wid;
+  if (w >= nitems) return;
+  const Item it = items[w];
+  const Panel P = panels[it.panel];
+  const int m = P.m;
+  int mp = 4;
+  while (mp < m) mp <<= 1;
+  const float* inc = in + int64_t(blockIdx.y) * ld_in * kMR;
+  unsigned char* base = msm + wid * kMSWarpSmem;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  unsigned char* stage0 = base + 64;
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < kMStages; s++) mbar_init(bar + s, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  MrCursor pc{it.seg_b, 0}, cc{it.seg_b, 0};
+  int issued = 0;
+  // packs and issues the next stage; false when nothing is left
+  // Packs and issues the next stage: per piece, lane 0 raises the stage's
+  // transaction count (no arrival) and starts its two copies; the stage's one
+  // arrival comes after the last piece, so the phase cannot complete before
+  // every copy is accounted for.  ok_ is false when nothing is left.
+#define HODLR_MRS_ISSUE(ok_)                                                                      \
+  do {                                                                                            \
+    const int st_ = issued % kMStages;                                                            \
+    unsigned char* su_ = stage0 + st_ * (kMSUBytes + kMSXBytes);                                  \
+    int used_ = 0, rows_ = 0, nc_, by_, c0_;                                                      \
+    int64_t s_;                                                                                   \
+    if (lane == 0) fence_proxy_async();                                                           \
+    while (mr_next_piece(segs, it.seg_e, m, pc, used_, rows_, s_, c0_, nc_, by_)) {               \
+      if (lane == 0) {                                                                            \
+        const Seg S_ = segs[s_];                                                                  \
+        mbar_expect_tx_only(bar + st_, uint32_t(by_ + nc_ * kMRowBytes));                         \
+        bulk_g2s(su_ + used_, static_cast<const float*>(S_.A) + int64_t(c0_) * m, uint32_t(by_), bar + st_); \
+        bulk_g2s(su_ + kMSUBytes + rows_ * kMRowBytes, inc + (S_.in_off + c0_) * kMR,            \
+                 uint32_t(nc_ * kMRowBytes), bar + st_);                                          \
+      }                                                                                           \
+      used_ += by_;                                                                               \
+      rows_ += nc_;                                                                               \
+    }                                                                                             \
+    ok_ = rows_ > 0;                                                                              \
+    if (ok_) {                                                                                    \
+      if (lane == 0) mbar_arrive(bar + st_);                                                      \
+      issued++;                                                                                   \
+    }                                                                                             \
+  } while (0)
+  bool more = true;
+  for (int q = 0; q < kMStages && more; q++) HODLR_MRS_ISSUE(more);
+  float acc[32];
+#pragma unroll
+  for (int i = 0; i < 32; i++) acc[i] = 0.f;
+  for (int q = 0; q < issued; q++) {
+    const int st = q % kMStages;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(bar + st, uint32_t(q / kMStages) & 1u));
+    if (!ok) {
+      if (lane == 0) atomicAdd(&g_stream_timeouts, 1u);
+      for (int t = q; t < issued; t++) mbar_wait(bar + t % kMStages, uint32_t(t / kMStages) & 1u);
+      return;
+    }
+    const unsigned char* su = stage0 + st * (kMSUBytes + kMSXBytes);
+    const float* xs = reinterpret_cast<const float*>(su + kMSUBytes);
+    int used = 0, rows = 0, nc, by, c0;
+    int64_t sg;
+    while (mr_next_piece(segs, it.seg_e, m, cc, used, rows, sg, c0, nc, by)) {
+      const float* ua = reinterpret_cast<const float*>(su + used);
+      const float* xr = xs + rows * kMR + lane;
+      // rows 0 .. mp-1 (mp = next power of two >= m, at least 4): sums of rows
+      // m .. mp-1 read neighbouring bytes of the warp's stage and are never stored
+      if (mp <= 4)
+        mr_cols<4>(ua, m, xr, nc, acc);
+      else if (mp <= 8)
+        mr_cols<8>(ua, m, xr, nc, acc);
+      else if (mp <= 16)
+        mr_cols<16>(ua, m, xr, nc, acc);
+      else
+        mr_cols<32>(ua, m, xr, nc, acc);
+      used += by;
+      rows += nc;
+    }
+    __syncwarp();
+    if (more) HODLR_MRS_ISSUE(more);  // into the stage just consumed (the ring is full while more)
+  }
+#undef HODLR_MRS_ISSUE
+  float* yo = y + int64_t(blockIdx.y) * ld_y * kMR + P.yoff * kMR;
+#pragma unroll
+  for (int i = 0; i < 32; i++)
+    if (i < m) yo[int64_t(i) * kMR + lane] = acc[i];
+}
+
+// acc[i] += U[i][j] x[j] over a stage's columns: H4 groups of 4 rows (a full
+// tile), or h4 of them checked per group (H4 == 0, the last tile)
+template <int H4>
+__device__ __forceinline__ void mr_tile(const unsigned char* us, int colb, const float* xs, int nc, int lane, int h4,
+                                        float (&acc)[128]) {
+  for (int j = 0; j < nc; j++) {
+    const float x = xs[j * kMR + lane];
+    const float4* u4 = reinterpret_cast<const float4*>(us + j * colb);
+#pragma unroll
+    for (int r = 0; r < 32; r++)
+      if (H4 ? r < H4 : r < h4) {
+        const float4 u = u4[r];
+        acc[4 * r] = __fmaf_rn(u.x, x, acc[4 * r]);
+        acc[4 * r + 1] = __fmaf_rn(u.y, x, acc[4 * r + 1]);
+        acc[4 * r + 2] = __fmaf_rn(u.z, x, acc[4 * r + 2]);
+        acc[4 * r + 3] = __fmaf_rn(u.w, x, acc[4 * r + 3]);
+      }
+  }
+}
+
+// Panels of more than 32 rows: item = row tile t (up to 128 rows) times a
+// run of segments; lane c keeps the tile's row sums; runs of tile columns and
+// their input rows are staged.
+constexpr int kMTUBytes = 4096;
+constexpr int kMTXBytes = 4096;  // 32 input rows
+constexpr int kMTWarpSmem = 64 + kMStages * (kMTUBytes + kMTXBytes);
+static_assert(kMTWarpSmem % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
+
+__global__ void __launch_bounds__(kMWarps * 32, 2)
+    panel_tile_mr_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs,
+                         const Item* __restrict__ items, int nitems, float* __restrict__ ypart, int64_t ypart_ld,
+                         const float* __restrict__ in, int64_t ld_in, float* __restrict__ y, int64_t ld_y) {
+  constexpr int T = 128;
+  extern __shared__ __align__(16) unsigned char msm[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kMWarps + wid;
+  if (w >= nitems) return;
+  const Item it = items[w];
+  const Panel P = panels[it.panel];
+  const int m = P.m;
+  const float* inc = in + int64_t(blockIdx.y) * ld_in * kMR;
+  const int t = it.chunk;
+  const int rows = min(T, m - t * T);
+  const int64_t h = tile_height(m, t, 4);
+  const int colb = int(h) * 4;
+  const int h4 = int(h) / 4;
+  const int cps = min(kMTUBytes / colb, kMTXBytes / kMRowBytes);
+  float acc[T];
+#pragma unroll
+  for (int i = 0; i < T; i++) acc[i] = 0.f;
+  unsigned char* base = msm + wid * kMTWarpSmem;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  unsigned char* stage0 = base + 64;
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < kMStages; s++) mbar_init(bar + s, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  int64_t ps = it.seg_b;
+  int pc = 0, issued = 0;
+#define HODLR_MRT_ISSUE()                                                                          \
+  do {                                                                                             \
+    while (ps < it.seg_e && pc >= segs[ps].K) {                                                    \
+      ps++;                                                                                        \
+      pc = 0;                                                                                      \
+    }                                                                                              \
+    if (ps >= it.seg_e) break;                                                                     \
+    const Seg S_ = segs[ps];                                                                       \
+    const int nc_ = min(cps, S_.K - pc);                                                           \
+    if (lane == 0) {                                                                               \
+      const int st_ = issued % kMStages;                                                           \
+      unsigned char* dst_ = stage0 + st_ * (kMTUBytes + kMTXBytes);                                \
+      const float* src_ = static_cast<const float*>(S_.A) + int64_t(t) * T * S_.K + int64_t(pc) * h; \
+      fence_proxy_async();                                                                         \
+      mbar_expect_tx(bar + st_, uint32_t(nc_) * uint32_t(colb + kMRowBytes));                      \
+      bulk_g2s(dst_, src_, uint32_t(nc_ * colb), bar + st_);                                       \
+      bulk_g2s(dst_ + kMTUBytes, inc + (S_.in_off + pc) * kMR, uint32_t(nc_ * kMRowBytes), bar + st_); \
+    }                                                                                              \
+    pc += nc_;                                                                                     \
+    issued++;                                                                                      \
+  } while (0)
+  for (int q = 0; q < kMStages; q++) HODLR_MRT_ISSUE();
+  int64_t cs = it.seg_b;
+  int cc = 0;
+  for (int q = 0; q < issued; q++) {
+    while (cc >= segs[cs].K) {
+      cs++;
+      cc = 0;
+    }
+    const int nc = min(cps, segs[cs].K - cc);
+    const int st = q % kMStages;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(bar + st, uint32_t(q / kMStages) & 1u));
+    if (!ok) {
+      if (lane == 0) atomicAdd(&g_stream_timeouts, 1u);
+      for (int u = q; u < issued; u++) mbar_wait(bar + u % kMStages, uint32_t(u / kMStages) & 1u);
+      return;
+    }
+    const unsigned char* us = stage0 + st * (kMTUBytes + kMTXBytes);
+    const float* xs = reinterpret_cast<const float*>(us + kMTUBytes);
+    if (h4 == T / 4)
+      mr_tile<T / 4>(us, colb, xs, nc, lane, h4, acc);
+    else
+      mr_tile<0>(us, colb, xs, nc, lane, h4, acc);
+    cc += nc;
+    __syncwarp();
+    HODLR_MRT_ISSUE();
+  }
+#undef HODLR_MRT_ISSUE
+  float* dst = it.part < 0 ? y + int64_t(blockIdx.y) * ld_y * kMR + (P.yoff + int64_t(t) * T) * kMR
+                           : ypart + int64_t(blockIdx.y) * ypart_ld * kMR + int64_t(it.part) * T * kMR;
+#pragma unroll
+  for (int i = 0; i < T; i++)
+    if (i < rows) dst[int64_t(i) * kMR + lane] = acc[i];
+}
+
+__global__ void __launch_bounds__(256) panel_fix_mr_kernel(const Panel* __restrict__ panels,
+                                                           const PanelFix* __restrict__ fix, int nfix,
+                                                           const float* __restrict__ ypart, int64_t ypart_ld,
+                                                           float* __restrict__ y, int64_t ld_y) {
+  constexpr int rows = 128;
+  const int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const int64_t fq = t / kMR;
+  const int c = int(t % kMR);
+  const int f = int(fq / rows), q = int(fq % rows);
+  if (f >= nfix) return;
+  const PanelFix F = fix[f];
+  const Panel P = panels[F.panel];
+  const int i = F.chunk * rows + q;
+  if (i >= P.m) return;
+  const float* yp = ypart + int64_t(blockIdx.y) * ypart_ld * kMR;
+  float acc = 0.f;
+  for (int g = 0; g < F.count; g++) acc += yp[((int64_t(F.part) + g) * rows + q) * kMR + c];
+  y[int64_t(blockIdx.y) * ld_y * kMR + (P.yoff + i) * kMR + c] = acc;
+}
+
+// in (chunk ch, interleaved) <- x (caller order, column major total_n x k)
+__global__ void __launch_bounds__(256) batch_gather_mr_kernel(const BatchInst* __restrict__ inst,
+                                                              const float* __restrict__ x, int64_t total_n, int k,
+                                                              float* __restrict__ in, int64_t ld_in, int ch) {
+  const BatchInst I = inst[blockIdx.y];
+  float* inc = in + int64_t(ch) * ld_in * kMR;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < I.n * kMR;
+       e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = e / kMR;
+    const int c = int(e % kMR), col = ch * kMR + c;
+    inc[(I.in_base + r) * kMR + c] = col < k ? x[int64_t(col) * total_n + I.x_base + I.perm[r]] : 0.f;
+  }
+}
+
+__global__ void __launch_bounds__(256) batch_combine_mr_kernel(const BatchInst* __restrict__ inst,
+                                                               const float* __restrict__ y, int64_t ld_y,
+                                                               float* __restrict__ out, int64_t total_n, int k, int ch) {
+  const BatchInst I = inst[blockIdx.y];
+  const float* yc = y + int64_t(ch) * ld_y * kMR;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < I.n * kMR;
+       e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t r = e / kMR;
+    const int c = int(e % kMR), col = ch * kMR + c;
+    if (col >= k) continue;
+    double acc = double(yc[(I.y_base + r) * kMR + c]);
+    for (int s = 1; s < I.nslots; s++) acc += double(yc[(I.y_base + int64_t(s) * I.n + r) * kMR + c]);
+    out[int64_t(col) * total_n + I.x_base + I.perm[r]] = float(acc);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_zgemv_mr(const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix, float* zpart,
+                            int64_t zpart_ld, float* in, int64_t ld_in, int nchunks, cudaStream_t st) {
+  if (nitems <= 0) return cudaSuccess;
+  count_launches(nfix > 0 ? 2 : 1);
+  cudaFuncSetAttribute(zgemv_mr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMWarps * kMWarpSmem);
+  dim3 g(unsigned((nitems + kMWarps - 1) / kMWarps), unsigned(nchunks));
+  zgemv_mr_kernel<<<g, kMWarps * 32, kMWarps * kMWarpSmem, st>>>(zb, items, nitems, zpart, zpart_ld, in, ld_in);
+  if (nfix > 0) {
+    dim3 gf(unsigned((int64_t(nfix) * kMR + 255) / 256), unsigned(nchunks));
+    zfix_mr_kernel<<<gf, 256, 0, st>>>(fix, nfix, zpart, zpart_ld, in, ld_in);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_panels_mr(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big,
+                             int nbig, const PanelFix* fix, int nfix, float* ypart, int64_t ypart_ld, const float* in,
+                             int64_t ld_in, float* y, int64_t ld_y, int nchunks, cudaStream_t st) {
+  if (nsmall + nbig <= 0) return cudaSuccess;
+  count_launches(uint64_t(nbig > 0) + uint64_t(nsmall > 0) + uint64_t(nfix > 0));
+  if (nbig > 0) {
+    cudaFuncSetAttribute(panel_tile_mr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMWarps * kMTWarpSmem);
+    dim3 g(unsigned((nbig + kMWarps - 1) / kMWarps), unsigned(nchunks));
+    panel_tile_mr_kernel<<<g, kMWarps * 32, kMWarps * kMTWarpSmem, st>>>(panels, segs, big, nbig, ypart, ypart_ld, in,
+                                                                          ld_in, y, ld_y);
+  }
+  if (nsmall > 0) {
+    cudaFuncSetAttribute(panel_small_mr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMWarps * kMSWarpSmem);
+    dim3 g(unsigned((nsmall + kMWarps - 1) / kMWarps), unsigned(nchunks));
+    panel_small_mr_kernel<<<g, kMWarps * 32, kMWarps * kMSWarpSmem, st>>>(panels, segs, small, nsmall, in, ld_in, y,
+                                                                           ld_y);
+  }
+  if (nfix > 0) {
+    dim3 gf(unsigned((int64_t(nfix) * 128 * kMR + 255) / 256), unsigned(nchunks));
+    panel_fix_mr_kernel<<<gf, 256, 0, st>>>(panels, fix, nfix, ypart, ypart_ld, y, ld_y);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_gather_mr(const BatchInst* inst, int count, int64_t max_n, const float* x, int64_t total_n,
+                                   int k, float* in, int64_t ld_in, int nchunks, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  for (int ch = 0; ch < nchunks; ch++) {
+    count_launches(1);
+    batch_gather_mr_kernel<<<batch_grid(count, max_n * kMR), 256, 0, st>>>(inst, x, total_n, k, in, ld_in, ch);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_combine_mr(const BatchInst* inst, int count, int64_t max_n, const float* y, int64_t ld_y,
+                                    float* out, int64_t total_n, int k, int nchunks, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  for (int ch = 0; ch < nchunks; ch++) {
+    count_launches(1);
+    batch_combine_mr_kernel<<<batch_grid(count, max_n * kMR), 256, 0, st>>>(inst, y, ld_y, out, total_n, k, ch);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace hodlr

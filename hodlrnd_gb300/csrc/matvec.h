@@ -151,6 +151,24 @@ cudaError_t launch_batch_gather(Prec x, const BatchInst* inst, int count, int64_
 cudaError_t launch_batch_combine(Prec x, const BatchInst* inst, int count, int64_t max_n, const void* y, void* out,
                                  cudaStream_t st);
 
+// ---- several right-hand sides: FP32 factors and vectors ---------------------
+// A chunk of kMR right-hand sides is stored interleaved: entry e of a vector
+// buffer holds the chunk's kMR values at e * kMR .. e * kMR + kMR - 1.
+// Buffers hold nchunks chunks of ld entries each (grid.y runs over chunks);
+// zpart / ypart hold zpart_ld / ypart_ld entries per chunk.
+constexpr int kMR = 32;
+cudaError_t launch_zgemv_mr(const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix, float* zpart,
+                            int64_t zpart_ld, float* in, int64_t ld_in, int nchunks, cudaStream_t st);
+// output slots: ld_y entries per chunk, panel rows at P.yoff
+cudaError_t launch_panels_mr(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big,
+                             int nbig, const PanelFix* fix, int nfix, float* ypart, int64_t ypart_ld, const float* in,
+                             int64_t ld_in, float* y, int64_t ld_y, int nchunks, cudaStream_t st);
+// x, out: caller order, column major total_n x k (FP32); chunk ch holds columns ch*kMR ..
+cudaError_t launch_batch_gather_mr(const BatchInst* inst, int count, int64_t max_n, const float* x, int64_t total_n,
+                                   int k, float* in, int64_t ld_in, int nchunks, cudaStream_t st);
+cudaError_t launch_batch_combine_mr(const BatchInst* inst, int count, int64_t max_n, const float* y, int64_t ld_y,
+                                    float* out, int64_t total_n, int k, int nchunks, cudaStream_t st);
+
 // out[i] = (hi, lo) FP32 pair of x[i] (hi = x rounded to FP32, lo = the rest)
 cudaError_t launch_split(const double* x, void* out, int64_t n, cudaStream_t st);
 

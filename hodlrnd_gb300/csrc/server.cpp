@@ -355,6 +355,10 @@ void execute(hodlr_server* s, Admitted& a, Done& d, std::unique_ptr<Geometry>& b
   r.t_total_s = seconds_since(j.t_submit);
 }
 
+// The operator of a request is kept resident when its build succeeded,
+// whatever the solve's outcome (non-convergence included).
+bool g_built_ok(const hodlr_result& r) { return r.built == 1 && r.actual_bytes > 0; }
+
 void worker(hodlr_server* s) {
   std::unique_lock<std::mutex> lock(s->mu);
   for (;;) {
@@ -400,7 +404,7 @@ void worker(hodlr_server* s) {
           else f = 0.5 * f + 0.5 * ratio;
         }
         s->st.builds++;
-        if (j.key && d.res.status == HODLR_OK) {
+        if (j.key && g_built_ok(d.res)) {
           built->busy = 0;
           built->last_use = ++s->tick;
           s->used += built->bytes;

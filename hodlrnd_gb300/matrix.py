@@ -27,7 +27,7 @@ def _dp(a):
 class HODLRdD_matrix:
     def __init__(self, userkernel, gridPoints, x1, x2, *, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0,
                  precision="fp64", restart=100, tol=None, max_iter=0, device=0, device_budget_bytes=0, rank_cap=0,
-                 inner_tol=0.0, max_outer=0, ortho="auto", relax=True):
+                 inner_tol=0.0, max_outer=0, ortho="auto", relax=True, relax_below=0.0):
         self.kernel = userkernel
         self.points = np.ascontiguousarray(gridPoints, dtype=np.float64)
         if self.points.ndim != 2:
@@ -56,6 +56,7 @@ class HODLRdD_matrix:
         p.max_outer = int(max_outer)
         p.ortho = {"auto": _lib.HODLR_ORTHO_AUTO, "mgs": _lib.HODLR_ORTHO_MGS, "cgs2": _lib.HODLR_ORTHO_CGS2}[ortho]
         p.relax = _lib.HODLR_RELAX_AUTO if relax else _lib.HODLR_RELAX_OFF
+        p.relax_below = float(relax_below)
         self.params = p
         self._ctx = None
         self._op = None
@@ -165,6 +166,12 @@ class HODLRdD_matrix:
         self._need_op()
         _lib.check(_lib.lib().hodlr_set_solver(self._op, int(restart), float(tol) if tol else 0.0, int(max_iter),
                                                float(inner_tol), int(max_outer)), self._ctx)
+
+    def set_relax(self, relax=True, relax_below=0.0):
+        """FP32-factor solves: relaxed products on/off and their threshold (0: tol * 1e5)."""
+        self._need_op()
+        _lib.check(_lib.lib().hodlr_set_relax(self._op, _lib.HODLR_RELAX_AUTO if relax else _lib.HODLR_RELAX_OFF,
+                                              float(relax_below)), self._ctx)
 
     # ------------------------------------------------------------ introspection
     def statistics(self):

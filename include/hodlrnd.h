@@ -84,9 +84,11 @@ typedef struct hodlr_params {
   double inner_tol;  /* MIXED: relative-residual target of each FP32 inner GMRES (<= 0: default 1e-4) */
   int32_t ortho;     /* GMRES orthogonalisation, HODLR_ORTHO_* */
   int32_t relax;     /* FP32_FACTORS: HODLR_RELAX_AUTO (relaxed products once the residual allows) or _OFF */
+  double relax_below; /* FP32_FACTORS: relative residual estimate below which products are relaxed
+                         (<= 0: the default, tol * 1e5) */
 } hodlr_params;
 
-/* FP32_FACTORS solves: once GMRES's residual estimate is below tol * 1e6, the
+/* FP32_FACTORS solves: once GMRES's residual estimate is below relax_below, the
  * matvecs sum the FP32 products in plain FP32 (about 1e-6 relative, which an
  * inexact Krylov method tolerates at that residual) instead of compensated
  * FP32; the solve ends only when the true residual, with compensated
@@ -162,6 +164,9 @@ int hodlr_solve_device(hodlr_op* op, const double* d_b, double* d_x, int64_t nrh
  * <= 0 select 100 / eps_aca / N, inner_tol and max_outer <= 0 the defaults. */
 int hodlr_set_solver(hodlr_op* op, int32_t restart, double tol, int64_t max_iter, double inner_tol,
                      int32_t max_outer);
+/* Relaxed-product settings (relax, relax_below of hodlr_params) for later
+ * solves of an FP32_FACTORS operator.  No counterpart in the reference. */
+int hodlr_set_relax(hodlr_op* op, int32_t relax, double relax_below);
 
 typedef struct hodlr_stats {
   int64_t n, depth, n_leaves, n_far_blocks, n_dense_far_blocks, n_near_blocks, max_rank;

@@ -77,13 +77,16 @@ def test_mixed_batch_fp32_vectors_and_solves():
     B = HODLRdD_batch([k for _, k in inst], [p for p, _ in inst], [box] * len(inst), **params)
     off = B.offsets
     rng = np.random.default_rng(2)
-    X = torch.tensor(rng.standard_normal((2, off[-1])), dtype=torch.float32, device="cuda")
+    # 40 right-hand sides: two chunks of 32 (the second padded) of the
+    # multi-RHS kernels, each factor byte read once per chunk
+    nrhs = 40
+    X = torch.tensor(rng.standard_normal((nrhs, off[-1])), dtype=torch.float32, device="cuda")
     Y = torch.empty_like(X)
-    B.matvec_device(X.data_ptr(), Y.data_ptr(), 2, torch.cuda.current_stream().cuda_stream)
+    B.matvec_device(X.data_ptr(), Y.data_ptr(), nrhs, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     for i, (p, k) in enumerate(inst):
         M = HODLRdD_matrix(k, p, *box, Nmax=64, eps_ACA=1e-6).Assemble_matrix_operators()
-        for c in range(2):
+        for c in (0, 1, 31, 32, 39):
             x = X[c, off[i]:off[i + 1]].double().cpu().numpy()
             y = M * x
             assert np.linalg.norm(Y[c, off[i]:off[i + 1]].double().cpu().numpy() - y) / np.linalg.norm(y) < 1e-5
