@@ -7,7 +7,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libhodlrnd_gb300.so")
+# HODLRND_LIBRARY selects another build of the library (for example one
+# compiled with different HODLR_TUNE_* ring shapes)
+LIB_PATH = os.environ.get("HODLRND_LIBRARY") or os.path.join(HERE, "libhodlrnd_gb300.so")
 
 HODLR_OK = 0
 HODLR_ERR_INVALID = 1

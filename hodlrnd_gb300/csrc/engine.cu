@@ -200,6 +200,7 @@ struct hodlr_ctx {
 struct hodlr_op {
   hodlr_ctx* ctx = nullptr;
   bool keep_host_plans = false;  // set for the operators of a batch
+  std::vector<void*> far_chunks; // factor chunks written by the ACA batches (freed by relayout_far)
   bool batch_owned = false;      // freed by hodlr_batch_destroy only
   bool relaxed = false;  // FP32 factors: matvecs use relaxed accumulation (set by the solver)
   unsigned int* h_waits = nullptr;  // pinned: streaming-kernel wait give-ups (read_stream_timeouts)
@@ -743,6 +744,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     for (size_t j = 0; j < nops; j++)
       if (bytes[j] > 0) {
         chunk[j] = static_cast<char*>(ops[j]->mem.alloc(bytes[j], "far-field factors"));
+        ops[j]->far_chunks.push_back(chunk[j]);
         CK(cudaMemsetAsync(chunk[j], 0, bytes[j], st));  // tile padding rows must read as zero
       }
     for (size_t q = 0; q < batch.size(); q++) {
@@ -1097,9 +1099,70 @@ void build_prepare(hodlr_op* op, const double* points, const double* box_lo, con
   op->st.t_near_s = t2 - t1;
 }
 
+// FP32 far field: moves every block's U (or dense tile) into one buffer in
+// the far plan's panel order -- the segments of a panel then sit back to
+// back, each padded to 16 bytes, so the leaf-panel kernel streams a panel
+// with one bulk copy per stage -- and every V into a second buffer; the ACA
+// batches' chunks are freed.
+void relayout_far(hodlr_op* op, cudaStream_t st) {
+  const size_t nb = op->far.size();
+  if (nb == 0 || op->p.precision == HODLR_PREC_FP64) return;
+  const int esz = 4;
+  std::vector<uint64_t> uoff(nb, 0), voff(nb, 0);
+  uint64_t ubytes = 0, vbytes = 0;
+  const Tree& t = op->tree;
+  // op->far is grouped by (level, target): the plan's panel order
+  for (size_t q = 0; q < nb; q++) {
+    const int l = op->far[q].level;
+    const int64_t m = t.count[size_t(t.gid(l, op->far[q].t))], n = t.count[size_t(t.gid(l, op->far[q].s))];
+    if (op->dense[q]) {
+      uoff[q] = ubytes;
+      ubytes += (uint64_t(stored_elems(m, n, esz)) * esz + 15) / 16 * 16;
+    } else if (op->rank[q] > 0) {
+      uoff[q] = ubytes;
+      ubytes += (uint64_t(stored_elems(m, op->rank[q], esz)) * esz + 15) / 16 * 16;
+      voff[q] = vbytes;
+      vbytes += (uint64_t(n) * uint64_t(vpad(op->rank[q], esz)) * esz + 15) / 16 * 16;
+    }
+  }
+  char* fu = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(ubytes, 16), "far-field factors (panel order)"));
+  char* fv = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(vbytes, 16), "far-field V factors"));
+  std::vector<CopyDesc> cd;
+  cd.reserve(nb * 2);
+  for (size_t q = 0; q < nb; q++) {
+    const int l = op->far[q].level;
+    const int64_t m = t.count[size_t(t.gid(l, op->far[q].t))], n = t.count[size_t(t.gid(l, op->far[q].s))];
+    if (op->dense[q]) {
+      const uint64_t b = (uint64_t(stored_elems(m, n, esz)) * esz + 15) / 16 * 16;
+      cd.push_back({op->uptr[q], fu + uoff[q], b});
+      op->uptr[q] = fu + uoff[q];
+    } else if (op->rank[q] > 0) {
+      const uint64_t bu = (uint64_t(stored_elems(m, op->rank[q], esz)) * esz + 15) / 16 * 16;
+      const uint64_t bv = (uint64_t(n) * uint64_t(vpad(op->rank[q], esz)) * esz + 15) / 16 * 16;
+      cd.push_back({op->uptr[q], fu + uoff[q], bu});
+      cd.push_back({op->vptr[q], fv + voff[q], bv});
+      op->uptr[q] = fu + uoff[q];
+      op->vptr[q] = fv + voff[q];
+    }
+  }
+  // descriptors in slices of 2^20 (one CTA each)
+  const size_t slice = size_t(1) << 20;
+  CopyDesc* d_cd = op->mem.alloc_n<CopyDesc>(std::min(cd.size(), slice) + 1, "relayout descriptors");
+  for (size_t b = 0; b < cd.size(); b += slice) {
+    const size_t k = std::min(slice, cd.size() - b);
+    CK(cudaMemcpyAsync(d_cd, cd.data() + b, k * sizeof(CopyDesc), cudaMemcpyHostToDevice, st));
+    CK(launch_copy16(d_cd, int(k), st));
+    CK(cudaStreamSynchronize(st));
+  }
+  op->mem.release(d_cd);
+  for (void* c : op->far_chunks) op->mem.release(c);
+  op->far_chunks.clear();
+}
+
 // Plans, work vectors and statistics, once the far blocks are compressed.
 void build_finish(hodlr_op* op, BuildState& bs, cudaStream_t st) {
   const int64_t n = op->n;
+  relayout_far(op, st);
   const std::vector<const void*>& uptr = op->uptr;
   const std::vector<const void*>& vptr = op->vptr;
   // plans

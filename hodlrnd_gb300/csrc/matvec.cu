@@ -225,10 +225,34 @@ __device__ __forceinline__ float2 to_input<FH>(float a) {
 // copies, R rows per stage (R a multiple of G, so every lane's row order is
 // the one above).  Other items (blocks of more than 128 FP32 or 64 FP64
 // columns) load V directly.
-constexpr int kZWarps = 4;            // warps per CTA of zgemv_kernel
-constexpr int kZStages = 3;           // ring stages per warp
-constexpr int kZStageBytes = 2048;    // V bytes per stage
-constexpr int kZXBytes = 1056;        // input bytes per stage: <= 128 rows x 8 bytes + 2 x 15 alignment slack, rounded to 16
+// Ring shapes (stages x bytes) of the staged kernels; HODLR_TUNE_* override
+// them at compile time for tuning runs.  Two stages per warp measured best on
+// GB300 (the shared memory per warp, not the stage count, limits the warps
+// per SM, and more warps hide more latency than deeper rings).
+#ifndef HODLR_TUNE_Z_STAGES
+#define HODLR_TUNE_Z_STAGES 2
+#endif
+#ifndef HODLR_TUNE_Z_BYTES
+#define HODLR_TUNE_Z_BYTES 2048
+#endif
+#ifndef HODLR_TUNE_P_STAGES
+#define HODLR_TUNE_P_STAGES 2
+#endif
+#ifndef HODLR_TUNE_P_BYTES
+#define HODLR_TUNE_P_BYTES 4096
+#endif
+#ifndef HODLR_TUNE_S_STAGES
+#define HODLR_TUNE_S_STAGES 2
+#endif
+#ifndef HODLR_TUNE_S_BYTES
+#define HODLR_TUNE_S_BYTES 2048
+#endif
+constexpr int kZWarps = 4;                      // warps per CTA of zgemv_kernel
+constexpr int kZStages = HODLR_TUNE_Z_STAGES;   // ring stages per warp
+constexpr int kZStageBytes = HODLR_TUNE_Z_BYTES;  // V bytes per stage
+// input bytes per stage: at most kZStageBytes / 16 rows of 8 bytes, plus 2 x 15
+// bytes of alignment slack, rounded to 16
+constexpr int kZXBytes = (kZStageBytes / 16) * 8 + 32;
 constexpr int kZWarpSmem = 64 + kZStages * (kZStageBytes + kZXBytes);
 static_assert(kZWarpSmem % 16 == 0 && kZXBytes % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
 
@@ -372,10 +396,10 @@ __global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const typena
 // slice's first lane starts, kSStages rounds ahead; each round's mbarrier
 // expects one arrival per slice.  Column j of a piece goes to accumulator
 // j & 1; the slices are added by shuffles at the end.
-constexpr int kSWarps = 4;         // warps per CTA of panel_small_kernel
-constexpr int kSStages = 3;
-constexpr int kSUBytes = 2048;     // segment bytes per round (all slices)
-constexpr int kSXBytes = 2048;     // input bytes per round (all slices)
+constexpr int kSWarps = 4;                     // warps per CTA of panel_small_kernel
+constexpr int kSStages = HODLR_TUNE_S_STAGES;
+constexpr int kSUBytes = HODLR_TUNE_S_BYTES;   // segment bytes per round (all slices)
+constexpr int kSXBytes = HODLR_TUNE_S_BYTES;   // input bytes per round (all slices)
 constexpr int kSWarpSmem = 64 + kSStages * (kSUBytes + kSXBytes);
 static_assert(kSWarpSmem % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
 
@@ -507,8 +531,8 @@ __global__ void __launch_bounds__(kSWarps * 32, 4)
 // kPStageBytes of tile and kPCols columns per stage.  Column j of a segment
 // goes to accumulator set j & 1.
 constexpr int kPWarps = 4;           // warps per CTA of panel_tile_kernel
-constexpr int kPStages = 3;
-constexpr int kPStageBytes = 4096;
+constexpr int kPStages = HODLR_TUNE_P_STAGES;
+constexpr int kPStageBytes = HODLR_TUNE_P_BYTES;
 constexpr int kPCols = 64;           // columns per stage at most
 constexpr int kPXBytes = kPCols * 8 + 32;
 constexpr int kPWarpSmem = 64 + kPStages * (kPStageBytes + kPXBytes);
@@ -917,6 +941,7 @@ static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix
                                                      static_cast<TI*>(in), ld_in);
   } else {
     dim3 g(unsigned((nitems + kZWarps - 1) / kZWarps), unsigned(nrhs));
+    cudaFuncSetAttribute(zgemv_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, kZWarps * kZWarpSmem);
     zgemv_kernel<TA, TACC><<<g, kZWarps * 32, kZWarps * kZWarpSmem, st>>>(zb, items, nitems, static_cast<TY*>(zpart),
                                                                            static_cast<TI*>(in), ld_in);
   }
@@ -1060,6 +1085,20 @@ cudaError_t launch_batch_combine(Prec x, const BatchInst* inst, int count, int64
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(128) copy16_kernel(const CopyDesc* __restrict__ d) {
+  const CopyDesc D = d[blockIdx.x];
+  const int4* s = static_cast<const int4*>(D.src);
+  int4* t = static_cast<int4*>(D.dst);
+  for (uint64_t i = threadIdx.x; i < D.bytes / 16; i += blockDim.x) t[i] = s[i];
+}
+
+cudaError_t launch_copy16(const CopyDesc* d, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  count_launches(1);
+  copy16_kernel<<<unsigned(n), 128, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
 __global__ void split_kernel(const double* __restrict__ x, float2* __restrict__ out, int64_t n) {
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
     const double v = x[i];
@@ -1178,7 +1217,7 @@ cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, con
 namespace {
 
 constexpr int kMWarps = 4;
-constexpr int kMStages = 3;
+constexpr int kMStages = 2;
 constexpr int kMVBytes = 4096;                 // factor bytes per stage
 constexpr int kMXBytes = 4096;                 // input bytes per stage (32 rows of kMR floats)
 constexpr int kMRowBytes = kMR * 4;            // one interleaved entry

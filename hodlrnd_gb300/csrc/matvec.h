@@ -136,6 +136,14 @@ cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, 
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
                           int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st,
                           Accum acc = Accum::kByType);
+// Copy of `bytes` (a multiple of 16) from src to dst, both 16-byte aligned.
+struct CopyDesc {
+  const void* src;
+  void* dst;
+  uint64_t bytes;
+};
+cudaError_t launch_copy16(const CopyDesc* d, int n, cudaStream_t st);
+
 // One instance of a batch of operators: its n rows sit at x_base in the
 // caller's concatenated vectors, at in_base in the batch's input buffer and
 // at y_base in the batch's output slots (nslots slots of n rows each).
