@@ -591,6 +591,70 @@ def run_batch(args):
     B.close()
 
 
+def run_c4(args):
+    """The 4D workload: N = 65536 points uniform in [0,1]^4, A_ij =
+    1/(N^(1/2) |x_i - x_j|^2), A_ii = 1, Nmax = 128, eps_ACA = 1e-8, FP32
+    factors; for d' = -1 and d' = 0: the build, single right-hand-side matvecs
+    (FP32-factor and FP64 operators) and a 64-right-hand-side matvec
+    (multi-RHS kernels, FP32 vectors, one CUDA graph).  With this scaling the
+    operator's off-diagonal row sums grow like N^(1/2) and restarted GMRES
+    stagnates (relative residual about 0.2 after 600 iterations at N = 8192 in
+    the CPU oracle), so the workload is timed on matvecs, not solves."""
+    import torch
+
+    import hodlrnd_gb300 as h
+    from hodlrnd_gb300.batch import HODLRdD_batch
+
+    n, d = args.n if args.n != N_POINTS else 65536, 4
+    rng = np.random.default_rng(SEED + 4)
+    pts = rng.uniform(0.0, 1.0, (n, d))
+    kern = h.Kernel("inv_r2", 1.0 / n ** 0.5, 1.0)
+    box = ([0.0] * d, [1.0] * d)
+    st = torch.cuda.current_stream()
+    out = {"metric": "4D single-RHS and 64-RHS matvecs/s", "unit": "matvecs/s", "n_gpus": 1, "higher_is_better": True,
+           "data": "synthetic", "dtype": "fp32+fp64",
+           "config": {"workload": f"4D, N={n} uniform [0,1]^4, 1/(N^(1/2) r^2), A_ii=1, Nmax=128, eps_ACA=1e-8, "
+                                  "FP32 factors; d' = -1 and 0; 1 and 64 RHS"}, "cases": {}}
+    x = torch.randn(n, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(SEED))
+    y = torch.empty_like(x)
+    reps = max(args.steps, 3)
+    for dp in (-1, 0):
+        res = {}
+        for prec in ("fp32_factors", "fp64"):
+            t0 = time.perf_counter()
+            M = h.HODLRdD_matrix(kern, pts, *box, Nmax=128, eps_ACA=1e-8, INTERACTION_TYPE_ALLOWED=dp,
+                                 precision=prec).Assemble_matrix_operators()
+            t_build = time.perf_counter() - t0
+            r = matvec_rate(M, x, y, st)
+            s = M.statistics()
+            res[prec] = {"matvec_ms": r["ms"], "matvec_GBps": r["GBps"], "build_s": round(t_build, 3),
+                         "far_blocks": s["n_far_blocks"], "dense_far_blocks": s["n_dense_far_blocks"],
+                         "max_rank": s["max_rank"], "far_bytes": s["far_bytes"], "near_bytes": s["near_bytes"],
+                         "device_bytes": s["device_bytes"]}
+            M.close()
+        B = HODLRdD_batch([kern], [pts], [box], Nmax=128, eps_ACA=1e-8, INTERACTION_TYPE_ALLOWED=dp,
+                          precision="mixed")
+        X = torch.randn((64, n), dtype=torch.float32, device="cuda")
+        Y = torch.empty_like(X)
+        for _ in range(3):
+            B.matvec_device(X.data_ptr(), Y.data_ptr(), 64, st.cuda_stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            B.matvec_device(X.data_ptr(), Y.data_ptr(), 64, st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        res["rhs64_matvec"] = {"ms": round(ms, 3), "rhs_matvecs_per_s": round(64 / (ms / 1e3), 1),
+                               "single_rhs_equivalent_speedup_vs_fp32_factors": round(
+                                   res["fp32_factors"]["matvec_ms"] * 64 / ms, 2)}
+        B.close()
+        out["cases"][f"dprime={dp}"] = res
+    out["value"] = out["cases"]["dprime=0"]["rhs64_matvec"]["rhs_matvecs_per_s"]
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -604,7 +668,7 @@ def main():
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--instances", type=int, default=256)
-    ap.add_argument("--workload", choices=["solve", "serving", "batch"], default="solve",
+    ap.add_argument("--workload", choices=["solve", "serving", "batch", "c4"], default="solve",
                     help="serving: replay the request trace through the request loop (its own JSON line)")
     ap.add_argument("--requests", type=int, default=48)
     ap.add_argument("--pool", type=int, default=12)
@@ -616,6 +680,8 @@ def main():
         run_serving(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "c4":
+        run_c4(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

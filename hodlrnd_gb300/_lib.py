@@ -129,9 +129,11 @@ def lib():
     L.hodlr_tree_get.argtypes = [P, I64, I64, I64, I64, I64, I64, I64]
     L.hodlr_tree_destroy.argtypes = [P]
     L.hodlr_set_relax.argtypes = [P, ctypes.c_int32, ctypes.c_double]
+    L.hodlr_op_save.argtypes = [P, D, ctypes.c_char_p]
+    L.hodlr_op_load.argtypes = [P, ctypes.c_char_p, ctypes.POINTER(P)]
     L.hodlr_vec_load.argtypes = [ctypes.c_char_p, D, ctypes.c_int64, I64]
     L.hodlr_vec_save.argtypes = [ctypes.c_char_p, D, ctypes.c_int64]
-    for f in ("hodlr_set_relax", "hodlr_vec_load", "hodlr_vec_save", "hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
+    for f in ("hodlr_op_save", "hodlr_op_load", "hodlr_set_relax", "hodlr_vec_load", "hodlr_vec_save", "hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
               "hodlr_matvec_device", "hodlr_solve", "hodlr_solve_device", "hodlr_stats_get",
               "hodlr_get_permutation", "hodlr_get_blocks", "hodlr_tree_build", "hodlr_tree_sizes",
               "hodlr_tree_get", "hodlr_tree_destroy", "hodlr_get_block", "hodlr_trace_enable", "hodlr_trace_get", "hodlr_set_solver"):

@@ -200,6 +200,7 @@ struct hodlr_ctx {
 struct hodlr_op {
   hodlr_ctx* ctx = nullptr;
   bool keep_host_plans = false;  // set for the operators of a batch
+  std::vector<double> box_lo, box_hi;  // the build's bounding box (kept for hodlr_op_save)
   std::vector<void*> far_chunks; // factor chunks written by the ACA batches (freed by relayout_far)
   bool batch_owned = false;      // freed by hodlr_batch_destroy only
   bool relaxed = false;  // FP32 factors: matvecs use relaxed accumulation (set by the solver)
@@ -1051,6 +1052,8 @@ struct BuildState {
 void build_prepare(hodlr_op* op, const double* points, const double* box_lo, const double* box_hi, cudaStream_t st,
                    BuildState& bs) {
   const int64_t n = op->n;
+  op->box_lo.assign(box_lo, box_lo + op->p.ndim);
+  op->box_hi.assign(box_hi, box_hi + op->p.ndim);
   const double t0 = bs.t0 = now_s();
   TreeParams tp;
   tp.ndim = op->p.ndim;
@@ -1997,6 +2000,165 @@ int hodlr_batch_destroy(hodlr_batch* b) {
   cudaStreamSynchronize(b->ctx->stream);
   delete b;
   return HODLR_OK;
+}
+
+
+// ---- operator files ----------------------------------------------------------
+// Layout (host byte order): magic "HODLRGB\0", u32 version, hodlr_params,
+// hodlr_kernel_desc, i64 n, the n x ndim points (caller order), the box
+// (2 x ndim), i64 far-block count, per block i32 rank and i32 dense, then per
+// block its stored U (or dense tile) and V bytes, in far-block order, each as
+// the engine stores them (esz = 8 for FP64 operators, 4 otherwise).  Loading
+// rebuilds the tree, lists and near field from the points (deterministic) and
+// takes the far field from the file instead of running ACA.
+namespace {
+constexpr char kOpMagic[8] = {'H', 'O', 'D', 'L', 'R', 'G', 'B', 0};
+constexpr uint32_t kOpVersion = 1;
+
+struct OpFile {
+  std::FILE* f = nullptr;
+  ~OpFile() {
+    if (f) std::fclose(f);
+  }
+};
+
+uint64_t block_u_bytes(int64_t m, int64_t n, int32_t rank, int32_t dense, int esz) {
+  return uint64_t(stored_elems(m, dense ? n : rank, esz)) * uint64_t(esz);
+}
+uint64_t block_v_bytes(int64_t n, int32_t rank, int32_t dense, int esz) {
+  return dense ? 0 : uint64_t(n) * uint64_t(vpad(rank, esz)) * uint64_t(esz);
+}
+}  // namespace
+
+int hodlr_op_save(const hodlr_op* op, const double* points, const char* path) {
+  if (!op || !points || !path) return fail(op ? op->ctx : nullptr, HODLR_ERR_INVALID, "hodlr_op_save: null argument");
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    OpFile fh;
+    fh.f = std::fopen(path, "wb");
+    if (!fh.f) throw Failure{HODLR_ERR_IO, std::string("hodlr_op_save: cannot create ") + path};
+    auto put = [&](const void* p, size_t bytes) {
+      if (bytes && std::fwrite(p, 1, bytes, fh.f) != bytes)
+        throw Failure{HODLR_ERR_IO, std::string("hodlr_op_save: write failed: ") + path};
+    };
+    const int d = op->p.ndim;
+    put(kOpMagic, 8);
+    put(&kOpVersion, 4);
+    put(&op->p, sizeof(op->p));
+    put(&op->kd, sizeof(op->kd));
+    put(&op->n, 8);
+    put(points, sizeof(double) * size_t(op->n) * size_t(d));
+    put(op->box_lo.data(), sizeof(double) * size_t(d));
+    put(op->box_hi.data(), sizeof(double) * size_t(d));
+    const int64_t nb = int64_t(op->far.size());
+    put(&nb, 8);
+    put(op->rank.data(), 4 * size_t(nb));
+    put(op->dense.data(), 4 * size_t(nb));
+    const int esz = op->p.precision == HODLR_PREC_FP64 ? 8 : 4;
+    const Tree& t = op->tree;
+    std::vector<char> buf;
+    for (int64_t q = 0; q < nb; q++) {
+      const FarBlock& fb = op->far[size_t(q)];
+      const int64_t m = t.count[size_t(t.gid(fb.level, fb.t))], n = t.count[size_t(t.gid(fb.level, fb.s))];
+      const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
+      if (!dn && r <= 0) continue;
+      const uint64_t bu = block_u_bytes(m, n, r, dn, esz), bv = block_v_bytes(n, r, dn, esz);
+      buf.resize(bu + bv);
+      CK(cudaMemcpy(buf.data(), op->uptr[size_t(q)], bu, cudaMemcpyDeviceToHost));
+      if (bv) CK(cudaMemcpy(buf.data() + bu, op->vptr[size_t(q)], bv, cudaMemcpyDeviceToHost));
+      put(buf.data(), bu + bv);
+    }
+    if (std::fflush(fh.f) != 0) throw Failure{HODLR_ERR_IO, std::string("hodlr_op_save: write failed: ") + path};
+    return HODLR_OK;
+  });
+}
+
+int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out) {
+  if (!ctx || !path || !out) return fail(ctx, HODLR_ERR_INVALID, "hodlr_op_load: null argument");
+  *out = nullptr;
+  std::unique_ptr<hodlr_op> op(new hodlr_op());
+  return guarded(ctx, [&]() -> int {
+    CK(cudaSetDevice(ctx->p.device));
+    cudaStream_t st = ctx->stream;
+    OpFile fh;
+    fh.f = std::fopen(path, "rb");
+    if (!fh.f) throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: cannot open ") + path};
+    auto get = [&](void* p, size_t bytes) {
+      if (bytes && std::fread(p, 1, bytes, fh.f) != bytes)
+        throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: truncated file: ") + path};
+    };
+    char magic[8];
+    uint32_t version = 0;
+    get(magic, 8);
+    get(&version, 4);
+    if (std::memcmp(magic, kOpMagic, 8) != 0 || version != kOpVersion)
+      throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: not an operator file of this version: ") + path};
+    op->ctx = ctx;
+    get(&op->p, sizeof(op->p));
+    get(&op->kd, sizeof(op->kd));
+    get(&op->n, 8);
+    op->p.device = ctx->p.device;
+    op->mem.budget = ctx->p.device_budget_bytes;
+    const int d = op->p.ndim;
+    if (d < 1 || d > kMaxDim || op->n < 1 || op->n > (int64_t(1) << 31) - 1)
+      throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: corrupt header: ") + path};
+    std::memset(&op->st, 0, sizeof(op->st));
+    std::vector<double> pts(size_t(op->n) * size_t(d)), lo(static_cast<size_t>(d)), hi(static_cast<size_t>(d));
+    get(pts.data(), sizeof(double) * pts.size());
+    get(lo.data(), sizeof(double) * size_t(d));
+    get(hi.data(), sizeof(double) * size_t(d));
+    BuildState bs;
+    build_prepare(op.get(), pts.data(), lo.data(), hi.data(), st, bs);
+    int64_t nb = 0;
+    get(&nb, 8);
+    if (nb != int64_t(op->far.size()))
+      throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: far-block count does not match the tree: ") + path};
+    op->rank.assign(size_t(nb), 0);
+    op->dense.assign(size_t(nb), 0);
+    get(op->rank.data(), 4 * size_t(nb));
+    get(op->dense.data(), 4 * size_t(nb));
+    const int esz = op->p.precision == HODLR_PREC_FP64 ? 8 : 4;
+    const Tree& t = op->tree;
+    // one chunk in the compaction layout (each block's U then V, 16-byte aligned)
+    std::vector<uint64_t> off(size_t(nb), 0);
+    uint64_t total = 0;
+    for (int64_t q = 0; q < nb; q++) {
+      const FarBlock& fb = op->far[size_t(q)];
+      const int64_t m = t.count[size_t(t.gid(fb.level, fb.t))], n = t.count[size_t(t.gid(fb.level, fb.s))];
+      const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
+      if (r < 0 || r > std::min(m, n) || (dn != 0 && dn != 1))
+        throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: corrupt block table: ") + path};
+      off[size_t(q)] = total;
+      if (!dn && r <= 0) continue;
+      total += (block_u_bytes(m, n, r, dn, esz) + 15) / 16 * 16 + (block_v_bytes(n, r, dn, esz) + 15) / 16 * 16;
+    }
+    std::vector<char> host(std::max<uint64_t>(total, 16), 0);
+    op->uptr.assign(size_t(nb), nullptr);
+    op->vptr.assign(size_t(nb), nullptr);
+    char* chunk = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(total, 16), "far-field factors"));
+    op->far_chunks.push_back(chunk);
+    for (int64_t q = 0; q < nb; q++) {
+      const FarBlock& fb = op->far[size_t(q)];
+      const int64_t m = t.count[size_t(t.gid(fb.level, fb.t))], n = t.count[size_t(t.gid(fb.level, fb.s))];
+      const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
+      if (!dn && r <= 0) continue;
+      const uint64_t bu = block_u_bytes(m, n, r, dn, esz), bv = block_v_bytes(n, r, dn, esz);
+      const uint64_t vo = off[size_t(q)] + (bu + 15) / 16 * 16;
+      get(host.data() + off[size_t(q)], bu);
+      if (bv) get(host.data() + vo, bv);
+      op->uptr[size_t(q)] = chunk + off[size_t(q)];
+      op->vptr[size_t(q)] = dn ? nullptr : chunk + vo;
+    }
+    char extra;
+    if (std::fread(&extra, 1, 1, fh.f) == 1)
+      throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: trailing bytes: ") + path};
+    CK(cudaMemcpyAsync(chunk, host.data(), std::max<uint64_t>(total, 16), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    op->st.t_aca_s = 0.0;
+    build_finish(op.get(), bs, st);
+    *out = op.release();
+    return HODLR_OK;
+  });
 }
 
 }  // extern "C"

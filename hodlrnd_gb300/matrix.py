@@ -10,6 +10,7 @@ compile-time constants (include/myHeaders.hpp:35-48) are keyword arguments
 with the same names.
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -104,6 +105,37 @@ class HODLRdD_matrix:
         _lib.check(L.hodlr_build(self._ctx, _dp(self.points), self.N, _dp(self.x1), _dp(self.x2), ctypes.byref(kd),
                                  ctypes.byref(op)), self._ctx)
         self._op = op
+        return self
+
+    # ------------------------------------------------------------ files
+    def save(self, path):
+        """Write the built operator to `path` (hodlr_op_save): parameters,
+        kernel, points, box, block ranks and the compressed far field."""
+        self._need_op()
+        _lib.check(_lib.lib().hodlr_op_save(self._op, _dp(self.points), os.fsencode(path)), self._ctx)
+
+    @classmethod
+    def load(cls, path, device=0):
+        """An operator read back by hodlr_op_load (no ACA) on `device`."""
+        L = _lib.lib()
+        self = cls.__new__(cls)
+        p = _lib.HodlrParams()
+        L.hodlr_params_default(ctypes.byref(p))
+        p.device = int(device)
+        self.params = p
+        self._tree = None
+        self._op = None
+        self.last_solve = None
+        self.kernel = None
+        self.points = None
+        ctx = ctypes.c_void_p()
+        _lib.check(L.hodlr_ctx_create(ctypes.byref(p), ctypes.byref(ctx)))
+        self._ctx = ctx
+        op = ctypes.c_void_p()
+        _lib.check(L.hodlr_op_load(self._ctx, os.fsencode(path), ctypes.byref(op)), self._ctx)
+        self._op = op
+        st = self.statistics()
+        self.N = int(st["n"])
         return self
 
     def _need_op(self):

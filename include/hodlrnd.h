@@ -132,6 +132,17 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
                 const hodlr_kernel_desc* kernel, hodlr_op** out);
 int hodlr_op_destroy(hodlr_op* op);
 
+/* Operator files.  hodlr_op_save writes the operator built from `points`
+ * (the caller-order n x ndim array given to hodlr_build) with its parameters,
+ * kernel, box, block ranks and compressed far field; hodlr_op_load rebuilds
+ * the tree, lists and near field from the points and takes the far field from
+ * the file (no ACA), on ctx's device.  Matvecs and solves of the loaded
+ * operator equal the saved one's bit for bit.  Malformed files give
+ * HODLR_ERR_IO.  No counterpart in the reference (it keeps no operator
+ * beyond its process). */
+int hodlr_op_save(const hodlr_op* op, const double* points, const char* path);
+int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out);
+
 /* y = A x (HODLRdD_matrix::operator*, include/HDD_matrix.hpp:43-47).  Host
  * pointers, n x nrhs column-major, caller's point order. */
 int hodlr_matvec(hodlr_op* op, const double* x, double* y, int64_t nrhs);

@@ -252,3 +252,28 @@ def test_relaxed_products_keep_the_true_residual():
     assert rel(xr, xc) < 1e-6
     Mr.close()
     Mc.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_factors", "mixed"])
+def test_operator_file_round_trip(tmp_path, precision):
+    """hodlr_op_save / hodlr_op_load: the loaded operator (tree and near field
+    rebuilt, far field from the file, no ACA) gives the same bits."""
+    c = cases.REF_CASES["hodlr3d_n4096"]
+    f = dict(np.load(os.path.join(GOLDEN, "ref_hodlr3d_n4096.npz")))
+    M = build(c, f["points"], precision=precision)
+    path = tmp_path / "op.bin"
+    M.save(path)
+    L = HODLRdD_matrix.load(path)
+    assert L.statistics()["n_far_blocks"] == M.statistics()["n_far_blocks"]
+    assert L.statistics()["far_bytes"] == M.statistics()["far_bytes"]
+    assert np.array_equal(L.blocks()["rank"], M.blocks()["rank"])
+    assert np.array_equal(L * f["x"], M * f["x"])
+    assert np.array_equal(L.solve(f["b"]), M.solve(f["b"]))
+    # a damaged file is refused
+    blob = path.read_bytes()
+    (tmp_path / "cut.bin").write_bytes(blob[:len(blob) // 2])
+    with pytest.raises(_lib.HodlrError) as e:
+        HODLRdD_matrix.load(tmp_path / "cut.bin")
+    assert e.value.code == _lib.HODLR_ERR_IO
+    L.close()
+    M.close()
