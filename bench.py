@@ -225,7 +225,7 @@ def run_gb300(args):
     stats = M.statistics()
     others = {}
     if not args.headline_only:
-        for prec in ("fp64", "mixed", "fp32_factors"):
+        for prec in ("fp64", "mixed", "fp32_factors", "bf16_factors"):
             if prec != args.precision:
                 others[prec] = h.HODLRdD_matrix(kern, pts, *box, precision=prec, **common).Assemble_matrix_operators()
 
@@ -272,6 +272,10 @@ def run_gb300(args):
                          "inner_iterations": [i["iterations"] for i in inf],
                          "outer_iterations": [i["outer_iterations"] for i in inf],
                          "rel_residual": max(i["rel_residual"] for i in inf)}
+        if "fp64" in others and prec != "fp64":
+            b0 = B[0].cpu().numpy()
+            engines[prec]["rel_residual_fp64_operator"] = float(
+                np.linalg.norm(b0 - others["fp64"] * X2[0].cpu().numpy()) / np.linalg.norm(b0))
 
     # ---- single-RHS matvec throughput of each engine's operator
     matvec = {p: matvec_rate(Mm, B[0], X2[0], stream)
@@ -360,6 +364,9 @@ ENGINE_NOTES = {
                     "field; FP64 GMRES (restart 100, x0 = b) on the FP32-stored operator",
     "mixed": "far-field U, V in FP32; FP64 iterative refinement around FP32 GMRES (inner tol 1e-4)",
     "fp64": "all FP64 (the reference's arithmetic)",
+    "bf16_factors": "far-field U, V and dense far tiles in BF16 with FP32 per-row / per-column scales; FP64 near "
+                    "field; FP64 GMRES on the BF16-stored operator (its residual against the FP64 operator is the "
+                    "BF16 rounding of the far field, about 1e-3)",
 }
 
 
@@ -620,7 +627,7 @@ def run_c4(args):
     reps = max(args.steps, 3)
     for dp in (-1, 0):
         res = {}
-        for prec in ("fp32_factors", "fp64"):
+        for prec in ("fp32_factors", "bf16_factors", "fp64"):
             t0 = time.perf_counter()
             M = h.HODLRdD_matrix(kern, pts, *box, Nmax=128, eps_ACA=1e-8, INTERACTION_TYPE_ALLOWED=dp,
                                  precision=prec).Assemble_matrix_operators()
@@ -662,8 +669,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=N_POINTS)
-    ap.add_argument("--precision", choices=["fp32_factors", "mixed", "fp64"], default="fp32_factors",
-                    help="engine timed for `value`; the other two are timed beside it")
+    ap.add_argument("--precision", choices=["fp32_factors", "mixed", "fp64", "bf16_factors"],
+                    default="fp32_factors", help="engine timed for `value`; the others are timed beside it")
     ap.add_argument("--other-steps", type=int, default=3)
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")

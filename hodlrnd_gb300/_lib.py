@@ -31,6 +31,7 @@ HODLR_KERNEL_EXP_NEG_R = 4
 HODLR_PREC_FP64 = 0
 HODLR_PREC_MIXED = 1
 HODLR_PREC_FP32_FACTORS = 2
+HODLR_PREC_BF16_FACTORS = 3
 
 HODLR_ORTHO_AUTO = 0
 HODLR_ORTHO_MGS = 1

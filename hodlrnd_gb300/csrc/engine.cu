@@ -360,6 +360,7 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
       const TileDesc& d = nt.tiles[q];
       Seg s;
       s.A = static_cast<const char*>(base) + size_t(d.off) * esz;
+      s.cscale = nullptr;
       s.in_off = d.s_begin;
       s.K = d.n;
       s.pad = 0;
@@ -434,10 +435,14 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
       const int32_t ns = int32_t(t.count[size_t(gs)]);
       Seg s;
       s.pad = 0;
+      s.cscale = nullptr;
       if (op->dense[q]) {
         s.A = uptr[q];
         s.in_off = t.begin[size_t(gs)];
         s.K = ns;
+        if (a == Prec::kB)
+          s.cscale = reinterpret_cast<const float*>(static_cast<const char*>(uptr[q]) +
+                                                    far_u_data_bytes(p.m, ns, 0, true, a));
         segs.push_back(s);
       } else if (op->rank[q] > 0) {
         ZBlock z;
@@ -446,6 +451,9 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
         z.z_off = zoff;
         z.n = ns;
         z.r = op->rank[q];
+        z.zscale = a == Prec::kB ? reinterpret_cast<const float*>(static_cast<const char*>(vptr[q]) +
+                                                                  far_v_data_bytes(ns, z.r, false, a))
+                                 : nullptr;
         zb.push_back(z);
         s.A = uptr[q];
         s.in_off = zoff;
@@ -489,8 +497,8 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   std::vector<ZItem> zit;
   std::vector<ZFix> zfix;
   int64_t nzpart = 0;
-  const int esz = a == Prec::kD ? 8 : 4;
-  const int cmax = 32 * (16 / esz);
+  const int esz = prec_size(a);
+  const int cmax = std::min(32 * (16 / esz), kZPart);  // BF16: 128 of the 256 a warp could load
   for (size_t q = 0; q < zb.size(); q++) {
     const int n = zb[q].n, r = zb[q].r;
     const int rp = int(vpad(r, esz));
@@ -532,6 +540,11 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   }
 }
 
+// Element type of the far-field storage.
+Prec far_prec(const hodlr_params& p) {
+  return p.precision == HODLR_PREC_FP64 ? Prec::kD : p.precision == HODLR_PREC_BF16_FACTORS ? Prec::kB : Prec::kF;
+}
+
 // ACA of every far block of the given operators (one, or the instances of a
 // batch: their blocks share every launch), in workspace-bounded batches;
 // compacted factors go to per-batch chunks of each operator's memory (FP64 or
@@ -559,8 +572,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   const size_t nb = size_t(boff[nops]);
   if (nb == 0) return;
   const int ndim = op0->p.ndim;
-  const Prec fp = op0->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
-  const size_t esz = fp == Prec::kD ? 8 : 4;
+  const Prec fp = far_prec(op0->p);
   const int cap0 = op0->p.rank_cap > 0 ? op0->p.rank_cap : 64;
   // global block g = boff[j] + b: operator j, its far block b
   std::vector<int32_t> job(nb), cap(nb), mm(nb), nn(nb);
@@ -737,9 +749,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
       off[q] = bytes[size_t(job[g])];
       const int64_t r = op->rank[b];
-      const uint64_t ub = (uint64_t(stored_elems(mm[g], op->dense[b] ? nn[g] : r, int(esz))) * esz + 15) / 16 * 16;
-      const uint64_t vb = op->dense[b] ? 0 : (uint64_t(nn[g]) * uint64_t(vpad(r, int(esz))) * esz + 15) / 16 * 16;
-      bytes[size_t(job[g])] += ub + vb;
+      bytes[size_t(job[g])] += far_u_bytes(mm[g], nn[g], r, op->dense[b], fp) + far_v_bytes(nn[g], r, op->dense[b], fp);
     }
     std::vector<char*> chunk(nops, nullptr);
     for (size_t j = 0; j < nops; j++)
@@ -760,8 +770,14 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       c.t_map = desc[q].t_map;
       c.s_map = desc[q].s_map;
       c.ws = desc[q].ws;
+      const int32_t rk = std::max(op->rank[b], 0);
       c.u_dst = ch + off[q];
-      c.v_dst = ch + off[q] + (uint64_t(stored_elems(mm[g], std::max(op->rank[b], 0), int(esz))) * esz + 15) / 16 * 16;
+      c.v_dst = ch + off[q] + far_u_bytes(mm[g], nn[g], rk, op->dense[b], fp);
+      c.s_dst = nullptr;
+      if (fp == Prec::kB)
+        c.s_dst = reinterpret_cast<float*>(op->dense[b]
+                                               ? ch + off[q] + far_u_data_bytes(mm[g], nn[g], rk, true, fp)
+                                               : static_cast<char*>(c.v_dst) + far_v_data_bytes(nn[g], rk, false, fp));
       c.m = mm[g];
       c.n = nn[g];
       c.rank = op->rank[b];
@@ -818,14 +834,16 @@ void compute_stats(hodlr_op* op) {
   s.n_flop = flop;
   s.memory_gb = 8e-9 * flop;
   s.compression_ratio = flop / (double(op->n) * double(op->n));
-  const double fesz = op->p.precision == HODLR_PREC_FP64 ? 8.0 : 4.0;
+  const double fesz = double(prec_size(far_prec(op->p)));
   s.near_bytes = uint64_t(s.near_entries * 8.0 * (op->p.precision == HODLR_PREC_MIXED ? 1.5 : 1.0));
   s.far_bytes = uint64_t((s.far_entries + s.dense_far_entries) * fesz);
   s.device_bytes = op->mem.used;
   // Algorithmic bytes per launch of each operator kernel: stored matrix
   // entries once, plus each vector once (re-reads of x are not counted).
-  double lr_rows = 0.0, lr_cols = 0.0, zsum = 0.0;
+  // BF16 factors add their FP32 scales: one per z column, one per dense-tile column.
+  double lr_rows = 0.0, lr_cols = 0.0, zsum = 0.0, dense_cols = 0.0;
   for (size_t b = 0; b < op->far.size(); b++) {
+    if (op->dense[b]) dense_cols += double(t.count[size_t(t.gid(op->far[b].level, op->far[b].s))]);
     if (op->dense[b] || op->rank[b] == 0) continue;
     const double m = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].t))]);
     const double n = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].s))]);
@@ -834,12 +852,14 @@ void compute_stats(hodlr_op* op) {
     zsum += double(op->rank[b]);
   }
   const double N = double(op->n), slots = double(op->nslots);
+  const double ss = far_prec(op->p) == Prec::kB ? 4.0 : 0.0;
   for (int v = 0; v < 2; v++) {  // v = 0: FP64 vectors, 1: FP32 vectors
     const double sx = v == 0 ? 8.0 : 4.0, snear = v == 0 ? 8.0 : 4.0;
     const int kb = v == 0 ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
-    op->tr.bytes[kb + 0] = lr_cols * fesz + zsum * sx + N * sx;
+    op->tr.bytes[kb + 0] = lr_cols * fesz + zsum * (sx + ss) + N * sx;
     op->tr.bytes[kb + 1] = s.near_entries * snear + 2.0 * N * sx;
-    op->tr.bytes[kb + 2] = (lr_rows + s.dense_far_entries) * fesz + zsum * sx + N * sx + N * (slots - 1.0) * sx;
+    op->tr.bytes[kb + 2] = (lr_rows + s.dense_far_entries) * fesz + dense_cols * ss + zsum * sx + N * sx +
+                           N * (slots - 1.0) * sx;
     op->tr.bytes[kb + 3] = N * slots * sx + N * sx;
   }
 }
@@ -872,10 +892,12 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
   Tracer& tr = op->tr;
   if (plan.nzb > 0) tr.start(kb + 0, st);
-  // FP32 factors with FP64 vectors: compensated (or, while the solver allows
-  // it, relaxed) FP32 accumulation on split inputs
-  const bool df = plan.a_far == Prec::kF && px == Prec::kD;
-  const Accum acc = !df ? Accum::kByType : op->relaxed ? Accum::kRelaxed : Accum::kCompensated;
+  // FP32 or BF16 factors with FP64 vectors: compensated (or, while the solver
+  // allows it, relaxed) FP32 accumulation on split inputs
+  const bool df = plan.a_far != Prec::kD && px == Prec::kD;
+  const Accum acc = !df                       ? Accum::kByType
+                    : op->relaxed ? Accum::kRelaxed
+                                  : Accum::kCompensated;
   void* fin = in;
   if (df) {
     fin = op->d_in2;
@@ -934,14 +956,15 @@ void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr
       return apply_tree<double>(op, op->plan64, xi, yo, op->d_in64, op->d_y64, st);
     };
     GmresResult r;
-    // FP32 factors: relaxed accumulation once the residual estimate is below
+    // FP32 or BF16 factors: relaxed accumulation once the residual estimate is below
     // relax_below (tol * 1e5) -- an inexact Krylov method may take products with relative
     // error up to about tol / |r_k| (Simoncini and Szyld, SIAM J. Sci.
     // Comput. 25 (2003); Bouras and Fraysse, SIAM J. Matrix Anal. Appl. 26
     // (2005)), and relaxed products are accurate to about 1e-6 -- then the
     // true residual with compensated products decides, and GMRES continues
     // from x with compensated products while it is above tol.
-    const bool relax = p.precision == HODLR_PREC_FP32_FACTORS && p.relax != HODLR_RELAX_OFF;
+    const bool relax = (p.precision == HODLR_PREC_FP32_FACTORS || p.precision == HODLR_PREC_BF16_FACTORS) &&
+                       p.relax != HODLR_RELAX_OFF;
     const double relax_at = p.relax_below > 0 ? p.relax_below : std::min(1.0, tol * kRelaxFactor);
     std::function<void(double)> progress;
     if (relax) progress = [op, relax_at](double res) { op->relaxed = res < relax_at; };
@@ -1110,7 +1133,7 @@ void build_prepare(hodlr_op* op, const double* points, const double* box_lo, con
 void relayout_far(hodlr_op* op, cudaStream_t st) {
   const size_t nb = op->far.size();
   if (nb == 0 || op->p.precision == HODLR_PREC_FP64) return;
-  const int esz = 4;
+  const Prec fp = far_prec(op->p);
   std::vector<uint64_t> uoff(nb, 0), voff(nb, 0);
   uint64_t ubytes = 0, vbytes = 0;
   const Tree& t = op->tree;
@@ -1118,15 +1141,11 @@ void relayout_far(hodlr_op* op, cudaStream_t st) {
   for (size_t q = 0; q < nb; q++) {
     const int l = op->far[q].level;
     const int64_t m = t.count[size_t(t.gid(l, op->far[q].t))], n = t.count[size_t(t.gid(l, op->far[q].s))];
-    if (op->dense[q]) {
-      uoff[q] = ubytes;
-      ubytes += (uint64_t(stored_elems(m, n, esz)) * esz + 15) / 16 * 16;
-    } else if (op->rank[q] > 0) {
-      uoff[q] = ubytes;
-      ubytes += (uint64_t(stored_elems(m, op->rank[q], esz)) * esz + 15) / 16 * 16;
-      voff[q] = vbytes;
-      vbytes += (uint64_t(n) * uint64_t(vpad(op->rank[q], esz)) * esz + 15) / 16 * 16;
-    }
+    if (!op->dense[q] && op->rank[q] <= 0) continue;
+    uoff[q] = ubytes;
+    ubytes += far_u_bytes(m, n, op->rank[q], op->dense[q], fp);
+    voff[q] = vbytes;
+    vbytes += far_v_bytes(n, op->rank[q], op->dense[q], fp);
   }
   char* fu = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(ubytes, 16), "far-field factors (panel order)"));
   char* fv = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(vbytes, 16), "far-field V factors"));
@@ -1135,16 +1154,11 @@ void relayout_far(hodlr_op* op, cudaStream_t st) {
   for (size_t q = 0; q < nb; q++) {
     const int l = op->far[q].level;
     const int64_t m = t.count[size_t(t.gid(l, op->far[q].t))], n = t.count[size_t(t.gid(l, op->far[q].s))];
-    if (op->dense[q]) {
-      const uint64_t b = (uint64_t(stored_elems(m, n, esz)) * esz + 15) / 16 * 16;
-      cd.push_back({op->uptr[q], fu + uoff[q], b});
-      op->uptr[q] = fu + uoff[q];
-    } else if (op->rank[q] > 0) {
-      const uint64_t bu = (uint64_t(stored_elems(m, op->rank[q], esz)) * esz + 15) / 16 * 16;
-      const uint64_t bv = (uint64_t(n) * uint64_t(vpad(op->rank[q], esz)) * esz + 15) / 16 * 16;
-      cd.push_back({op->uptr[q], fu + uoff[q], bu});
-      cd.push_back({op->vptr[q], fv + voff[q], bv});
-      op->uptr[q] = fu + uoff[q];
+    if (!op->dense[q] && op->rank[q] <= 0) continue;
+    cd.push_back({op->uptr[q], fu + uoff[q], far_u_bytes(m, n, op->rank[q], op->dense[q], fp)});
+    op->uptr[q] = fu + uoff[q];
+    if (!op->dense[q]) {
+      cd.push_back({op->vptr[q], fv + voff[q], far_v_bytes(n, op->rank[q], false, fp)});
       op->vptr[q] = fv + voff[q];
     }
   }
@@ -1169,7 +1183,7 @@ void build_finish(hodlr_op* op, BuildState& bs, cudaStream_t st) {
   const std::vector<const void*>& uptr = op->uptr;
   const std::vector<const void*>& vptr = op->vptr;
   // plans
-  const Prec fp = op->p.precision == HODLR_PREC_FP64 ? Prec::kD : Prec::kF;
+  const Prec fp = far_prec(op->p);
   build_near_plan(op, bs.nt, bs.near64, Prec::kD, op->plan64, st);
   build_far_plan(op, uptr, vptr, fp, op->plan64, st);
   if (op->p.precision == HODLR_PREC_MIXED) {
@@ -1509,7 +1523,8 @@ int hodlr_ctx_create(const hodlr_params* params, hodlr_ctx** out) {
   if (!(p.eps_aca > 0.0) || !(p.eps_aca < 1.0))
     return fail(nullptr, HODLR_ERR_INVALID, "eps_aca must be in (0, 1) (values >= 1 select a fixed rank in the "
                                             "reference, which this engine does not support)");
-  if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED && p.precision != HODLR_PREC_FP32_FACTORS)
+  if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED && p.precision != HODLR_PREC_FP32_FACTORS &&
+      p.precision != HODLR_PREC_BF16_FACTORS)
     return fail(nullptr, HODLR_ERR_INVALID, "unknown precision");
   if (p.restart < 0 || p.restart > 1000) return fail(nullptr, HODLR_ERR_INVALID, "restart must be in 0..1000");
   if (p.ortho < HODLR_ORTHO_AUTO || p.ortho > HODLR_ORTHO_CGS2)
@@ -1754,42 +1769,64 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
     if (n) *n = nn;
     if (rank) *rank = op->rank[size_t(b)];
     if (dense) *dense = op->dense[size_t(b)];
-    const bool f32 = op->p.precision != HODLR_PREC_FP64;
+    const Prec fp = far_prec(op->p);
+    const int esz = prec_size(fp);
+    // stored values (FP64, FP32 or BF16 bits) of `count` elements as doubles
+    auto to_double = [&](const void* src, size_t count) {
+      std::vector<double> out(count);
+      if (fp == Prec::kD) {
+        CK(cudaMemcpy(out.data(), src, count * 8, cudaMemcpyDeviceToHost));
+      } else if (fp == Prec::kF) {
+        std::vector<float> t32(count);
+        CK(cudaMemcpy(t32.data(), src, count * 4, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < count; i++) out[i] = double(t32[i]);
+      } else {
+        std::vector<uint16_t> t16(count);
+        CK(cudaMemcpy(t16.data(), src, count * 2, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < count; i++) {
+          const uint32_t bits = uint32_t(t16[i]) << 16;
+          float f;
+          std::memcpy(&f, &bits, 4);
+          out[i] = double(f);
+        }
+      }
+      return out;
+    };
+    auto scales = [&](const void* at, size_t count) {
+      std::vector<float> s(count);
+      CK(cudaMemcpy(s.data(), at, count * 4, cudaMemcpyDeviceToHost));
+      return s;
+    };
     // copy a stored rows x cols matrix (tiled layout, matvec.h) to a dense column-major dst
     auto fetch = [&](const void* src, size_t rows, size_t cols, double* dst) {
       if (!dst || !src || rows * cols == 0) return;
-      const int esz = f32 ? 4 : 8;
-      const size_t total = size_t(stored_elems(int64_t(rows), int64_t(cols), esz));
-      std::vector<double> tmp(total);
-      if (f32) {
-        std::vector<float> t32(total);
-        CK(cudaMemcpy(t32.data(), src, total * 4, cudaMemcpyDeviceToHost));
-        for (size_t i = 0; i < total; i++) tmp[i] = double(t32[i]);
-      } else {
-        CK(cudaMemcpy(tmp.data(), src, total * 8, cudaMemcpyDeviceToHost));
-      }
+      const std::vector<double> tmp = to_double(src, size_t(stored_elems(int64_t(rows), int64_t(cols), esz)));
       for (size_t c = 0; c < cols; c++)
         for (size_t r = 0; r < rows; r++)
           dst[c * rows + r] = tmp[size_t(elem_offset(int64_t(r), int64_t(c), int64_t(rows), int64_t(cols), esz))];
     };
     CK(cudaSetDevice(op->p.device));
     CK(cudaStreamSynchronize(op->ctx->stream));
+    const char* ub = static_cast<const char*>(op->uptr[size_t(b)]);
     if (op->dense[size_t(b)]) {
-      fetch(op->uptr[size_t(b)], size_t(mm), size_t(nn), U);
+      fetch(ub, size_t(mm), size_t(nn), U);
+      if (U && ub && fp == Prec::kB) {  // BF16: A = A' diag(column scales)
+        const std::vector<float> cs = scales(ub + far_u_data_bytes(mm, nn, 0, true, fp), size_t(nn));
+        for (size_t c = 0; c < size_t(nn); c++)
+          for (size_t r = 0; r < size_t(mm); r++) U[c * size_t(mm) + r] *= double(cs[c]);
+      }
     } else {
       const size_t r = size_t(std::max(op->rank[size_t(b)], 0));
-      fetch(op->uptr[size_t(b)], size_t(mm), r, U);
-      if (V && op->vptr[size_t(b)] && r > 0) {  // V is row major, nn x vpad(r)
-        const int esz = f32 ? 4 : 8;
+      fetch(ub, size_t(mm), r, U);
+      const char* vb = static_cast<const char*>(op->vptr[size_t(b)]);
+      if (U && vb && r > 0 && fp == Prec::kB) {  // BF16: U V^T = U' diag(z scales) V'^T
+        const std::vector<float> zs = scales(vb + far_v_data_bytes(nn, int64_t(r), false, fp), r);
+        for (size_t k = 0; k < r; k++)
+          for (size_t i = 0; i < size_t(mm); i++) U[k * size_t(mm) + i] *= double(zs[k]);
+      }
+      if (V && vb && r > 0) {  // V is row major, nn x vpad(r)
         const size_t rp = size_t(vpad(int64_t(r), esz));
-        std::vector<double> tmp(size_t(nn) * rp);
-        if (f32) {
-          std::vector<float> t32(tmp.size());
-          CK(cudaMemcpy(t32.data(), op->vptr[size_t(b)], t32.size() * 4, cudaMemcpyDeviceToHost));
-          for (size_t i = 0; i < t32.size(); i++) tmp[i] = double(t32[i]);
-        } else {
-          CK(cudaMemcpy(tmp.data(), op->vptr[size_t(b)], tmp.size() * 8, cudaMemcpyDeviceToHost));
-        }
+        const std::vector<double> tmp = to_double(vb, size_t(nn) * rp);
         for (size_t k = 0; k < r; k++)
           for (size_t j = 0; j < size_t(nn); j++) V[k * size_t(nn) + j] = tmp[j * rp + k];
       }
@@ -1902,6 +1939,8 @@ int hodlr_build_batch(hodlr_ctx* ctx, int32_t count, const double* const* points
   }
   if (kernels[0].kind < HODLR_KERNEL_INV_R || kernels[0].kind > HODLR_KERNEL_EXP_NEG_R)
     return fail(ctx, HODLR_ERR_INVALID, "hodlr_build_batch: unknown kernel kind");
+  if (ctx->p.precision == HODLR_PREC_BF16_FACTORS)
+    return fail(ctx, HODLR_ERR_INVALID, "hodlr_build_batch: batches store FP64 or FP32 factors");
   std::unique_ptr<hodlr_batch> b(new hodlr_batch());
   b->ctx = ctx;
   b->vec = ctx->p.precision == HODLR_PREC_MIXED ? Prec::kF : Prec::kD;
@@ -2008,7 +2047,7 @@ int hodlr_batch_destroy(hodlr_batch* b) {
 // hodlr_kernel_desc, i64 n, the n x ndim points (caller order), the box
 // (2 x ndim), i64 far-block count, per block i32 rank and i32 dense, then per
 // block its stored U (or dense tile) and V bytes, in far-block order, each as
-// the engine stores them (esz = 8 for FP64 operators, 4 otherwise).  Loading
+// the engine stores them (FP64, FP32 or BF16 with its scales).  Loading
 // rebuilds the tree, lists and near field from the points (deterministic) and
 // takes the far field from the file instead of running ACA.
 namespace {
@@ -2022,12 +2061,10 @@ struct OpFile {
   }
 };
 
-uint64_t block_u_bytes(int64_t m, int64_t n, int32_t rank, int32_t dense, int esz) {
-  return uint64_t(stored_elems(m, dense ? n : rank, esz)) * uint64_t(esz);
+uint64_t block_u_bytes(int64_t m, int64_t n, int32_t rank, int32_t dense, Prec p) {
+  return far_u_bytes(m, n, rank, dense != 0, p);
 }
-uint64_t block_v_bytes(int64_t n, int32_t rank, int32_t dense, int esz) {
-  return dense ? 0 : uint64_t(n) * uint64_t(vpad(rank, esz)) * uint64_t(esz);
-}
+uint64_t block_v_bytes(int64_t n, int32_t rank, int32_t dense, Prec p) { return far_v_bytes(n, rank, dense != 0, p); }
 }  // namespace
 
 int hodlr_op_save(const hodlr_op* op, const double* points, const char* path) {
@@ -2054,7 +2091,7 @@ int hodlr_op_save(const hodlr_op* op, const double* points, const char* path) {
     put(&nb, 8);
     put(op->rank.data(), 4 * size_t(nb));
     put(op->dense.data(), 4 * size_t(nb));
-    const int esz = op->p.precision == HODLR_PREC_FP64 ? 8 : 4;
+    const Prec esz = far_prec(op->p);
     const Tree& t = op->tree;
     std::vector<char> buf;
     for (int64_t q = 0; q < nb; q++) {
@@ -2117,7 +2154,7 @@ int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out) {
     op->dense.assign(size_t(nb), 0);
     get(op->rank.data(), 4 * size_t(nb));
     get(op->dense.data(), 4 * size_t(nb));
-    const int esz = op->p.precision == HODLR_PREC_FP64 ? 8 : 4;
+    const Prec esz = far_prec(op->p);
     const Tree& t = op->tree;
     // one chunk in the compaction layout (each block's U then V, 16-byte aligned)
     std::vector<uint64_t> off(size_t(nb), 0);
@@ -2130,7 +2167,7 @@ int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out) {
         throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: corrupt block table: ") + path};
       off[size_t(q)] = total;
       if (!dn && r <= 0) continue;
-      total += (block_u_bytes(m, n, r, dn, esz) + 15) / 16 * 16 + (block_v_bytes(n, r, dn, esz) + 15) / 16 * 16;
+      total += block_u_bytes(m, n, r, dn, esz) + block_v_bytes(n, r, dn, esz);
     }
     std::vector<char> host(std::max<uint64_t>(total, 16), 0);
     op->uptr.assign(size_t(nb), nullptr);
@@ -2143,7 +2180,7 @@ int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out) {
       const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
       if (!dn && r <= 0) continue;
       const uint64_t bu = block_u_bytes(m, n, r, dn, esz), bv = block_v_bytes(n, r, dn, esz);
-      const uint64_t vo = off[size_t(q)] + (bu + 15) / 16 * 16;
+      const uint64_t vo = off[size_t(q)] + bu;
       get(host.data() + off[size_t(q)], bu);
       if (bv) get(host.data() + vo, bv);
       op->uptr[size_t(q)] = chunk + off[size_t(q)];

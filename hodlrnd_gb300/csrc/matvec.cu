@@ -1,4 +1,6 @@
 // HODLR matvec kernels (see matvec.h).
+#include <cuda_bf16.h>
+
 #include "bulk.cuh"
 #include "device.cuh"
 #include "matvec.h"
@@ -20,8 +22,22 @@ __device__ __forceinline__ T ldg(const T* p) {
   return __ldg(p);
 }
 
+// BF16 storage element (bits only; arithmetic converts to FP32)
+struct bf16 {
+  unsigned short b;
+};
+template <>
+__device__ __forceinline__ bf16 ldg<bf16>(const bf16* p) {
+  return bf16{__ldg(reinterpret_cast<const unsigned short*>(p))};
+}
+__device__ __forceinline__ float bf2f(unsigned short b) { return __uint_as_float(uint32_t(b) << 16); }
+
 template <typename T>
 struct Vec16;
+template <>
+struct Vec16<bf16> {
+  using type = uint4;  // 8 BF16 values
+};
 template <>
 struct Vec16<float> {
   using type = float4;
@@ -55,6 +71,8 @@ struct Acc<float> {
   static __device__ __forceinline__ A zero() { return 0.f; }
   static __device__ __forceinline__ void fma(A& a, float v, X x) { a += v * x; }
   static __device__ __forceinline__ A add(A a, A b) { return a + b; }
+  static __device__ __forceinline__ A scale(A a, float s) { return a * s; }
+  static __device__ __forceinline__ X xscale(X x, float s) { return x * s; }
   static __device__ __forceinline__ A shfl_xor(A a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
   static __device__ __forceinline__ X shfl(X x, int src) { return __shfl_sync(0xffffffffu, x, src); }
   static __device__ __forceinline__ double value(A a) { return double(a); }
@@ -70,6 +88,8 @@ struct Acc<double> {
   static __device__ __forceinline__ void fma(A& a, float v, X x) { a += double(v) * x; }
   static __device__ __forceinline__ void fma(A& a, double v, X x) { a += v * x; }
   static __device__ __forceinline__ A add(A a, A b) { return a + b; }
+  static __device__ __forceinline__ A scale(A a, float s) { return a * double(s); }
+  static __device__ __forceinline__ X xscale(X x, float s) { return x * double(s); }
   static __device__ __forceinline__ A shfl_xor(A a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
   static __device__ __forceinline__ X shfl(X x, int src) { return __shfl_sync(0xffffffffu, x, src); }
   static __device__ __forceinline__ double value(A a) { return a; }
@@ -102,6 +122,13 @@ struct Acc<DF> {
     a.hi = s;
     a.lo = __fadd_rn(a.lo, __fadd_rn(t, e));
   }
+  static __device__ __forceinline__ void fma(A& a, bf16 v, X x) { fma(a, bf2f(v.b), x); }
+  // (hi + lo) * s with the rounding error of hi * s kept (TwoProduct by FMA)
+  static __device__ __forceinline__ A scale(A a, float s) {
+    const float p = __fmul_rn(a.hi, s);
+    return DF{p, __fmaf_rn(a.lo, s, __fmaf_rn(a.hi, s, -p))};
+  }
+  static __device__ __forceinline__ X xscale(X x, float s) { return scale(x, s); }
   static __device__ __forceinline__ A add(A a, A b) {
     const float s = __fadd_rn(a.hi, b.hi);
     const float bb = __fsub_rn(s, a.hi);
@@ -159,7 +186,10 @@ struct Acc<FH> {
   static __device__ __forceinline__ X in(float v) { return v; }
   static __device__ __forceinline__ A zero() { return 0.f; }
   static __device__ __forceinline__ void fma(A& a, float v, X x) { a = __fmaf_rn(v, x, a); }
+  static __device__ __forceinline__ void fma(A& a, bf16 v, X x) { a = __fmaf_rn(bf2f(v.b), x, a); }
   static __device__ __forceinline__ A add(A a, A b) { return a + b; }
+  static __device__ __forceinline__ A scale(A a, float s) { return a * s; }
+  static __device__ __forceinline__ X xscale(X x, float s) { return x * s; }
   static __device__ __forceinline__ A shfl_xor(A a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
   static __device__ __forceinline__ X shfl(X x, int src) { return __shfl_sync(0xffffffffu, x, src); }
   static __device__ __forceinline__ double value(A a) { return double(a); }
@@ -186,8 +216,24 @@ __device__ __forceinline__ void axpy16(const double2& a, X x, typename Acc<TACC>
   Acc<TACC>::fma(acc[1], a.y, x);
 }
 
+template <typename TACC, typename X>
+__device__ __forceinline__ void axpy16(const uint4& a, X x, typename Acc<TACC>::A* acc) {
+  Acc<TACC>::fma(acc[0], __uint_as_float(a.x << 16), x);
+  Acc<TACC>::fma(acc[1], __uint_as_float(a.x & 0xffff0000u), x);
+  Acc<TACC>::fma(acc[2], __uint_as_float(a.y << 16), x);
+  Acc<TACC>::fma(acc[3], __uint_as_float(a.y & 0xffff0000u), x);
+  Acc<TACC>::fma(acc[4], __uint_as_float(a.z << 16), x);
+  Acc<TACC>::fma(acc[5], __uint_as_float(a.z & 0xffff0000u), x);
+  Acc<TACC>::fma(acc[6], __uint_as_float(a.w << 16), x);
+  Acc<TACC>::fma(acc[7], __uint_as_float(a.w & 0xffff0000u), x);
+}
+
 template <typename T>
 __device__ __forceinline__ T vzero();
+template <>
+__device__ __forceinline__ uint4 vzero<uint4>() {
+  return make_uint4(0u, 0u, 0u, 0u);
+}
 template <>
 __device__ __forceinline__ float4 vzero<float4>() {
   return make_float4(0.f, 0.f, 0.f, 0.f);
@@ -195,6 +241,25 @@ __device__ __forceinline__ float4 vzero<float4>() {
 template <>
 __device__ __forceinline__ double2 vzero<double2>() {
   return make_double2(0.0, 0.0);
+}
+
+// Input value of column j of a segment: x_j, times the column scale of a BF16
+// dense tile (cs non-null).
+template <typename TACC, typename TX>
+__device__ __forceinline__ typename Acc<TACC>::X seg_in(TX x, const float* cs, int j) {
+  return cs ? Acc<TACC>::xscale(Acc<TACC>::in(x), __ldg(cs + j)) : Acc<TACC>::in(x);
+}
+
+// An input value back in the staged (hi, lo) form, after scaling.
+template <typename TACC>
+__device__ __forceinline__ float2 x_pair(typename Acc<TACC>::X x);
+template <>
+__device__ __forceinline__ float2 x_pair<DF>(DF x) {
+  return make_float2(x.hi, x.lo);
+}
+template <>
+__device__ __forceinline__ float2 x_pair<FH>(float x) {
+  return make_float2(x, 0.f);
 }
 
 template <typename TACC>
@@ -246,6 +311,12 @@ __device__ __forceinline__ float2 to_input<FH>(float a) {
 #endif
 #ifndef HODLR_TUNE_S_BYTES
 #define HODLR_TUNE_S_BYTES 2048
+#endif
+#ifndef HODLR_TUNE_S_MINB
+#define HODLR_TUNE_S_MINB 4  // leaf-panel CTAs per SM the register allocation must allow
+#endif
+#ifndef HODLR_TUNE_P_MINB
+#define HODLR_TUNE_P_MINB 4
 #endif
 constexpr int kZWarps = 4;                      // warps per CTA of zgemv_kernel
 constexpr int kZStages = HODLR_TUNE_Z_STAGES;   // ring stages per warp
@@ -364,6 +435,8 @@ __global__ void __launch_bounds__(kZWarps * 32) zgemv_kernel(const ZBlock* __res
 #pragma unroll
     for (int q = 0; q < CPL; q++) {
       const int c = p * CPL + q;
+      // BF16: z columns carry the product of U's and V's column scales
+      if (sizeof(TA) == 2 && Z.zscale && it.k0 + c < Z.r) acc[q] = AC::scale(acc[q], __ldg(Z.zscale + it.k0 + c));
       if (it.part < 0) {
         if (it.k0 + c < Z.r) z[it.k0 + c] = to_input<TACC>(acc[q]);
       } else {
@@ -395,20 +468,30 @@ __global__ void zfix_kernel(const ZFix* __restrict__ fix, int nfix, const typena
 // below to the one above) is staged in shared memory by bulk copies that the
 // slice's first lane starts, kSStages rounds ahead; each round's mbarrier
 // expects one arrival per slice.  Column j of a piece goes to accumulator
-// j & 1; the slices are added by shuffles at the end.
+// j & 1; the slices are added by shuffles at the end.  For a BF16 dense tile
+// the slice's lanes first multiply the staged inputs by the tile's column
+// scales, in place (once per column rather than once per entry).
 constexpr int kSWarps = 4;                     // warps per CTA of panel_small_kernel
 constexpr int kSStages = HODLR_TUNE_S_STAGES;
 constexpr int kSUBytes = HODLR_TUNE_S_BYTES;   // segment bytes per round (all slices)
-constexpr int kSXBytes = HODLR_TUNE_S_BYTES;   // input bytes per round (all slices)
-constexpr int kSWarpSmem = 64 + kSStages * (kSUBytes + kSXBytes);
-static_assert(kSWarpSmem % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
+// input bytes per round (all slices): twice as many for BF16, whose pieces
+// hold more columns per byte of segment
+template <typename TA>
+__host__ __device__ constexpr int s_xbytes() { return sizeof(TA) == 2 ? 2 * kSUBytes : kSUBytes; }
+template <typename TA>
+__host__ __device__ constexpr int s_warp_smem() { return 64 + kSStages * (kSUBytes + s_xbytes<TA>()); }
+// every slice's piece holds at least 16 bytes' worth of columns (cmax >= Q
+// below) for any m <= 32 with these budgets
+static_assert(kSUBytes >= 2048 && kSUBytes % 16 == 0, "leaf-panel stage too small");
+static_assert(s_warp_smem<float>() % 16 == 0 && s_warp_smem<bf16>() % 16 == 0,
+              "bulk copy destinations must stay 16-byte aligned");
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 
 template <typename TA, typename TACC>
-__global__ void __launch_bounds__(kSWarps * 32, 4)
+__global__ void __launch_bounds__(kSWarps * 32, HODLR_TUNE_S_MINB)
     panel_small_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
                        int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
                        typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
@@ -417,6 +500,7 @@ __global__ void __launch_bounds__(kSWarps * 32, 4)
   using AC = Acc<TACC>;
   constexpr int esz = int(sizeof(TA));
   constexpr int Q = 16 / esz;  // piece columns are a multiple of Q
+  constexpr int kSXBytes = s_xbytes<TA>(), kSWarpSmem = s_warp_smem<TA>();
   extern __shared__ __align__(16) unsigned char ssm[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w = blockIdx.x * kSWarps + wid;
@@ -493,6 +577,20 @@ __global__ void __launch_bounds__(kSWarps * 32, 4)
       for (int t = q; t < min(q + kSStages, rounds); t++) mbar_wait(bar + t % kSStages, uint32_t(t / kSStages) & 1u);
       return;
     }
+    if constexpr (sizeof(TA) == 2) {
+      // BF16 dense tile: the slice's lanes multiply the staged inputs by the
+      // column scales once, in place, before the products
+      if (cs < it.seg_e) {
+        const Seg S = segs[cs];
+        if (S.cscale) {
+          const int c = min(cmax, S.K - cc);
+          const int xo = int((reinterpret_cast<uintptr_t>(inc + S.in_off + cc) & 15u) / sizeof(TX));
+          TX* sx = reinterpret_cast<TX*>(stage0 + st * (kSUBytes + kSXBytes) + kSUBytes + sl * xb) + xo;
+          for (int j = i; j < c; j += mpad) sx[j] = x_pair<TACC>(seg_in<TACC>(sx[j], S.cscale, cc + j));
+        }
+      }
+      __syncwarp();
+    }
     if (cs < it.seg_e) {
       const Seg S = segs[cs];
       const int c = min(cmax, S.K - cc);
@@ -525,11 +623,12 @@ __global__ void __launch_bounds__(kSWarps * 32, 4)
 // Phase 2, panels of more than 32 rows: item chunk = row tile t of the
 // panel (T = 512 / sizeof(TA) rows, lane l owns rows t*T + l*RPL ..).  Every
 // segment's tile is h x K, column major with column stride h (h = the tile's
-// row count rounded up to 4), so a run of its columns is one contiguous byte
+// row count rounded up to height_quantum rows), so a run of its columns is one contiguous byte
 // range, and so is the run of their input values.  Both are staged through a
 // per-warp ring of kPStages shared-memory stages by bulk copies, at most
 // kPStageBytes of tile and kPCols columns per stage.  Column j of a segment
-// goes to accumulator set j & 1.
+// goes to accumulator set j & 1.  BF16 dense tiles: the warp multiplies the
+// staged inputs by the column scales first, as in the leaf-panel kernel.
 constexpr int kPWarps = 4;           // warps per CTA of panel_tile_kernel
 constexpr int kPStages = HODLR_TUNE_P_STAGES;
 constexpr int kPStageBytes = HODLR_TUNE_P_BYTES;
@@ -539,7 +638,7 @@ constexpr int kPWarpSmem = 64 + kPStages * (kPStageBytes + kPXBytes);
 static_assert(kPWarpSmem % 16 == 0 && kPXBytes % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
 
 template <typename TA, typename TACC>
-__global__ void __launch_bounds__(kPWarps * 32, 4)
+__global__ void __launch_bounds__(kPWarps * 32, HODLR_TUNE_P_MINB)
     panel_tile_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
                       int nitems, typename IO<TACC>::TY* __restrict__ ypart,
                       const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
@@ -627,26 +726,36 @@ __global__ void __launch_bounds__(kPWarps * 32, 4)
     const int xo = int((reinterpret_cast<uintptr_t>(inc + S.in_off + cc) & 15u) / sizeof(TX));
     const TX* xsm = reinterpret_cast<const TX*>(xbuf + st * kPXBytes) + xo;
     const unsigned char* us = ubuf + st * kPStageBytes + lane * 16;
+    if constexpr (sizeof(TA) == 2) {
+      // BF16 dense tile: the staged inputs times the column scales, once, in place
+      if (S.cscale) {
+        TX* xw = const_cast<TX*>(xsm);
+        for (int j = lane; j < nc; j += 32) xw[j] = x_pair<TACC>(seg_in<TACC>(xw[j], S.cscale, cc + j));
+        __syncwarp();
+      }
+    }
+#define HODLR_XIN(j_) AC::in(xsm[j_])
     int j = 0;
     for (; j + 1 < nc; j += 2) {
       const VT v0 = act ? *reinterpret_cast<const VT*>(us + j * colb) : vzero<VT>();
       const VT v1 = act ? *reinterpret_cast<const VT*>(us + (j + 1) * colb) : vzero<VT>();
       // column cc + j has the parity of cc + j
       if (((cc + j) & 1) == 0) {
-        axpy16<TACC>(v0, AC::in(xsm[j]), a0);
-        axpy16<TACC>(v1, AC::in(xsm[j + 1]), a1);
+        axpy16<TACC>(v0, HODLR_XIN(j), a0);
+        axpy16<TACC>(v1, HODLR_XIN(j + 1), a1);
       } else {
-        axpy16<TACC>(v0, AC::in(xsm[j]), a1);
-        axpy16<TACC>(v1, AC::in(xsm[j + 1]), a0);
+        axpy16<TACC>(v0, HODLR_XIN(j), a1);
+        axpy16<TACC>(v1, HODLR_XIN(j + 1), a0);
       }
     }
     if (j < nc) {
       const VT v0 = act ? *reinterpret_cast<const VT*>(us + j * colb) : vzero<VT>();
       if (((cc + j) & 1) == 0)
-        axpy16<TACC>(v0, AC::in(xsm[j]), a0);
+        axpy16<TACC>(v0, HODLR_XIN(j), a0);
       else
-        axpy16<TACC>(v0, AC::in(xsm[j]), a1);
+        axpy16<TACC>(v0, HODLR_XIN(j), a1);
     }
+#undef HODLR_XIN
     cc += nc;
     __syncwarp();
     HODLR_PANEL_ISSUE_NEXT();  // the next run, if any, into the stage just consumed
@@ -919,6 +1028,66 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
   }
 }
 
+// BF16 storage of the same blocks, every factor scaled per column.  A dense
+// tile keeps, per column j, the FP32 scale c_j = max_i |A_ij| (in s_dst) and
+// the BF16 entries A_ij / c_j (round to nearest even); a low-rank block keeps
+// per column k the scales su_k = max_i |U_ik|, sv_k = max_j |V_jk| and
+// U_ik / su_k, V_jk / sv_k in BF16, with su_k * sv_k (the scale of
+// z_k = V_k^T x) in s_dst.  A zero column gets scale 1.  One warp per column.
+__device__ __forceinline__ unsigned short to_bf16_bits(double v) {
+  return __bfloat16_as_ushort(__float2bfloat16_rn(float(v)));
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) compact_bf16_kernel(PointsDev P, KernelDev K, const double* __restrict__ ws,
+                                                           const int32_t* __restrict__ lmap,
+                                                           const CompactDesc* __restrict__ blocks, int nblocks) {
+  const CompactDesc B = blocks[blockIdx.x];
+  unsigned short* u = static_cast<unsigned short*>(B.u_dst);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  if (B.kscale != 0.0) K.scale = B.kscale;
+  if (B.dense) {
+    for (int j = warp; j < B.n; j += nw) {
+      double mx = 0.0;
+      for (int i = lane; i < B.m; i += 32) {
+        double xi[D];
+        load_point<D>(P, B.t_begin + i, xi);
+        mx = fmax(mx, fabs(kernel_entry<D>(P, K, B.t_begin + i, B.s_begin + j, xi)));
+      }
+      mx = warp_max(mx);
+      const float sc = mx > 0.0 ? float(mx) : 1.0f;
+      for (int i = lane; i < B.m; i += 32) {
+        double xi[D];
+        load_point<D>(P, B.t_begin + i, xi);
+        u[elem_offset(i, j, B.m, B.n, 2)] = to_bf16_bits(kernel_entry<D>(P, K, B.t_begin + i, B.s_begin + j, xi) / sc);
+      }
+      if (lane == 0) B.s_dst[j] = sc;
+    }
+  } else {
+    const double* Vw = ws + B.ws + int64_t(B.m) * B.cap;
+    unsigned short* v = static_cast<unsigned short*>(B.v_dst);
+    const int64_t rp = vpad(B.rank, 2);
+    for (int k = warp; k < B.rank; k += nw) {
+      const double* Uk = ws + B.ws + int64_t(k) * B.m;
+      const double* Vk = Vw + int64_t(k) * B.n;
+      double mu = 0.0, mv = 0.0;
+      for (int i = lane; i < B.m; i += 32) mu = fmax(mu, fabs(Uk[i]));
+      for (int j = lane; j < B.n; j += 32) mv = fmax(mv, fabs(Vk[j]));
+      mu = warp_max(mu);
+      mv = warp_max(mv);
+      const float su = mu > 0.0 ? float(mu) : 1.0f, sv = mv > 0.0 ? float(mv) : 1.0f;
+      for (int i = lane; i < B.m; i += 32)
+        u[elem_offset(lmap[B.t_map + i] - B.t_begin, k, B.m, B.rank, 2)] = to_bf16_bits(Uk[i] / su);
+      for (int j = lane; j < B.n; j += 32) v[(lmap[B.s_map + j] - B.s_begin) * rp + k] = to_bf16_bits(Vk[j] / sv);
+      if (lane == 0) B.s_dst[k] = su * sv;
+    }
+  }
+}
+
 unsigned warps_grid(int64_t items) { return unsigned((items + kWarpsPerCta - 1) / kWarpsPerCta); }
 
 unsigned vec_grid(int64_t n) {
@@ -935,7 +1104,7 @@ static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix
                     int64_t ld_in, int nrhs, cudaStream_t st) {
   using TI = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
-  if (sizeof(TA) == 8) {
+  if constexpr (sizeof(TA) == 8) {  // FP64 storage: direct loads
     dim3 g(warps_grid(nitems), unsigned(nrhs));
     zgemv_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(zb, items, nitems, static_cast<TY*>(zpart),
                                                      static_cast<TI*>(in), ld_in);
@@ -961,6 +1130,10 @@ cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, i
     zgemv_t<float, DF>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else if (a == Prec::kF && x == Prec::kD && acc == Accum::kRelaxed)
     zgemv_t<float, FH>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+  else if (a == Prec::kB && x == Prec::kD && acc == Accum::kRelaxed)
+    zgemv_t<bf16, FH>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
+  else if (a == Prec::kB && x == Prec::kD)
+    zgemv_t<bf16, DF>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else if (a == Prec::kF && x == Prec::kF)
     zgemv_t<float, float>(zb, items, nitems, fix, nfix, zpart, in, ld_in, nrhs, st);
   else
@@ -968,18 +1141,14 @@ cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, i
   return cudaGetLastError();
 }
 
+// FP32 and BF16 storage: the bulk-copy staged kernels
 template <typename TA, typename TACC>
-static void panels_t(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big, int nbig,
-                     const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y, int64_t ld_y,
-                     int nslots, int nrhs, cudaStream_t st) {
+static void panels_staged(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big,
+                          int nbig, const void* in, int64_t ld_in, void* ypart, void* y, int64_t ld_y, int nslots,
+                          int nrhs, cudaStream_t st) {
   using TI = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
-  if (nbig > 0 && sizeof(TA) == 8) {
-    dim3 g(warps_grid(nbig), unsigned(nrhs));
-    panel_tile_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, big, nbig, static_cast<TY*>(ypart),
-                                                          static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y,
-                                                          nslots);
-  } else if (nbig > 0) {
+  if (nbig > 0) {
     dim3 g(unsigned((nbig + kPWarps - 1) / kPWarps), unsigned(nrhs));
     // above the default 48 KB of dynamic shared memory; set on every launch
     // (the attribute is per device and cheap to set)
@@ -989,16 +1158,35 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
         panels, segs, big, nbig, static_cast<TY*>(ypart), static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y,
         nslots);
   }
-  if (nsmall > 0 && sizeof(TA) == 8) {
-    dim3 g(warps_grid(nsmall), unsigned(nrhs));
-    panel_small_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TI*>(in),
-                                                           ld_in, static_cast<TY*>(y), ld_y, nslots);
-  } else if (nsmall > 0) {
+  if (nsmall > 0) {
     dim3 g(unsigned((nsmall + kSWarps - 1) / kSWarps), unsigned(nrhs));
     cudaFuncSetAttribute(panel_small_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kSWarps * kSWarpSmem);
-    panel_small_kernel<TA, TACC><<<g, kSWarps * 32, kSWarps * kSWarpSmem, st>>>(
+                         kSWarps * s_warp_smem<TA>());
+    panel_small_kernel<TA, TACC><<<g, kSWarps * 32, kSWarps * s_warp_smem<TA>(), st>>>(
         panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots);
+  }
+}
+
+template <typename TA, typename TACC>
+static void panels_t(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big, int nbig,
+                     const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y, int64_t ld_y,
+                     int nslots, int nrhs, cudaStream_t st) {
+  using TI = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
+  if constexpr (sizeof(TA) == 8) {  // FP64 storage: direct loads
+    if (nbig > 0) {
+      dim3 g(warps_grid(nbig), unsigned(nrhs));
+      panel_tile_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, big, nbig, static_cast<TY*>(ypart),
+                                                            static_cast<const TI*>(in), ld_in, static_cast<TY*>(y),
+                                                            ld_y, nslots);
+    }
+    if (nsmall > 0) {
+      dim3 g(warps_grid(nsmall), unsigned(nrhs));
+      panel_small_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TI*>(in),
+                                                             ld_in, static_cast<TY*>(y), ld_y, nslots);
+    }
+  } else {
+    panels_staged<TA, TACC>(panels, segs, small, nsmall, big, nbig, in, ld_in, ypart, y, ld_y, nslots, nrhs, st);
   }
   if (nfix > 0) {
     const int rows = int(tile_rows(int(sizeof(TA))));
@@ -1007,6 +1195,7 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
                                              static_cast<TY*>(y), ld_y, nslots);
   }
 }
+
 
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
@@ -1022,6 +1211,12 @@ cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, 
   else if (a == Prec::kF && x == Prec::kD && acc == Accum::kRelaxed)
     panels_t<float, FH>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
                         st);
+  else if (a == Prec::kB && x == Prec::kD && acc == Accum::kRelaxed)
+    panels_t<bf16, FH>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
+                       st);
+  else if (a == Prec::kB && x == Prec::kD)
+    panels_t<bf16, DF>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
+                       st);
   else if (a == Prec::kF && x == Prec::kF)
     panels_t<float, float>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
                            st);
@@ -1182,6 +1377,8 @@ static void compact_d(const PointsDev& P, const KernelDev& K, const double* ws, 
                       const CompactDesc* blocks, int nblocks, Prec op, cudaStream_t st) {
   if (op == Prec::kD)
     compact_kernel<D, double><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, lmap, blocks, nblocks);
+  else if (op == Prec::kB)
+    compact_bf16_kernel<D><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, lmap, blocks, nblocks);
   else
     compact_kernel<D, float><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, lmap, blocks, nblocks);
 }

@@ -34,19 +34,22 @@ struct Panel {
 // With m <= 32 it is plain column major.  Larger matrices are read 16 bytes
 // per lane, 32 lanes per warp, so they are cut into row tiles of
 // tile_rows(esz) = 512 / esz rows (128 FP32, 64 FP64), each tile stored
-// column major on its own with its height rounded up to 4 rows (zero padding):
-// a warp working on one tile then streams one contiguous region.
+// column major on its own with its height rounded up to a multiple of
+// height_quantum(esz) rows (zero padding; 4, or 8 for BF16 so that every
+// column starts on 16 bytes): a warp working on one tile then streams one
+// contiguous region.
 __host__ __device__ inline int64_t tile_rows(int esz) { return 512 / esz; }
+__host__ __device__ inline int64_t height_quantum(int esz) { return esz < 4 ? 16 / esz : 4; }
 __host__ __device__ inline int64_t tile_height(int64_t m, int64_t t, int esz) {
-  const int64_t T = tile_rows(esz);
+  const int64_t T = tile_rows(esz), q = height_quantum(esz);
   int64_t rows = m - t * T;
   if (rows > T) rows = T;
-  return (rows + 3) / 4 * 4;
+  return (rows + q - 1) / q * q;
 }
 __host__ __device__ inline int64_t stored_elems(int64_t m, int64_t K, int esz) {
   if (m <= 32) return m * K;
-  const int64_t T = tile_rows(esz), full = m / T, rem = m - full * T;
-  return (full * T + (rem + 3) / 4 * 4) * K;
+  const int64_t T = tile_rows(esz), full = m / T, rem = m - full * T, q = height_quantum(esz);
+  return (full * T + (rem + q - 1) / q * q) * K;
 }
 __host__ __device__ inline int64_t elem_offset(int64_t i, int64_t k, int64_t m, int64_t K, int esz) {
   if (m <= 32) return k * m + i;
@@ -59,6 +62,7 @@ struct Seg {
   int64_t in_off;  // offset of the K inputs in the input buffer
   int32_t K;
   int32_t pad;
+  const float* cscale;  // BF16 dense tiles: the K column scales (input j is multiplied by cscale[j]); else null
 };
 
 // One warp's share of phase 2: rows chunk * kRowsPerItem(prec) ... of the
@@ -95,6 +99,7 @@ struct ZBlock {
   int64_t x_off;   // tree position of the source node
   int64_t z_off;   // offset of z_b in the input buffer
   int32_t n, r;
+  const float* zscale;  // BF16: the r column scales of z; else null
 };
 
 // One warp's share of phase 1: columns [k0, k0 + nk) of block zb (all of
@@ -116,7 +121,29 @@ struct ZFix {
 };
 
 // Element types: A = stored matrix, X = vectors, ACC = accumulation.
-enum class Prec { kD, kF };  // double, float
+enum class Prec { kD, kF, kB };  // double, float, bfloat16 (far-field storage only)
+
+__host__ __device__ inline int prec_size(Prec p) { return p == Prec::kD ? 8 : p == Prec::kF ? 4 : 2; }
+
+// Storage of one far block (m x n, rank r, or dense), 16-byte aligned pieces:
+// U (or the dense tile), then for BF16 a dense tile's n FP32 column scales;
+// V, then for BF16 the r FP32 column scales of z (the product of U's and V's
+// column scales).  BF16 thus stores every factor per-column scaled.
+__host__ __device__ inline uint64_t round16(uint64_t b) { return (b + 15) / 16 * 16; }
+__host__ __device__ inline uint64_t far_u_data_bytes(int64_t m, int64_t n, int64_t r, bool dense, Prec p) {
+  const int esz = prec_size(p);
+  return round16(uint64_t(stored_elems(m, dense ? n : r, esz)) * uint64_t(esz));
+}
+__host__ __device__ inline uint64_t far_u_bytes(int64_t m, int64_t n, int64_t r, bool dense, Prec p) {
+  return far_u_data_bytes(m, n, r, dense, p) + ((p == Prec::kB && dense) ? round16(uint64_t(n) * 4) : 0);
+}
+__host__ __device__ inline uint64_t far_v_data_bytes(int64_t n, int64_t r, bool dense, Prec p) {
+  const int esz = prec_size(p);
+  return dense ? 0 : round16(uint64_t(n) * uint64_t(vpad(r, esz)) * uint64_t(esz));
+}
+__host__ __device__ inline uint64_t far_v_bytes(int64_t n, int64_t r, bool dense, Prec p) {
+  return far_v_data_bytes(n, r, dense, p) + ((p == Prec::kB && !dense) ? round16(uint64_t(r) * 4) : 0);
+}
 
 // in:   input buffer [x (ld_in rows of x) | z], nrhs columns with leading dimension ld_in
 // y:    output slots, slot s of column c at y + (c * nslots + s) * ld_y
@@ -185,7 +212,7 @@ cudaError_t launch_split(const double* x, void* out, int64_t n, cudaStream_t st)
 // (every wait is bounded); the value is valid once `st` has synchronised.
 cudaError_t read_stream_timeouts(unsigned int* host, cudaStream_t st);
 // rows handled by one big-panel item for stored element size `a`
-inline int rows_per_item(Prec a) { return a == Prec::kD ? 64 : 128; }
+inline int rows_per_item(Prec a) { return int(tile_rows(prec_size(a))); }
 // out[perm[i] + c*ld_out] (or out[i + c*ld_out] when perm == NULL) =
 //   sum_s y[(c*nslots + s)*ld_y + i], i < n
 cudaError_t launch_combine(Prec x, const void* y, int64_t ld_y, int nslots, int64_t n, int nrhs, const int64_t* perm,
@@ -218,6 +245,7 @@ struct CompactDesc {
   int32_t cap;        // workspace columns (V starts after m * cap doubles)
   int32_t pad;
   double kscale;      // kernel scale for a dense block's entries; 0: the launch's K.scale
+  float* s_dst;       // BF16: column scales of a dense tile, or z column scales of a low-rank block
 };
 // U row i (reference order) lands on tree row lmap[t_map + i] - t_begin; V likewise.
 cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,

@@ -91,7 +91,7 @@ int predict(const hodlr_params& p, const double* pts, int64_t n, const double* l
   for (int64_t k = 0; k + 1 < int64_t(nl.leaf_ptr.size()); k++)
     for (int64_t q = nl.leaf_ptr[size_t(k)]; q < nl.leaf_ptr[size_t(k + 1)]; q++)
       near_entries += double(t.count[size_t(t.gid(L, k))]) * double(t.count[size_t(t.gid(L, nl.src[size_t(q)]))]);
-  const double fesz = p.precision == HODLR_PREC_FP64 ? 8.0 : 4.0;
+  const double fesz = p.precision == HODLR_PREC_FP64 ? 8.0 : p.precision == HODLR_PREC_BF16_FACTORS ? 2.0 : 4.0;
   double far_entries = 0, sum_mn = 0;
   for (const hodlr::FarBlock& b : far) {
     const double m = double(t.count[size_t(t.gid(b.level, b.t))]);

@@ -49,7 +49,8 @@ class HODLRdD_matrix:
         p.tol = float(tol) if tol is not None else 0.0
         p.max_iter = int(max_iter)
         p.precision = {"fp64": _lib.HODLR_PREC_FP64, "mixed": _lib.HODLR_PREC_MIXED,
-                       "fp32_factors": _lib.HODLR_PREC_FP32_FACTORS}[precision]
+                       "fp32_factors": _lib.HODLR_PREC_FP32_FACTORS,
+                       "bf16_factors": _lib.HODLR_PREC_BF16_FACTORS}[precision]
         p.device = int(device)
         p.device_budget_bytes = int(device_budget_bytes)
         p.rank_cap = int(rank_cap)

@@ -87,7 +87,8 @@ def make_params(ndim, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0, precis
     p.tol = float(tol) if tol is not None else 0.0
     p.max_iter = int(max_iter)
     p.precision = {"fp64": _lib.HODLR_PREC_FP64, "mixed": _lib.HODLR_PREC_MIXED,
-                   "fp32_factors": _lib.HODLR_PREC_FP32_FACTORS}[precision]
+                   "fp32_factors": _lib.HODLR_PREC_FP32_FACTORS,
+                   "bf16_factors": _lib.HODLR_PREC_BF16_FACTORS}[precision]
     p.inner_tol = float(inner_tol)
     p.max_outer = int(max_outer)
     p.ortho = {"auto": _lib.HODLR_ORTHO_AUTO, "mgs": _lib.HODLR_ORTHO_MGS, "cgs2": _lib.HODLR_ORTHO_CGS2}[ortho]

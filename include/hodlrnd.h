@@ -63,6 +63,10 @@ typedef struct hodlr_kernel_desc {
 #define HODLR_PREC_FP64 0  /* everything FP64 (the reference's arithmetic, include/myHeaders.hpp:66-72) */
 #define HODLR_PREC_MIXED 1 /* far-field U, V in FP32; FP64 near field; solve = FP64 iterative
                               refinement around an FP32 inner GMRES */
+#define HODLR_PREC_BF16_FACTORS 3 /* far-field U, V and dense far blocks in BF16 with one FP32 scale per
+                                     column of U and V (folded into z) or per row of a dense block; products
+                                     summed in FP32; FP64 near field; FP64 GMRES.  For loose eps_aca
+                                     (about 1e-4): BF16 keeps 8 significant bits. */
 #define HODLR_PREC_FP32_FACTORS 2 /* far-field U, V in FP32, every product accumulated in compensated
                                      FP32 (FP64-level accuracy); FP64 near field; FP64 GMRES as the
                                      reference's solve, on the FP32-stored operator */

@@ -254,7 +254,7 @@ def test_relaxed_products_keep_the_true_residual():
     Mc.close()
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32_factors", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32_factors", "mixed", "bf16_factors"])
 def test_operator_file_round_trip(tmp_path, precision):
     """hodlr_op_save / hodlr_op_load: the loaded operator (tree and near field
     rebuilt, far field from the file, no ACA) gives the same bits."""
