@@ -199,7 +199,10 @@ def matvec_rate(M, x, y, stream):
     M.trace(False)
     ms = t0.elapsed_time(t1) / MATVEC_REPS
     nbytes = sum(v["bytes_per_launch"] * v["launches"] for v in tr.values()) / MATVEC_REPS
-    return {"ms": round(ms, 4), "bytes": nbytes, "GBps": round(nbytes / (ms / 1e3) / 1e9, 1)}
+    groups = {k: {"ms": round(v["total_ms"] / v["launches"], 4),
+                  "GBps": round(v["bytes_per_launch"] / (v["total_ms"] / v["launches"] / 1e3) / 1e9, 1)}
+              for k, v in tr.items() if v["launches"]}
+    return {"ms": round(ms, 4), "bytes": nbytes, "GBps": round(nbytes / (ms / 1e3) / 1e9, 1), "groups": groups}
 
 
 def run_gb300(args):
@@ -600,13 +603,16 @@ def run_batch(args):
 
 def run_c4(args):
     """The 4D workload: N = 65536 points uniform in [0,1]^4, A_ij =
-    1/(N^(1/2) |x_i - x_j|^2), A_ii = 1, Nmax = 128, eps_ACA = 1e-8, FP32
-    factors; for d' = -1 and d' = 0: the build, single right-hand-side matvecs
-    (FP32-factor and FP64 operators) and a 64-right-hand-side matvec
-    (multi-RHS kernels, FP32 vectors, one CUDA graph).  With this scaling the
-    operator's off-diagonal row sums grow like N^(1/2) and restarted GMRES
-    stagnates (relative residual about 0.2 after 600 iterations at N = 8192 in
-    the CPU oracle), so the workload is timed on matvecs, not solves."""
+    1/(N^(1/2) |x_i - x_j|^2), A_ii = 1, Nmax = 128, for d' = -1 and d' = 0:
+    eps_ACA = 1e-4 with BF16 per-column-scaled factors and FP32 accumulation,
+    then eps_ACA = 1e-8 with FP32 factors (and the FP64 operator beside it);
+    for each the build and single right-hand-side matvecs, and a
+    64-right-hand-side matvec of the 1e-8 FP32 operator (multi-RHS kernels,
+    FP32 vectors, one CUDA graph).  Each reduced-precision product is compared
+    with the FP64 operator's on the same x.  With this scaling the operator's
+    off-diagonal row sums grow like N^(1/2) and restarted GMRES stagnates
+    (relative residual about 0.2 after 600 iterations at N = 8192 in the CPU
+    oracle), so the workload is timed on matvecs, not solves."""
     import torch
 
     import hodlrnd_gb300 as h
@@ -619,26 +625,35 @@ def run_c4(args):
     box = ([0.0] * d, [1.0] * d)
     st = torch.cuda.current_stream()
     out = {"metric": "4D single-RHS and 64-RHS matvecs/s", "unit": "matvecs/s", "n_gpus": 1, "higher_is_better": True,
-           "data": "synthetic", "dtype": "fp32+fp64",
-           "config": {"workload": f"4D, N={n} uniform [0,1]^4, 1/(N^(1/2) r^2), A_ii=1, Nmax=128, eps_ACA=1e-8, "
-                                  "FP32 factors; d' = -1 and 0; 1 and 64 RHS"}, "cases": {}}
+           "data": "synthetic", "dtype": "bf16+fp32+fp64",
+           "config": {"workload": f"4D, N={n} uniform [0,1]^4, 1/(N^(1/2) r^2), A_ii=1, Nmax=128; d' = -1 and 0; "
+                                  "eps_ACA=1e-4 BF16 per-column-scaled factors, FP32 accumulation; eps_ACA=1e-8 "
+                                  "FP32 factors; 1 and 64 RHS"}, "cases": {}}
     x = torch.randn(n, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(SEED))
     y = torch.empty_like(x)
     reps = max(args.steps, 3)
+    engines = (("bf16_factors", 1e-4, "always"), ("fp32_factors", 1e-8, True), ("fp64", 1e-8, True))
     for dp in (-1, 0):
-        res = {}
-        for prec in ("fp32_factors", "bf16_factors", "fp64"):
+        res, ys = {}, {}
+        for prec, eps, relax in engines:
             t0 = time.perf_counter()
-            M = h.HODLRdD_matrix(kern, pts, *box, Nmax=128, eps_ACA=1e-8, INTERACTION_TYPE_ALLOWED=dp,
-                                 precision=prec).Assemble_matrix_operators()
+            M = h.HODLRdD_matrix(kern, pts, *box, Nmax=128, eps_ACA=eps, INTERACTION_TYPE_ALLOWED=dp,
+                                 precision=prec, relax=relax).Assemble_matrix_operators()
             t_build = time.perf_counter() - t0
             r = matvec_rate(M, x, y, st)
+            ys[prec] = y.cpu().numpy().copy()
             s = M.statistics()
-            res[prec] = {"matvec_ms": r["ms"], "matvec_GBps": r["GBps"], "build_s": round(t_build, 3),
+            res[prec] = {"eps_ACA": eps, "accumulation": "fp32" if relax == "always" else
+                         ("fp64" if prec == "fp64" else "compensated fp32"),
+                         "matvec_ms": r["ms"], "matvec_GBps": r["GBps"], "matvec_groups": r["groups"],
+                         "build_s": round(t_build, 3),
                          "far_blocks": s["n_far_blocks"], "dense_far_blocks": s["n_dense_far_blocks"],
                          "max_rank": s["max_rank"], "far_bytes": s["far_bytes"], "near_bytes": s["near_bytes"],
                          "device_bytes": s["device_bytes"]}
             M.close()
+        y64 = ys["fp64"]
+        for prec in ("bf16_factors", "fp32_factors"):
+            res[prec]["rel_diff_vs_fp64_operator"] = float(np.linalg.norm(ys[prec] - y64) / np.linalg.norm(y64))
         B = HODLRdD_batch([kern], [pts], [box], Nmax=128, eps_ACA=1e-8, INTERACTION_TYPE_ALLOWED=dp,
                           precision="mixed")
         X = torch.randn((64, n), dtype=torch.float32, device="cuda")

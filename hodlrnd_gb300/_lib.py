@@ -39,6 +39,16 @@ HODLR_ORTHO_CGS2 = 2
 
 HODLR_RELAX_AUTO = 0
 HODLR_RELAX_OFF = 1
+HODLR_RELAX_ALWAYS = 2
+
+
+def relax_code(relax):
+    """True: relaxed products once the residual allows; False: never; "always": every product."""
+    if isinstance(relax, str):
+        if relax != "always":
+            raise ValueError(f"relax: True, False or 'always', not {relax!r}")
+        return HODLR_RELAX_ALWAYS
+    return HODLR_RELAX_AUTO if relax else HODLR_RELAX_OFF
 
 
 class HodlrParams(ctypes.Structure):

@@ -896,8 +896,8 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   // allows it, relaxed) FP32 accumulation on split inputs
   const bool df = plan.a_far != Prec::kD && px == Prec::kD;
   const Accum acc = !df                       ? Accum::kByType
-                    : op->relaxed ? Accum::kRelaxed
-                                  : Accum::kCompensated;
+                    : op->relaxed || op->p.relax == HODLR_RELAX_ALWAYS ? Accum::kRelaxed
+                                                                       : Accum::kCompensated;
   void* fin = in;
   if (df) {
     fin = op->d_in2;
@@ -1529,8 +1529,8 @@ int hodlr_ctx_create(const hodlr_params* params, hodlr_ctx** out) {
   if (p.restart < 0 || p.restart > 1000) return fail(nullptr, HODLR_ERR_INVALID, "restart must be in 0..1000");
   if (p.ortho < HODLR_ORTHO_AUTO || p.ortho > HODLR_ORTHO_CGS2)
     return fail(nullptr, HODLR_ERR_INVALID, "unknown orthogonalisation");
-  if (p.relax != HODLR_RELAX_AUTO && p.relax != HODLR_RELAX_OFF)
-    return fail(nullptr, HODLR_ERR_INVALID, "relax must be HODLR_RELAX_AUTO or HODLR_RELAX_OFF");
+  if (p.relax != HODLR_RELAX_AUTO && p.relax != HODLR_RELAX_OFF && p.relax != HODLR_RELAX_ALWAYS)
+    return fail(nullptr, HODLR_ERR_INVALID, "relax must be HODLR_RELAX_AUTO, _OFF or _ALWAYS");
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev == 0)
@@ -1706,8 +1706,8 @@ int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_so
 
 int hodlr_set_relax(hodlr_op* op, int32_t relax, double relax_below) {
   if (!op) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_set_relax: null argument");
-  if (relax != HODLR_RELAX_AUTO && relax != HODLR_RELAX_OFF)
-    return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_set_relax: relax must be HODLR_RELAX_AUTO or HODLR_RELAX_OFF");
+  if (relax != HODLR_RELAX_AUTO && relax != HODLR_RELAX_OFF && relax != HODLR_RELAX_ALWAYS)
+    return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_set_relax: relax must be HODLR_RELAX_AUTO, _OFF or _ALWAYS");
   op->p.relax = relax;
   op->p.relax_below = relax_below;
   return HODLR_OK;

@@ -70,37 +70,38 @@ __global__ void __launch_bounds__(kThreads)
 
 // Classical Gram-Schmidt, one pass (applied twice per Arnoldi step: CGS2).
 // cgs_dots: part[j * kVecCtas + cta] = this CTA's share of <w, v_j> for
-// j < nv, eight vectors at a time so each thread keeps eight loads in flight.
+// j < nv.  Grid kVecCtas x ceil(nv / 8): CTA (cta, g) takes vectors
+// 8g .. 8g + 7, so every group runs at once and each thread keeps eight
+// loads in flight; a partial's summation order depends only on cta.
+constexpr int kDotGroup = 8;
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     cgs_dots_kernel(const T* __restrict__ w, const T* __restrict__ V, int64_t n, int nv, double* __restrict__ part) {
-  constexpr int U = 8;
+  constexpr int U = kDotGroup;
   __shared__ double sh[U][kThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int j0 = 0; j0 < nv; j0 += U) {
-    const int jn = min(U, nv - j0);
-    double acc[U];
+  const int j0 = blockIdx.y * U;
+  const int jn = min(U, nv - j0);
+  double acc[U];
 #pragma unroll
-    for (int u = 0; u < U; u++) acc[u] = 0.0;
-    for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads) {
-      const double wi = to_d(w[i]);
+  for (int u = 0; u < U; u++) acc[u] = 0.0;
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads) {
+    const double wi = to_d(w[i]);
 #pragma unroll
-      for (int u = 0; u < U; u++)
-        if (u < jn) acc[u] += to_d(V[int64_t(j0 + u) * n + i]) * wi;
-    }
+    for (int u = 0; u < U; u++)
+      if (u < jn) acc[u] += to_d(V[int64_t(j0 + u) * n + i]) * wi;
+  }
 #pragma unroll
-    for (int u = 0; u < U; u++) {
+  for (int u = 0; u < U; u++) {
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
-      if (lane == 0) sh[u][wid] = acc[u];
-    }
-    __syncthreads();
-    if (threadIdx.x < jn) {
-      double v = 0.0;
-      for (int q = 0; q < kThreads / 32; q++) v += sh[threadIdx.x][q];
-      part[int64_t(j0 + threadIdx.x) * kVecCtas + blockIdx.x] = v;
-    }
-    __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+    if (lane == 0) sh[u][wid] = acc[u];
+  }
+  __syncthreads();
+  if (threadIdx.x < jn) {
+    double v = 0.0;
+    for (int q = 0; q < kThreads / 32; q++) v += sh[threadIdx.x][q];
+    part[int64_t(j0 + threadIdx.x) * kVecCtas + blockIdx.x] = v;
   }
 }
 
@@ -363,7 +364,8 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
         // CGS2: two classical passes against v_0 .. v_i, |w|^2 from the second
         for (int pass = 0; pass < 2; pass++) {
           count_launches(3);
-          cgs_dots_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, i + 1, W.partk);
+          cgs_dots_kernel<T><<<dim3(kVecCtas, unsigned((i + 1 + kDotGroup - 1) / kDotGroup)), kThreads, 0, st>>>(
+              W.w, W.V, n, i + 1, W.partk);
           cgs_reduce_kernel<<<i + 1, kThreads, 0, st>>>(W.partk, W.hc, W.H + int64_t(i) * ldh, pass);
           cgs_update_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, i + 1, W.hc, pass == 1 ? part0 : nullptr);
         }

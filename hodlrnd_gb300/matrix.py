@@ -57,7 +57,7 @@ class HODLRdD_matrix:
         p.inner_tol = float(inner_tol)
         p.max_outer = int(max_outer)
         p.ortho = {"auto": _lib.HODLR_ORTHO_AUTO, "mgs": _lib.HODLR_ORTHO_MGS, "cgs2": _lib.HODLR_ORTHO_CGS2}[ortho]
-        p.relax = _lib.HODLR_RELAX_AUTO if relax else _lib.HODLR_RELAX_OFF
+        p.relax = _lib.relax_code(relax)
         p.relax_below = float(relax_below)
         self.params = p
         self._ctx = None
@@ -201,9 +201,10 @@ class HODLRdD_matrix:
                                                float(inner_tol), int(max_outer)), self._ctx)
 
     def set_relax(self, relax=True, relax_below=0.0):
-        """FP32-factor solves: relaxed products on/off and their threshold (0: tol * 1e5)."""
+        """FP32/BF16-factor solves: relaxed products (True: once the residual allows, False: never,
+        "always": every product, FP32 accumulation) and their threshold (0: tol * 1e5)."""
         self._need_op()
-        _lib.check(_lib.lib().hodlr_set_relax(self._op, _lib.HODLR_RELAX_AUTO if relax else _lib.HODLR_RELAX_OFF,
+        _lib.check(_lib.lib().hodlr_set_relax(self._op, _lib.relax_code(relax),
                                               float(relax_below)), self._ctx)
 
     # ------------------------------------------------------------ introspection

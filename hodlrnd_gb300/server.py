@@ -92,7 +92,7 @@ def make_params(ndim, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0, precis
     p.inner_tol = float(inner_tol)
     p.max_outer = int(max_outer)
     p.ortho = {"auto": _lib.HODLR_ORTHO_AUTO, "mgs": _lib.HODLR_ORTHO_MGS, "cgs2": _lib.HODLR_ORTHO_CGS2}[ortho]
-    p.relax = _lib.HODLR_RELAX_AUTO if relax else _lib.HODLR_RELAX_OFF
+    p.relax = _lib.relax_code(relax)
     p.relax_below = float(relax_below)
     return p
 

@@ -87,18 +87,22 @@ typedef struct hodlr_params {
   int32_t max_outer; /* MIXED: iterative-refinement sweeps (0 = default 10) */
   double inner_tol;  /* MIXED: relative-residual target of each FP32 inner GMRES (<= 0: default 1e-4) */
   int32_t ortho;     /* GMRES orthogonalisation, HODLR_ORTHO_* */
-  int32_t relax;     /* FP32_FACTORS: HODLR_RELAX_AUTO (relaxed products once the residual allows) or _OFF */
-  double relax_below; /* FP32_FACTORS: relative residual estimate below which products are relaxed
-                         (<= 0: the default, tol * 1e5) */
+  int32_t relax;     /* FP32_FACTORS, BF16_FACTORS: HODLR_RELAX_AUTO, _OFF or _ALWAYS */
+  double relax_below; /* FP32_FACTORS, BF16_FACTORS: relative residual estimate below which products
+                         are relaxed (<= 0: the default, tol * 1e5) */
 } hodlr_params;
 
-/* FP32_FACTORS solves: once GMRES's residual estimate is below relax_below, the
- * matvecs sum the FP32 products in plain FP32 (about 1e-6 relative, which an
- * inexact Krylov method tolerates at that residual) instead of compensated
- * FP32; the solve ends only when the true residual, with compensated
- * products, is at most tol (GMRES continues from x otherwise). */
+/* FP32_FACTORS and BF16_FACTORS solves: once GMRES's residual estimate is
+ * below relax_below, the matvecs sum the products in plain FP32 (about 1e-6
+ * relative, which an inexact Krylov method tolerates at that residual)
+ * instead of compensated FP32; the solve ends only when the true residual,
+ * with compensated products, is at most tol (GMRES continues from x
+ * otherwise).  HODLR_RELAX_OFF: compensated products throughout.
+ * HODLR_RELAX_ALWAYS: plain FP32 sums for every product (matvecs, solves and
+ * the true residual) -- FP32 accumulation, for loose tolerances (>= ~1e-5). */
 #define HODLR_RELAX_AUTO 0
 #define HODLR_RELAX_OFF 1
+#define HODLR_RELAX_ALWAYS 2
 
 /* GMRES orthogonalisation.  MGS is the reference's (include/GMRES.hpp:236-240)
  * and needs i + 2 kernel launches at Arnoldi step i; CGS2 (classical

@@ -50,7 +50,8 @@ def test_params_default_are_the_reference_defaults():
 
 
 @pytest.mark.parametrize("field,value", [("ndim", 0), ("ndim", 9), ("dprime", 2), ("dprime", -2), ("nmax", 0),
-                                         ("eps_aca", 0.0), ("eps_aca", 2.0), ("precision", 7)])
+                                         ("eps_aca", 0.0), ("eps_aca", 2.0), ("precision", 7), ("relax", 3),
+                                         ("ortho", 5)])
 def test_ctx_create_rejects_bad_parameters(field, value):
     L = _lib.lib()
     p = _lib.HodlrParams()
@@ -61,6 +62,14 @@ def test_ctx_create_rejects_bad_parameters(field, value):
     assert rc == _lib.HODLR_ERR_INVALID
     assert not ctx
     assert _lib.last_error(None)
+
+
+def test_relax_codes():
+    assert _lib.relax_code(True) == _lib.HODLR_RELAX_AUTO
+    assert _lib.relax_code(False) == _lib.HODLR_RELAX_OFF
+    assert _lib.relax_code("always") == _lib.HODLR_RELAX_ALWAYS
+    with pytest.raises(ValueError):
+        _lib.relax_code("sometimes")
 
 
 def test_null_arguments_are_rejected():

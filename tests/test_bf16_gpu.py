@@ -87,3 +87,23 @@ def test_bf16_solve_backward_error():
     assert np.linalg.norm(xb - x64) <= 0.1 * np.linalg.norm(x64)
     M64.close()
     Mb.close()
+
+
+def test_bf16_fp32_accumulation():
+    """relax="always": every product summed in plain FP32 (FP32 accumulation),
+    the true residual included -- within 1e-5 of the compensated products of
+    the same stored operator, and a solve at tol 1e-5 converges on it."""
+    c = cases.REF_CASES["hodlr3d_n4096"]
+    f = dict(np.load(os.path.join(GOLDEN, "ref_hodlr3d_n4096.npz")))
+    M64 = build(c, f["points"])
+    Mc = build(c, f["points"], precision="bf16_factors")
+    Mf = build(c, f["points"], precision="bf16_factors", relax="always", tol=1e-5)
+    yc, yf = Mc * f["x"], Mf * f["x"]
+    assert not np.array_equal(yc, yf)
+    assert np.linalg.norm(yf - yc) <= 1e-5 * np.linalg.norm(yc)
+    xf = Mf.solve(f["b"])
+    info = Mf.last_solve
+    assert info["converged"] == 1 and info["rel_residual"] <= 1e-5
+    assert np.linalg.norm(f["b"] - M64 * xf) <= 5e-3 * np.linalg.norm(f["b"])
+    for M in (M64, Mc, Mf):
+        M.close()
