@@ -318,6 +318,7 @@ NearTiles near_tiles(const Tree& t, const NearList& nl, int esz) {
 // far panels above 32 rows are many (one per node and level), near ones are
 // few (leaves above 32 points) and get more, smaller items.
 constexpr int kPanelCols = 256;
+constexpr int64_t kSmallItemBytes = 48 * 1024;  // factor bytes per leaf-panel item, about
 constexpr int kNearPanelCols = 48;
 
 // Runs of consecutive segments [begin, end) with about `max_cols` columns each.
@@ -467,7 +468,18 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
       const int np = int(panels.size());
       panels.push_back(p);
       if (p.m <= 32) {
-        small.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+        // one warp per leaf panel, or per run of about kSmallItemBytes of its
+        // factors when it has more (partial rows added by the fix-up kernel):
+        // a few panels with very long interaction lists would otherwise keep
+        // single warps busy long after the rest
+        const int max_cols = int(std::max<int64_t>(64, kSmallItemBytes / (int64_t(p.m) * prec_size(a))));
+        const std::vector<std::pair<int32_t, int32_t>> groups = column_groups(segs, p.seg_begin, p.seg_end, max_cols);
+        if (groups.size() == 1) {
+          small.push_back({np, 0, int32_t(p.seg_begin), int32_t(p.seg_end), -1});
+        } else {
+          pfix.push_back({np, 0, int32_t(nypart), int32_t(groups.size())});
+          for (auto& g : groups) small.push_back({np, 0, g.first, g.second, int32_t(nypart++)});
+        }
       } else {
         const std::vector<std::pair<int32_t, int32_t>> groups = column_groups(segs, p.seg_begin, p.seg_end, kPanelCols);
         const int rows = rows_per_item(a);
@@ -507,12 +519,14 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
       const int rows = std::max(1, kZItemBytes / (nk * esz));
       const int groups = (n + rows - 1) / rows;
       if (groups == 1) {
-        zit.push_back({int32_t(q), k0, nk, 0, n, -1});
+        zit.push_back({int32_t(q), k0, nk, 0, n, -1, 0, 0});
+        z_item_stages(zit.back(), r, esz);
         continue;
       }
       for (int c = 0; c < nk && k0 + c < r; c++) zfix.push_back({zb[q].z_off + k0 + c, int32_t(nzpart + c), groups});
       for (int g = 0; g < groups; g++) {
-        zit.push_back({int32_t(q), k0, nk, g * rows, std::min(n, (g + 1) * rows), int32_t(nzpart)});
+        zit.push_back({int32_t(q), k0, nk, g * rows, std::min(n, (g + 1) * rows), int32_t(nzpart), 0, 0});
+        z_item_stages(zit.back(), r, esz);
         nzpart += kZPart;
       }
     }

@@ -327,6 +327,59 @@ constexpr int kZXBytes = (kZStageBytes / 16) * 8 + 32;
 constexpr int kZWarpSmem = 64 + kZStages * (kZStageBytes + kZXBytes);
 static_assert(kZWarpSmem % 16 == 0 && kZXBytes % 16 == 0, "bulk copy destinations must stay 16-byte aligned");
 
+// The end of an item: acc[q] (column p * CPL + q of the item) is summed over
+// the G = 32 / P lanes sharing p by a transposed butterfly -- while a lane
+// holds several columns, each exchange hands half of them to the partner
+// lane and keeps the other half -- so lane l ends with the total of column
+// p * CPL + coff(l) + k in acc[k], k < w; lanes that differ only in the bits
+// of the plain exchanges that follow hold the same totals, and the one with
+// those bits clear writes them.
+template <typename TA, typename TACC>
+__device__ __forceinline__ void z_finish(typename Acc<TACC>::A* acc, int P, int lane, const ZItem& it,
+                                         const ZBlock& Z, typename IO<TACC>::TI* z,
+                                         typename IO<TACC>::TY* zpart) {
+  using AC = Acc<TACC>;
+  constexpr int CPL = 16 / int(sizeof(TA));
+  int coff = 0, w = CPL, o = 16;
+#pragma unroll
+  for (int lv = 0; (CPL >> lv) > 1; lv++, o >>= 1) {
+    if (o < P) break;
+    const int half = CPL >> (lv + 1);
+    const bool up = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < CPL / 2; k++) {
+      if (k < half) {
+        const typename AC::A send = up ? acc[k] : acc[k + half];
+        const typename AC::A keep = up ? acc[k + half] : acc[k];
+        acc[k] = AC::add(keep, AC::shfl_xor(send, o));
+      }
+    }
+    if (up) coff += half;
+    w = half;
+  }
+  bool writer = true;
+  for (; o >= P; o >>= 1) {  // w == 1 here
+    acc[0] = AC::add(acc[0], AC::shfl_xor(acc[0], o));
+    if (lane & o) writer = false;
+  }
+  const int p = lane % P;
+  if (!writer || p * CPL >= it.nk) return;
+#pragma unroll
+  for (int k = 0; k < CPL; k++) {
+    if (k < w) {
+      const int c = p * CPL + coff + k;  // column within the item
+      typename AC::A v = acc[k];
+      // BF16: z columns carry the product of U's and V's column scales
+      if (sizeof(TA) == 2 && Z.zscale && it.k0 + c < Z.r) v = AC::scale(v, __ldg(Z.zscale + it.k0 + c));
+      if (it.part < 0) {
+        if (it.k0 + c < Z.r) z[it.k0 + c] = to_input<TACC>(v);
+      } else {
+        zpart[it.part + c] = typename IO<TACC>::TY(AC::value(v));
+      }
+    }
+  }
+}
+
 template <typename TA, typename TACC>
 __global__ void __launch_bounds__(kZWarps * 32) zgemv_kernel(const ZBlock* __restrict__ zb,
                                                            const ZItem* __restrict__ items, int nitems,
@@ -346,27 +399,27 @@ __global__ void __launch_bounds__(kZWarps * 32) zgemv_kernel(const ZBlock* __res
   const TX* x = in + blockIdx.y * ld_in + Z.x_off;
   TX* z = in + blockIdx.y * ld_in + Z.z_off;
   const int lanes = (it.nk + CPL - 1) / CPL;
-  int P = 1;
-  while (P < lanes) P <<= 1;
+  const int P = lanes <= 1 ? 1 : 1 << (32 - __clz(lanes - 1));  // next power of two >= lanes
   const int G = 32 / P, g = lane / P, p = lane % P;
   const bool cact = p < lanes;
   typename AC::A acc[CPL];
 #pragma unroll
   for (int q = 0; q < CPL; q++) acc[q] = AC::zero();
-  if (it.k0 == 0 && it.nk == rp) {
+  if (it.nst > 0) {
     // rows of rowb = rp * sizeof(TA) bytes (16 .. 512, a multiple of 16); V
     // is 16-byte aligned (factor chunks are, and every block's V starts on a
     // 16-byte boundary), so every stage's source and size are too.  The input
     // run is copied from its 16-byte boundary below to the one above; the
-    // input buffers carry 16 bytes of padding at their end for that.
+    // input buffers carry 16 bytes of padding at their end for that.  R and
+    // nst come from z_item_stages: R a multiple of G, at most
+    // kZStageBytes / rowb rows.
     unsigned char* base = zsm + wid * kZWarpSmem;
     uint64_t* bar = reinterpret_cast<uint64_t*>(base);
     unsigned char* vbuf = base + 64;
     unsigned char* xbuf = vbuf + kZStages * kZStageBytes;
     const int rowb = int(rp) * int(sizeof(TA));
-    const int R = (kZStageBytes / rowb) / G * G;  // >= G since 4 P >= lanes
+    const int R = it.R, nst = it.nst;
     const int nrows = it.j1 - it.j0;
-    const int nst = (nrows + R - 1) / R;
     const TA* V = static_cast<const TA*>(Z.V) + int64_t(it.j0) * rp;
     const TX* xr = x + it.j0;
     if (lane == 0) {
@@ -428,22 +481,7 @@ __global__ void __launch_bounds__(kZWarps * 32) zgemv_kernel(const ZBlock* __res
       axpy16<TACC>(v, AC::in(x[j]), acc);
     }
   }
-  for (int o = P; o < 32; o <<= 1)
-#pragma unroll
-    for (int q = 0; q < CPL; q++) acc[q] = AC::add(acc[q], AC::shfl_xor(acc[q], o));
-  if (g == 0 && cact) {
-#pragma unroll
-    for (int q = 0; q < CPL; q++) {
-      const int c = p * CPL + q;
-      // BF16: z columns carry the product of U's and V's column scales
-      if (sizeof(TA) == 2 && Z.zscale && it.k0 + c < Z.r) acc[q] = AC::scale(acc[q], __ldg(Z.zscale + it.k0 + c));
-      if (it.part < 0) {
-        if (it.k0 + c < Z.r) z[it.k0 + c] = to_input<TACC>(acc[q]);
-      } else {
-        zpart[it.part + c] = typename IO<TACC>::TY(AC::value(acc[q]));
-      }
-    }
-  }
+  z_finish<TA, TACC>(acc, P, lane, it, Z, z, zpart);
 }
 
 template <typename TACC>
@@ -494,7 +532,8 @@ template <typename TA, typename TACC>
 __global__ void __launch_bounds__(kSWarps * 32, HODLR_TUNE_S_MINB)
     panel_small_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
                        int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
-                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
+                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots,
+                       typename IO<TACC>::TY* __restrict__ ypart) {
   using TX = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
   using AC = Acc<TACC>;
@@ -617,7 +656,14 @@ __global__ void __launch_bounds__(kSWarps * 32, HODLR_TUNE_S_MINB)
 #undef HODLR_SMALL_ISSUE
   typename AC::A acc = AC::add(a0, a1);
   for (int o = mpad; o < 32; o <<= 1) acc = AC::add(acc, AC::shfl_xor(acc, o));
-  if (sl == 0 && i < m) yo[i] = TY(AC::value(acc));
+  // a panel whose columns are split over several items: partial rows at
+  // ypart[part * tile_rows], added in part order by panel_fix_kernel
+  if (sl == 0 && i < m) {
+    if (it.part < 0)
+      yo[i] = TY(AC::value(acc));
+    else
+      ypart[int64_t(it.part) * tile_rows(int(sizeof(TA))) + i] = TY(AC::value(acc));
+  }
 }
 
 // Phase 2, panels of more than 32 rows: item chunk = row tile t of the
@@ -837,7 +883,8 @@ template <typename TA, typename TACC>
 __global__ void __launch_bounds__(256)
     panel_small_direct_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
                        int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
-                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots) {
+                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots,
+                       typename IO<TACC>::TY* __restrict__ ypart) {
   using TX = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
   const int w = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
@@ -874,7 +921,14 @@ __global__ void __launch_bounds__(256)
   }
   typename AC::A acc = AC::add(a0, a1);
   for (int o = mpad; o < 32; o <<= 1) acc = AC::add(acc, AC::shfl_xor(acc, o));
-  if (sl == 0 && i < m) yo[i] = TY(AC::value(acc));
+  // a panel whose columns are split over several items: partial rows at
+  // ypart[part * tile_rows], added in part order by panel_fix_kernel
+  if (sl == 0 && i < m) {
+    if (it.part < 0)
+      yo[i] = TY(AC::value(acc));
+    else
+      ypart[int64_t(it.part) * tile_rows(int(sizeof(TA))) + i] = TY(AC::value(acc));
+  }
 }
 
 template <typename TA, typename TACC>
@@ -1099,6 +1153,18 @@ unsigned vec_grid(int64_t n) {
 
 }  // namespace
 
+void z_item_stages(ZItem& it, int r, int esz) {
+  const int rp = int(vpad(r, esz));
+  it.R = it.nst = 0;
+  if (it.k0 != 0 || it.nk != rp || it.j1 <= it.j0) return;
+  const int lanes = (it.nk + 16 / esz - 1) / (16 / esz);
+  int P = 1;
+  while (P < lanes) P <<= 1;
+  const int G = 32 / P, rowb = rp * esz;
+  it.R = (kZStageBytes / rowb) / G * G;  // >= G: rowb <= 16 P, kZStageBytes >= 512
+  it.nst = (it.j1 - it.j0 + it.R - 1) / it.R;
+}
+
 template <typename TA, typename TACC>
 static void zgemv_t(const ZBlock* zb, const ZItem* items, int nitems, const ZFix* fix, int nfix, void* zpart, void* in,
                     int64_t ld_in, int nrhs, cudaStream_t st) {
@@ -1163,7 +1229,8 @@ static void panels_staged(const Panel* panels, const Seg* segs, const Item* smal
     cudaFuncSetAttribute(panel_small_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kSWarps * s_warp_smem<TA>());
     panel_small_kernel<TA, TACC><<<g, kSWarps * 32, kSWarps * s_warp_smem<TA>(), st>>>(
-        panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots);
+        panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots,
+        static_cast<TY*>(ypart));
   }
 }
 
@@ -1183,7 +1250,8 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
     if (nsmall > 0) {
       dim3 g(warps_grid(nsmall), unsigned(nrhs));
       panel_small_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TI*>(in),
-                                                             ld_in, static_cast<TY*>(y), ld_y, nslots);
+                                                             ld_in, static_cast<TY*>(y), ld_y, nslots,
+                                                             static_cast<TY*>(ypart));
     }
   } else {
     panels_staged<TA, TACC>(panels, segs, small, nsmall, big, nbig, in, ld_in, ypart, y, ld_y, nslots, nrhs, st);
@@ -1640,7 +1708,7 @@ __device__ __forceinline__ bool mr_next_piece(const Seg* segs, int64_t seg_e, in
 __global__ void __launch_bounds__(kMWarps * 32, 3)
     panel_small_mr_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs,
                           const Item* __restrict__ items, int nitems, const float* __restrict__ in, int64_t ld_in,
-                          float* __restrict__ y, int64_t ld_y) {
+                          float* __restrict__ y, int64_t ld_y, float* __restrict__ ypart, int64_t ypart_ld) {
   extern __shared__ __align__(16) unsigned char msm[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w = blockIdx.x * kMWarps + wid;
@@ -1728,7 +1796,9 @@ __global__ void __launch_bounds__(kMWarps * 32, 3)
     if (more) HODLR_MRS_ISSUE(more);  // into the stage just consumed (the ring is full while more)
   }
 #undef HODLR_MRS_ISSUE
-  float* yo = y + int64_t(blockIdx.y) * ld_y * kMR + P.yoff * kMR;
+  // split panels: partial rows at the part's 128-row block of ypart (panel_fix_mr_kernel)
+  float* yo = it.part < 0 ? y + int64_t(blockIdx.y) * ld_y * kMR + P.yoff * kMR
+                          : ypart + int64_t(blockIdx.y) * ypart_ld * kMR + int64_t(it.part) * 128 * kMR;
 #pragma unroll
   for (int i = 0; i < 32; i++)
     if (i < m) yo[int64_t(i) * kMR + lane] = acc[i];
@@ -1931,7 +2001,7 @@ cudaError_t launch_panels_mr(const Panel* panels, const Seg* segs, const Item* s
     cudaFuncSetAttribute(panel_small_mr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMWarps * kMSWarpSmem);
     dim3 g(unsigned((nsmall + kMWarps - 1) / kMWarps), unsigned(nchunks));
     panel_small_mr_kernel<<<g, kMWarps * 32, kMWarps * kMSWarpSmem, st>>>(panels, segs, small, nsmall, in, ld_in, y,
-                                                                           ld_y);
+                                                                           ld_y, ypart, ypart_ld);
   }
   if (nfix > 0) {
     dim3 gf(unsigned((int64_t(nfix) * 128 * kMR + 255) / 256), unsigned(nchunks));

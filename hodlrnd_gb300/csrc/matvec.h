@@ -109,7 +109,10 @@ struct ZItem {
   int32_t k0, nk;  // (padded) columns k0 .. k0 + nk - 1, at most 32 loads of 16 bytes
   int32_t j0, j1;  // rows j0 .. j1 - 1
   int32_t part;    // < 0: write z; else partial sums at zpart[part + c], c < nk
+  int32_t R, nst;  // items of whole rows (staged): V rows per ring stage, stage count; else 0, 0
 };
+// Sets R and nst of an item of block rank r stored with esz-byte elements.
+void z_item_stages(ZItem& it, int r, int esz);
 constexpr int kZPart = 128;          // partial-sum stride of one item (>= any nk)
 constexpr int kZItemBytes = 1 << 16;  // V bytes one item reads at most (when the block has that many)
 
