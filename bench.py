@@ -633,7 +633,9 @@ def run_c4(args):
     y = torch.empty_like(x)
     reps = max(args.steps, 3)
     engines = (("bf16_factors", 1e-4, "always"), ("fp32_factors", 1e-8, True), ("fp64", 1e-8, True))
-    for dp in (-1, 0):
+    if args.c4_engine != "all":  # one engine alone (a small case for profiling)
+        engines = tuple(e for e in engines if e[0] == args.c4_engine)
+    for dp in ((-1, 0) if args.c4_dprime is None else (args.c4_dprime,)):
         res, ys = {}, {}
         for prec, eps, relax in engines:
             t0 = time.perf_counter()
@@ -651,6 +653,9 @@ def run_c4(args):
                          "max_rank": s["max_rank"], "far_bytes": s["far_bytes"], "near_bytes": s["near_bytes"],
                          "device_bytes": s["device_bytes"]}
             M.close()
+        if args.c4_engine != "all":
+            out["cases"][f"dprime={dp}"] = res
+            continue
         y64 = ys["fp64"]
         for prec in ("bf16_factors", "fp32_factors"):
             res[prec]["rel_diff_vs_fp64_operator"] = float(np.linalg.norm(ys[prec] - y64) / np.linalg.norm(y64))
@@ -673,7 +678,9 @@ def run_c4(args):
                                    res["fp32_factors"]["matvec_ms"] * 64 / ms, 2)}
         B.close()
         out["cases"][f"dprime={dp}"] = res
-    out["value"] = out["cases"]["dprime=0"]["rhs64_matvec"]["rhs_matvecs_per_s"]
+    last = out["cases"][f"dprime={dp}"]
+    out["value"] = (last["rhs64_matvec"]["rhs_matvecs_per_s"] if "rhs64_matvec" in last
+                    else round(1e3 / next(iter(last.values()))["matvec_ms"], 1))
     print(json.dumps(out), flush=True)
 
 
@@ -693,6 +700,9 @@ def main():
     ap.add_argument("--workload", choices=["solve", "serving", "batch", "c4"], default="solve",
                     help="serving: replay the request trace through the request loop (its own JSON line)")
     ap.add_argument("--requests", type=int, default=48)
+    ap.add_argument("--c4-engine", choices=["all", "bf16_factors", "fp32_factors", "fp64"], default="all",
+                    help="c4: time one engine alone (no 64-RHS pass, no comparison)")
+    ap.add_argument("--c4-dprime", type=int, choices=[-1, 0], default=None, help="c4: one d' only")
     ap.add_argument("--pool", type=int, default=12)
     ap.add_argument("--slots", type=int, default=4)
     args = ap.parse_args()

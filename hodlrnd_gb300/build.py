@@ -51,7 +51,8 @@ def build(force=False):
         force = True  # objects from another architecture
     if force:
         for f in os.listdir(OBJ):
-            os.remove(os.path.join(OBJ, f))
+            if os.path.isfile(os.path.join(OBJ, f)):
+                os.remove(os.path.join(OBJ, f))
         if os.path.exists(LIB):
             os.remove(LIB)
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
