@@ -69,40 +69,106 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // Classical Gram-Schmidt, one pass (applied twice per Arnoldi step: CGS2).
+// Its O(n * nv) products run on the FP32 pipe: GB300's FP64 pipe, not HBM,
+// bounded the FP64 versions (84% FP64-pipe busy, 12% of DRAM bandwidth).
+// Each FP64 value is split into two floats from its bits alone (split_d),
+// products are formed as in Dot2 (Ogita, Rump and Oishi, SIAM J. Sci.
+// Comput. 26 (2005)): the product of the high parts exactly by FMA, the cross
+// terms rounded, every addition's error kept.  Dots and updates come out
+// within about 1e-14 of the exact values (FP64 summation of the same terms
+// is within n * 1.1e-16); only O(n) operations stay on the FP64 pipe.
+
+// a = hi + lo + e, |e| <= 2^-46 |a|: hi is a's sign, exponent and leading 24
+// significand bits, lo the next 23 bits (truncated), both exact floats, built
+// with integer operations only.  |a| < 2^-70 gives (0, 0) (its products with
+// the unit-norm basis vectors are below 1e-21); |a| >= 2^127 falls back to a
+// rounding conversion.
+__device__ __forceinline__ float2 split_d(double a) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(a));
+  const unsigned hi32 = unsigned(b >> 32), lo32 = unsigned(b);
+  const int e = int((hi32 >> 20) & 0x7ffu);
+  if (e < 1023 - 70) return make_float2(0.f, 0.f);
+  if (e > 1023 + 126) return make_float2(__double2float_rn(a), 0.f);
+  const unsigned sign = hi32 & 0x80000000u;
+  const unsigned m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+  const float hi = __uint_as_float(sign | (unsigned(e - 1023 + 127) << 23) | m23);
+  // the next 23 bits r as a float (2^23 + r - 2^23, exact), times 2^(e - 1069)
+  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((lo32 & 0x1fffffffu) >> 6)), 8388608.f);
+  const float lo = __fmul_rn(r, __uint_as_float(unsigned(e - 1069 + 127) << 23));
+  return make_float2(hi, __uint_as_float(__float_as_uint(lo) | sign));
+}
+__device__ __forceinline__ float2 split_t(double a) { return split_d(a); }
+__device__ __forceinline__ float2 split_t(float a) { return make_float2(a, 0.f); }
+
+// s + c += (a.x + a.y)(b.x + b.y)
+__device__ __forceinline__ void dot2_add(float& s, float& c, float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  const float pe = __fmaf_rn(a.x, b.x, -p);
+  const float t = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, pe));
+  const float s2 = __fadd_rn(s, p);
+  const float bb = __fsub_rn(s2, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(s2, bb)), __fsub_rn(p, bb));
+  s = s2;
+  c = __fadd_rn(c, __fadd_rn(err, t));
+}
+
+// (s, c) + (s2, c2) as an unevaluated FP32 pair (TwoSum on the high parts).
+__device__ __forceinline__ void pair_add(float& s, float& c, float s2, float c2) {
+  const float t = __fadd_rn(s, s2);
+  const float bb = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(s2, bb));
+  s = t;
+  c = __fadd_rn(__fadd_rn(c, c2), err);
+}
+
 // cgs_dots: part[j * kVecCtas + cta] = this CTA's share of <w, v_j> for
-// j < nv.  Grid kVecCtas x ceil(nv / 8): CTA (cta, g) takes vectors
-// 8g .. 8g + 7, so every group runs at once and each thread keeps eight
-// loads in flight; a partial's summation order depends only on cta.
+// j < nv and cta < kDotCtas.  Grid kDotCtas x ceil(nv / 8): CTA (cta, g)
+// takes vectors 8g .. 8g + 7, so every group runs at once and each thread
+// keeps eight loads in flight over about n / (kDotCtas * 256) elements; the
+// CTA's sums are combined as FP32 pairs (the FP64 pipe would bound a
+// reduction in FP64), and a partial's summation order depends only on cta.
 constexpr int kDotGroup = 8;
+constexpr int kDotCtas = 152;
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     cgs_dots_kernel(const T* __restrict__ w, const T* __restrict__ V, int64_t n, int nv, double* __restrict__ part) {
   constexpr int U = kDotGroup;
-  __shared__ double sh[U][kThreads / 32];
+  __shared__ float shs[U][kThreads / 32], shc[U][kThreads / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int j0 = blockIdx.y * U;
   const int jn = min(U, nv - j0);
-  double acc[U];
+  float as[U], ac[U];
 #pragma unroll
-  for (int u = 0; u < U; u++) acc[u] = 0.0;
-  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads) {
-    const double wi = to_d(w[i]);
+  for (int u = 0; u < U; u++) as[u] = ac[u] = 0.f;
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kDotCtas) * kThreads) {
+    const float2 wi = split_t(w[i]);
 #pragma unroll
     for (int u = 0; u < U; u++)
-      if (u < jn) acc[u] += to_d(V[int64_t(j0 + u) * n + i]) * wi;
+      if (u < jn) dot2_add(as[u], ac[u], split_t(V[int64_t(j0 + u) * n + i]), wi);
   }
 #pragma unroll
   for (int u = 0; u < U; u++) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
-    if (lane == 0) sh[u][wid] = acc[u];
+    for (int o = 16; o > 0; o >>= 1)
+      pair_add(as[u], ac[u], __shfl_xor_sync(0xffffffffu, as[u], o), __shfl_xor_sync(0xffffffffu, ac[u], o));
+    if (lane == 0) {
+      shs[u][wid] = as[u];
+      shc[u][wid] = ac[u];
+    }
   }
   __syncthreads();
   if (threadIdx.x < jn) {
-    double v = 0.0;
-    for (int q = 0; q < kThreads / 32; q++) v += sh[threadIdx.x][q];
-    part[int64_t(j0 + threadIdx.x) * kVecCtas + blockIdx.x] = v;
+    float vs = 0.f, vc = 0.f;
+    for (int q = 0; q < kThreads / 32; q++) pair_add(vs, vc, shs[threadIdx.x][q], shc[threadIdx.x][q]);
+    part[int64_t(j0 + threadIdx.x) * kVecCtas + blockIdx.x] = __dadd_rn(double(vs), double(vc));
   }
+}
+
+// Sum of the first kDotCtas partials in a fixed order (each CTA gets the same value).
+__device__ double reduce_dot_parts(const double* part) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < kDotCtas; i += kThreads) v += part[i];
+  return block_sum(v);
 }
 
 // One CTA per basis vector j: hc[j] = <w, v_j> from the partial sums (fixed
@@ -110,43 +176,72 @@ __global__ void __launch_bounds__(kThreads)
 __global__ void __launch_bounds__(kThreads)
     cgs_reduce_kernel(const double* __restrict__ part, double* __restrict__ hc, double* __restrict__ hcol, int second) {
   const int j = blockIdx.x;
-  const double v = reduce_parts(part + int64_t(j) * kVecCtas);
+  const double v = reduce_dot_parts(part + int64_t(j) * kVecCtas);
   if (threadIdx.x == 0) {
     hc[j] = v;
     hcol[j] = second ? __dadd_rn(hcol[j], v) : v;
   }
 }
 
-// w -= sum_j hc[j] v_j (in FP64, j in order, rounded to T once); with part,
-// also the partial sums of |w|^2 for the normalisation.
+// w -= sum_j hc[j] v_j: the sum of the products as above, then one FP64
+// subtraction, rounded to T once; with part, also the partial sums of |w|^2
+// for the normalisation (as FP32 pairs until one FP64 value per CTA).
+// nv <= kMaxBasis (the restart length + 1).
+constexpr int kMaxBasis = 1001;
 template <typename T>
 __global__ void __launch_bounds__(kThreads) cgs_update_kernel(T* __restrict__ w, const T* __restrict__ V, int64_t n,
                                                               int nv, const double* __restrict__ hc,
                                                               double* __restrict__ part) {
-  double acc = 0.0;
+  __shared__ float2 hs[kMaxBasis];
+  __shared__ float ps[kThreads / 32], pc[kThreads / 32];
+  for (int j = threadIdx.x; j < nv; j += kThreads) hs[j] = split_d(hc[j]);
+  __syncthreads();
+  float ns = 0.f, nc = 0.f;
   for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads) {
-    double wi = to_d(w[i]);
+    float s = 0.f, c = 0.f;
 #pragma unroll 8
-    for (int j = 0; j < nv; j++) wi = axmy(wi, hc[j], to_d(V[int64_t(j) * n + i]));
-    const T t = T(wi);
+    for (int j = 0; j < nv; j++) dot2_add(s, c, split_t(V[int64_t(j) * n + i]), hs[j]);
+    const T t = T(__dsub_rn(to_d(w[i]), __dadd_rn(double(s), double(c))));
     w[i] = t;
-    acc += to_d(t) * to_d(t);
+    const float2 ts = split_t(t);
+    dot2_add(ns, nc, ts, ts);
   }
   if (part) {
-    acc = block_sum(acc);
-    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      pair_add(ns, nc, __shfl_xor_sync(0xffffffffu, ns, o), __shfl_xor_sync(0xffffffffu, nc, o));
+    if (lane == 0) {
+      ps[wid] = ns;
+      pc[wid] = nc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float vs = 0.f, vc = 0.f;
+      for (int q = 0; q < kThreads / 32; q++) pair_add(vs, vc, ps[q], pc[q]);
+      part[blockIdx.x] = __dadd_rn(double(vs), double(vc));
+    }
   }
 }
 
 // h = sqrt(<w, w>) from part; v_next = (1 / h) * w (GMRES.hpp:241-242).
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    normalize_kernel(const T* w, T* vnext, int64_t n, const double* part, double* hout) {
-  const double h = sqrt(reduce_parts(part));
-  if (blockIdx.x == 0 && threadIdx.x == 0) *hout = h;
-  const double ih = 1.0 / h;
+    normalize_kernel(const T* w, T* vnext, int64_t n, const double* ih_ptr) {
+  const double ih = *ih_ptr;
   for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads)
     vnext[i] = T(__dmul_rn(ih, to_d(w[i])));
+}
+
+// h = sqrt(<w, w>) from part into *hout and 1 / h into *ihout, once (one CTA):
+// every CTA of normalize_kernel then multiplies by the same value without
+// summing the partials and dividing itself.
+__global__ void __launch_bounds__(kThreads) norm_recip_kernel(const double* part, double* hout, double* ihout) {
+  const double h = sqrt(reduce_parts(part));
+  if (threadIdx.x == 0) {
+    *hout = h;
+    *ihout = 1.0 / h;
+  }
 }
 
 // v0 = r * (1 / beta) (GMRES.hpp:220); s = beta e_0.
@@ -182,14 +277,26 @@ __device__ __forceinline__ void gen_rot(double dx, double dy, double& cs, double
 }
 
 // Rotations for column i of H and the residual estimate (GMRES.hpp:244-250).
-__global__ void givens_kernel(double* H, int ldh, double* rot, int restart, int i, double* scal) {
+// The running entry stays in a register (H and rot do not alias), so the
+// loads of the next entry and rotation are not held up by the stores.
+__global__ void givens_kernel(double* __restrict__ H, int ldh, double* __restrict__ rot, int restart, int i,
+                              double* __restrict__ scal) {
   double* cs = rot;
   double* sn = rot + (restart + 1);
   double* s = rot + 2 * (restart + 1);
   double* h = H + int64_t(i) * ldh;
-  for (int k = 0; k < i; k++) apply_rot(h[k], h[k + 1], cs[k], sn[k]);
-  gen_rot(h[i], h[i + 1], cs[i], sn[i]);
-  apply_rot(h[i], h[i + 1], cs[i], sn[i]);
+  double hk = h[0];
+  for (int k = 0; k < i; k++) {
+    double hk1 = h[k + 1];
+    apply_rot(hk, hk1, cs[k], sn[k]);
+    h[k] = hk;
+    hk = hk1;
+  }
+  double hi1 = h[i + 1];
+  gen_rot(hk, hi1, cs[i], sn[i]);
+  apply_rot(hk, hi1, cs[i], sn[i]);
+  h[i] = hk;
+  h[i + 1] = hi1;
   apply_rot(s[i], s[i + 1], cs[i], sn[i]);
   scal[0] = fabs(s[i + 1]) / scal[2];
 }
@@ -364,16 +471,16 @@ cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* 
         // CGS2: two classical passes against v_0 .. v_i, |w|^2 from the second
         for (int pass = 0; pass < 2; pass++) {
           count_launches(3);
-          cgs_dots_kernel<T><<<dim3(kVecCtas, unsigned((i + 1 + kDotGroup - 1) / kDotGroup)), kThreads, 0, st>>>(
+          cgs_dots_kernel<T><<<dim3(kDotCtas, unsigned((i + 1 + kDotGroup - 1) / kDotGroup)), kThreads, 0, st>>>(
               W.w, W.V, n, i + 1, W.partk);
           cgs_reduce_kernel<<<i + 1, kThreads, 0, st>>>(W.partk, W.hc, W.H + int64_t(i) * ldh, pass);
           cgs_update_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V, n, i + 1, W.hc, pass == 1 ? part0 : nullptr);
         }
         plast = part0;
       }
-      count_launches(1);
-      normalize_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V + int64_t(i + 1) * n, n, plast,
-                                                          W.H + (i + 1) + int64_t(i) * ldh);
+      count_launches(2);
+      norm_recip_kernel<<<1, kThreads, 0, st>>>(plast, W.H + (i + 1) + int64_t(i) * ldh, W.scal + 4);
+      normalize_kernel<T><<<kVecCtas, kThreads, 0, st>>>(W.w, W.V + int64_t(i + 1) * n, n, W.scal + 4);
       count_launches(1);
       givens_kernel<<<1, 1, 0, st>>>(W.H, ldh, W.rot, W.restart, i, W.scal);
       HODLR_TRY(cudaGetLastError());
