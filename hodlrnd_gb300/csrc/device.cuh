@@ -159,4 +159,24 @@ struct CtaTeam {
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// a = hi + lo + e, |e| <= 2^-46 |a|: hi is a's sign, exponent and leading 24
+// significand bits, lo the next 23 bits (truncated), both exact floats, built
+// with integer operations only (GB300's FP64 pipe is far slower than its
+// FP32 and integer pipes).  |a| < 2^-70 gives (0, 0), an absolute error below
+// 8.5e-22; |a| >= 2^127 falls back to a rounding conversion.
+__device__ __forceinline__ float2 split_d(double a) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(a));
+  const unsigned hi32 = unsigned(b >> 32), lo32 = unsigned(b);
+  const int e = int((hi32 >> 20) & 0x7ffu);
+  if (e < 1023 - 70) return make_float2(0.f, 0.f);
+  if (e > 1023 + 126) return make_float2(__double2float_rn(a), 0.f);
+  const unsigned sign = hi32 & 0x80000000u;
+  const unsigned m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+  const float hi = __uint_as_float(sign | (unsigned(e - 1023 + 127) << 23) | m23);
+  // the next 23 bits r as a float (2^23 + r - 2^23, exact), times 2^(e - 1069)
+  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((lo32 & 0x1fffffffu) >> 6)), 8388608.f);
+  const float lo = __fmul_rn(r, __uint_as_float(unsigned(e - 1069 + 127) << 23));
+  return make_float2(hi, __uint_as_float(__float_as_uint(lo) | sign));
+}
+
 }  // namespace hodlr

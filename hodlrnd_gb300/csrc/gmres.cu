@@ -71,32 +71,14 @@ __global__ void __launch_bounds__(kThreads)
 // Classical Gram-Schmidt, one pass (applied twice per Arnoldi step: CGS2).
 // Its O(n * nv) products run on the FP32 pipe: GB300's FP64 pipe, not HBM,
 // bounded the FP64 versions (84% FP64-pipe busy, 12% of DRAM bandwidth).
-// Each FP64 value is split into two floats from its bits alone (split_d),
+// Each FP64 value is split into two floats from its bits alone (split_d,
+// device.cuh),
 // products are formed as in Dot2 (Ogita, Rump and Oishi, SIAM J. Sci.
 // Comput. 26 (2005)): the product of the high parts exactly by FMA, the cross
 // terms rounded, every addition's error kept.  Dots and updates come out
 // within about 1e-14 of the exact values (FP64 summation of the same terms
 // is within n * 1.1e-16); only O(n) operations stay on the FP64 pipe.
 
-// a = hi + lo + e, |e| <= 2^-46 |a|: hi is a's sign, exponent and leading 24
-// significand bits, lo the next 23 bits (truncated), both exact floats, built
-// with integer operations only.  |a| < 2^-70 gives (0, 0) (its products with
-// the unit-norm basis vectors are below 1e-21); |a| >= 2^127 falls back to a
-// rounding conversion.
-__device__ __forceinline__ float2 split_d(double a) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(a));
-  const unsigned hi32 = unsigned(b >> 32), lo32 = unsigned(b);
-  const int e = int((hi32 >> 20) & 0x7ffu);
-  if (e < 1023 - 70) return make_float2(0.f, 0.f);
-  if (e > 1023 + 126) return make_float2(__double2float_rn(a), 0.f);
-  const unsigned sign = hi32 & 0x80000000u;
-  const unsigned m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
-  const float hi = __uint_as_float(sign | (unsigned(e - 1023 + 127) << 23) | m23);
-  // the next 23 bits r as a float (2^23 + r - 2^23, exact), times 2^(e - 1069)
-  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((lo32 & 0x1fffffffu) >> 6)), 8388608.f);
-  const float lo = __fmul_rn(r, __uint_as_float(unsigned(e - 1069 + 127) << 23));
-  return make_float2(hi, __uint_as_float(__float_as_uint(lo) | sign));
-}
 __device__ __forceinline__ float2 split_t(double a) { return split_d(a); }
 __device__ __forceinline__ float2 split_t(float a) { return make_float2(a, 0.f); }
 
