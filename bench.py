@@ -42,6 +42,23 @@ MATVEC_REPS = 10
 SERVING_MAX_ITER = 400
 
 
+def max_over_ranks(value, world, device="cuda"):
+    """The largest value over the ranks: the job's time is its slowest
+    replica's (one all-reduce of a scalar, after the timed region)."""
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(steps, world, seconds):
+    """Whole-job throughput: every rank's steps over the slowest rank's time."""
+    return steps * world / seconds
+
+
 def workload(n, rank):
     rng = np.random.default_rng(SEED + rank)
     pts = rng.uniform(0.0, 1.0, (n, NDIM))
@@ -258,11 +275,8 @@ def run_gb300(args):
     launches = _lib.lib().hodlr_kernel_launches() - launches0
     trace = M.trace()
     M.trace(False)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = K * world / (total_ms / 1e3)
+    total_ms = max_over_ranks(total_ms, world)
+    value = job_rate(K, world, total_ms / 1e3)
 
     # ---- the other engines on the same right-hand sides
     k2 = max(1, min(args.other_steps, K))
@@ -305,10 +319,7 @@ def run_gb300(args):
     for k in range(K):
         M.solve(hb[k].numpy(), out=hx[k].numpy())
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, world)
 
     # ---- roofline of the dominant kernel (largest share of traced device time)
     dom = max(trace.items(), key=lambda kv: kv[1]["total_ms"]) if trace else None
@@ -348,7 +359,7 @@ def run_gb300(args):
            "trace": {k: {"launches": v["launches"], "ms": round(v["total_ms"], 3),
                          "GBps": round(v["bytes_per_launch"] * v["launches"] / (v["total_ms"] / 1e3) / 1e9, 1)}
                      for k, v in trace.items()},
-           "e2e": {"value": round(K * world / e2e_s, 3), "unit": "solves/s", "h2d_bytes_per_step": 8 * n,
+           "e2e": {"value": round(job_rate(K, world, e2e_s), 3), "unit": "solves/s", "h2d_bytes_per_step": 8 * n,
                    "d2h_bytes_per_step": 8 * n},
            "gpu_launches": int(launches), "clocks": clk}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
