@@ -313,7 +313,7 @@ __device__ __forceinline__ float2 to_input<FH>(float a) {
 #define HODLR_TUNE_S_BYTES 2048
 #endif
 #ifndef HODLR_TUNE_S_MINB
-#define HODLR_TUNE_S_MINB 4  // leaf-panel CTAs per SM the register allocation must allow
+#define HODLR_TUNE_S_MINB 6  // leaf-panel CTAs per SM the register allocation must allow (no spills at 6)
 #endif
 #ifndef HODLR_TUNE_P_MINB
 #define HODLR_TUNE_P_MINB 4
