@@ -57,6 +57,47 @@ __device__ __forceinline__ void load_point(const PointsDev& P, int64_t i, double
   for (int k = 0; k < D; k++) xi[k] = P.x[k * P.ld + i];
 }
 
+// a = hi + lo + e, |e| <= 2^-46 |a|: hi is a's sign, exponent and leading 24
+// significand bits, lo the next 23 bits (truncated), both exact floats, built
+// with integer operations only (GB300's FP64 pipe is far slower than its
+// FP32 and integer pipes).  |a| < 2^-70 gives (0, 0), an absolute error below
+// 8.5e-22; |a| >= 2^127 falls back to a rounding conversion.
+__device__ __forceinline__ float2 split_d(double a) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(a));
+  const unsigned hi32 = unsigned(b >> 32), lo32 = unsigned(b);
+  const int e = int((hi32 >> 20) & 0x7ffu);
+  if (e < 1023 - 70) return make_float2(0.f, 0.f);
+  if (e > 1023 + 126) return make_float2(__double2float_rn(a), 0.f);
+  const unsigned sign = hi32 & 0x80000000u;
+  const unsigned m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
+  const float hi = __uint_as_float(sign | (unsigned(e - 1023 + 127) << 23) | m23);
+  // the next 23 bits r as a float (2^23 + r - 2^23, exact), times 2^(e - 1069)
+  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((lo32 & 0x1fffffffu) >> 6)), 8388608.f);
+  const float lo = __fmul_rn(r, __uint_as_float(unsigned(e - 1069 + 127) << 23));
+  return make_float2(hi, __uint_as_float(__float_as_uint(lo) | sign));
+}
+
+// s + c += (a.x + a.y)(b.x + b.y)
+__device__ __forceinline__ void dot2_add(float& s, float& c, float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  const float pe = __fmaf_rn(a.x, b.x, -p);
+  const float t = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, pe));
+  const float s2 = __fadd_rn(s, p);
+  const float bb = __fsub_rn(s2, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(s2, bb)), __fsub_rn(p, bb));
+  s = s2;
+  c = __fadd_rn(c, __fadd_rn(err, t));
+}
+
+// (s, c) + (s2, c2) as an unevaluated FP32 pair (TwoSum on the high parts).
+__device__ __forceinline__ void pair_add(float& s, float& c, float s2, float c2) {
+  const float t = __fadd_rn(s, s2);
+  const float bb = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(s2, bb));
+  s = t;
+  c = __fadd_rn(__fadd_rn(c, c2), err);
+}
+
 // ---------------------------------------------------------------- teams
 // A "team" is the group of threads that compresses one block: a warp, or a
 // whole CTA.  All members call every team function (uniform control flow).
@@ -158,25 +199,5 @@ struct CtaTeam {
 };
 
 __host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
-
-// a = hi + lo + e, |e| <= 2^-46 |a|: hi is a's sign, exponent and leading 24
-// significand bits, lo the next 23 bits (truncated), both exact floats, built
-// with integer operations only (GB300's FP64 pipe is far slower than its
-// FP32 and integer pipes).  |a| < 2^-70 gives (0, 0), an absolute error below
-// 8.5e-22; |a| >= 2^127 falls back to a rounding conversion.
-__device__ __forceinline__ float2 split_d(double a) {
-  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(a));
-  const unsigned hi32 = unsigned(b >> 32), lo32 = unsigned(b);
-  const int e = int((hi32 >> 20) & 0x7ffu);
-  if (e < 1023 - 70) return make_float2(0.f, 0.f);
-  if (e > 1023 + 126) return make_float2(__double2float_rn(a), 0.f);
-  const unsigned sign = hi32 & 0x80000000u;
-  const unsigned m23 = ((hi32 & 0xfffffu) << 3) | (lo32 >> 29);
-  const float hi = __uint_as_float(sign | (unsigned(e - 1023 + 127) << 23) | m23);
-  // the next 23 bits r as a float (2^23 + r - 2^23, exact), times 2^(e - 1069)
-  const float r = __fsub_rn(__uint_as_float(0x4B000000u | ((lo32 & 0x1fffffffu) >> 6)), 8388608.f);
-  const float lo = __fmul_rn(r, __uint_as_float(unsigned(e - 1069 + 127) << 23));
-  return make_float2(hi, __uint_as_float(__float_as_uint(lo) | sign));
-}
 
 }  // namespace hodlr

@@ -82,27 +82,6 @@ __global__ void __launch_bounds__(kThreads)
 __device__ __forceinline__ float2 split_t(double a) { return split_d(a); }
 __device__ __forceinline__ float2 split_t(float a) { return make_float2(a, 0.f); }
 
-// s + c += (a.x + a.y)(b.x + b.y)
-__device__ __forceinline__ void dot2_add(float& s, float& c, float2 a, float2 b) {
-  const float p = __fmul_rn(a.x, b.x);
-  const float pe = __fmaf_rn(a.x, b.x, -p);
-  const float t = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, pe));
-  const float s2 = __fadd_rn(s, p);
-  const float bb = __fsub_rn(s2, s);
-  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(s2, bb)), __fsub_rn(p, bb));
-  s = s2;
-  c = __fadd_rn(c, __fadd_rn(err, t));
-}
-
-// (s, c) + (s2, c2) as an unevaluated FP32 pair (TwoSum on the high parts).
-__device__ __forceinline__ void pair_add(float& s, float& c, float s2, float c2) {
-  const float t = __fadd_rn(s, s2);
-  const float bb = __fsub_rn(t, s);
-  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bb)), __fsub_rn(s2, bb));
-  s = t;
-  c = __fadd_rn(__fadd_rn(c, c2), err);
-}
-
 // cgs_dots: part[j * kVecCtas + cta] = this CTA's share of <w, v_j> for
 // j < nv and cta < kDotCtas.  Grid kDotCtas x ceil(nv / 8): CTA (cta, g)
 // takes vectors 8g .. 8g + 7, so every group runs at once and each thread
