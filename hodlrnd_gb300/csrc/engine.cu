@@ -318,7 +318,11 @@ NearTiles near_tiles(const Tree& t, const NearList& nl, int esz) {
 // far panels above 32 rows are many (one per node and level), near ones are
 // few (leaves above 32 points) and get more, smaller items.
 constexpr int kPanelCols = 256;
-constexpr int64_t kSmallItemBytes = 48 * 1024;  // factor bytes per leaf-panel item, about
+// factor bytes per leaf-panel item, about (HODLR_TUNE_SMALL_ITEM_BYTES overrides it for tuning runs)
+#ifndef HODLR_TUNE_SMALL_ITEM_BYTES
+#define HODLR_TUNE_SMALL_ITEM_BYTES (48 * 1024)
+#endif
+constexpr int64_t kSmallItemBytes = HODLR_TUNE_SMALL_ITEM_BYTES;
 constexpr int kNearPanelCols = 48;
 
 // Runs of consecutive segments [begin, end) with about `max_cols` columns each.

@@ -114,7 +114,12 @@ struct ZItem {
 // Sets R and nst of an item of block rank r stored with esz-byte elements.
 void z_item_stages(ZItem& it, int r, int esz);
 constexpr int kZPart = 128;          // partial-sum stride of one item (>= any nk)
-constexpr int kZItemBytes = 1 << 16;  // V bytes one item reads at most (when the block has that many)
+// V bytes one item reads at most (when the block has that many); HODLR_TUNE_Z_ITEM_BYTES
+// overrides it for tuning runs
+#ifndef HODLR_TUNE_Z_ITEM_BYTES
+#define HODLR_TUNE_Z_ITEM_BYTES (1 << 17)
+#endif
+constexpr int kZItemBytes = HODLR_TUNE_Z_ITEM_BYTES;
 
 // z[zpos] = sum_{q < count} zpart[part + q * kZPart]
 struct ZFix {

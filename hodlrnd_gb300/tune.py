@@ -5,9 +5,11 @@
 The staged kernels of csrc/matvec.cu take their ring shapes (stages per warp
 and bytes per stage of V^T x, node-panel and leaf-panel rings, and the
 leaf/node-panel CTAs per SM the register allocation must allow) from
-HODLR_TUNE_* macros.  For each variant -- a JSON object of macro overrides,
-e.g. {"P_STAGES": 3, "P_BYTES": 2048} -- this builds matvec.cu with those
-values into a variant library, links it with the other
+HODLR_TUNE_* macros, and the plan's item sizes (Z_ITEM_BYTES: V bytes per
+V^T x item; SMALL_ITEM_BYTES: factor bytes per leaf-panel item) too.  For
+each variant -- a JSON object of macro overrides, e.g. {"P_STAGES": 3,
+"P_BYTES": 2048} -- this builds matvec.cu and engine.cu with those values
+into a variant library, links them with the other
 objects of the in-place build (variant files go to hodlrnd_gb300/_tune/,
 git-ignored), and times a headline-engine operator with it
 in a child process (HODLRND_LIBRARY selects the library): the build, one
@@ -36,20 +38,28 @@ DEFAULT_VARIANTS = {
 }
 
 
+# plan-level knobs (item sizes) live in the plan code too, so variants rebuild
+# both translation units
+TUNED_SOURCES = ("matvec.cu", "engine.cu")
+
+
 def _variant_lib(name, overrides):
     tdir = os.path.join(B.HERE, "_tune")
     os.makedirs(tdir, exist_ok=True)
     tag = "".join(c if c.isalnum() else "_" for c in name)
-    obj = os.path.join(tdir, f"matvec_{tag}.o")
     lib = os.path.join(tdir, f"lib_{tag}.so")
     defs = [f"-DHODLR_TUNE_{k}={int(v)}" for k, v in overrides.items()]
-    cmd = [B.nvcc(), "-c", os.path.join(B.CSRC, "matvec.cu"), "-o", obj, "-std=c++17", "-O3", "-lineinfo",
-           "-Xcompiler", B.HOST_FLAGS] + B.ARCH + ["-Xptxas", "-O3"] + defs
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"variant {name}: nvcc failed\n{r.stderr[-2000:]}")
-    objs = [os.path.join(B.OBJ, os.path.splitext(s)[0] + ".o") for s in B.SOURCES if s != "matvec.cu"]
-    r = subprocess.run([B.nvcc(), "-shared", "-o", lib, obj] + objs + B.ARCH + ["-Xcompiler", "-fopenmp", "-lgomp"],
+    tuned = []
+    for src in TUNED_SOURCES:
+        obj = os.path.join(tdir, f"{os.path.splitext(src)[0]}_{tag}.o")
+        cmd = [B.nvcc(), "-c", os.path.join(B.CSRC, src), "-o", obj, "-std=c++17", "-O3", "-lineinfo",
+               "-Xcompiler", B.HOST_FLAGS] + B.ARCH + ["-Xptxas", "-O3"] + defs
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"variant {name}: nvcc failed for {src}\n{r.stderr[-2000:]}")
+        tuned.append(obj)
+    objs = [os.path.join(B.OBJ, os.path.splitext(s)[0] + ".o") for s in B.SOURCES if s not in TUNED_SOURCES]
+    r = subprocess.run([B.nvcc(), "-shared", "-o", lib] + tuned + objs + B.ARCH + ["-Xcompiler", "-fopenmp", "-lgomp"],
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"variant {name}: link failed\n{r.stderr[-2000:]}")
