@@ -57,7 +57,8 @@ class HodlrParams(ctypes.Structure):
                 ("max_iter", ctypes.c_int64), ("precision", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("device_budget_bytes", ctypes.c_uint64), ("rank_cap", ctypes.c_int32),
                 ("max_outer", ctypes.c_int32), ("inner_tol", ctypes.c_double), ("ortho", ctypes.c_int32),
-                ("relax", ctypes.c_int32), ("relax_below", ctypes.c_double)]
+                ("relax", ctypes.c_int32), ("relax_below", ctypes.c_double),
+                ("stored_margin", ctypes.c_double)]
 
 
 class HodlrKernelDesc(ctypes.Structure):
@@ -68,7 +69,7 @@ class HodlrKernelDesc(ctypes.Structure):
 class HodlrSolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int64), ("outer_iterations", ctypes.c_int64),
                 ("rel_residual", ctypes.c_double), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("seconds", ctypes.c_double)]
+                ("seconds", ctypes.c_double), ("stop_tol", ctypes.c_double)]
 
 
 class HodlrStats(ctypes.Structure):

@@ -960,9 +960,20 @@ Ortho ortho_of(const hodlr_params& p) {
 }
 
 // Solve in tree order on device buffers b, x (one right-hand side).
+// The stored-operator residual a solve stops at, as a fraction of tol: FP32
+// factors differ from the FP64 operator by their rounding (about 5e-9 relative
+// at eps_aca 1e-8, measured at N = 262144), so their solves stop at half of
+// tol to keep the residual against the FP64 operator below tol too.
+double stored_margin(const hodlr_params& p) {
+  if (p.stored_margin > 0) return p.stored_margin;
+  return (p.precision == HODLR_PREC_FP32_FACTORS || p.precision == HODLR_PREC_MIXED) ? 0.5 : 1.0;
+}
+
 void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr_solve_info* info) {
   const hodlr_params& p = op->p;
-  const double tol = p.tol > 0 ? p.tol : p.eps_aca;
+  const double tol_req = p.tol > 0 ? p.tol : p.eps_aca;
+  const double tol = tol_req * stored_margin(p);
+  info->stop_tol = tol;
   const int64_t max_iter = p.max_iter > 0 ? p.max_iter : op->n;
   const int restart = p.restart > 0 ? p.restart : 100;
   const double t0 = now_s();
@@ -983,7 +994,7 @@ void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr
     // from x with compensated products while it is above tol.
     const bool relax = (p.precision == HODLR_PREC_FP32_FACTORS || p.precision == HODLR_PREC_BF16_FACTORS) &&
                        p.relax != HODLR_RELAX_OFF;
-    const double relax_at = p.relax_below > 0 ? p.relax_below : std::min(1.0, tol * kRelaxFactor);
+    const double relax_at = p.relax_below > 0 ? p.relax_below : std::min(1.0, tol_req * kRelaxFactor);
     std::function<void(double)> progress;
     if (relax) progress = [op, relax_at](double res) { op->relaxed = res < relax_at; };
     op->relaxed = false;
@@ -1508,6 +1519,25 @@ void batch_apply_mr(hodlr_batch& b, const float* x, float* y, int64_t nrhs, cuda
   CK(launch_batch_combine_mr(b.d_inst, count, b.max_n, b.d_y_mr, b.ycol, y, b.total_n, int(nrhs), nch, st));
 }
 
+// Why the parameters cannot be used (null when they can): the checks of
+// hodlr_ctx_create, applied again to the parameters read from an operator file.
+const char* params_problem(const hodlr_params& p) {
+  if (p.ndim < 1 || p.ndim > kMaxDim) return "ndim must be in 1..8";
+  if (p.nmax < 1) return "nmax must be positive";
+  if (p.dprime < -1 || p.dprime > p.ndim - 1) return "dprime must be in -1..ndim-1";
+  if (!(p.eps_aca > 0.0) || !(p.eps_aca < 1.0))
+    return "eps_aca must be in (0, 1) (values >= 1 select a fixed rank in the reference, which this engine does "
+           "not support)";
+  if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED && p.precision != HODLR_PREC_FP32_FACTORS &&
+      p.precision != HODLR_PREC_BF16_FACTORS)
+    return "unknown precision";
+  if (p.restart < 0 || p.restart > 1000) return "restart must be in 0..1000";
+  if (p.ortho < HODLR_ORTHO_AUTO || p.ortho > HODLR_ORTHO_CGS2) return "unknown orthogonalisation";
+  if (p.relax != HODLR_RELAX_AUTO && p.relax != HODLR_RELAX_OFF && p.relax != HODLR_RELAX_ALWAYS)
+    return "relax must be HODLR_RELAX_AUTO, _OFF or _ALWAYS";
+  return nullptr;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1535,20 +1565,8 @@ int hodlr_ctx_create(const hodlr_params* params, hodlr_ctx** out) {
   if (!params || !out) return fail(nullptr, HODLR_ERR_INVALID, "hodlr_ctx_create: null argument");
   *out = nullptr;
   const hodlr_params& p = *params;
-  if (p.ndim < 1 || p.ndim > kMaxDim) return fail(nullptr, HODLR_ERR_INVALID, "ndim must be in 1..8");
-  if (p.nmax < 1) return fail(nullptr, HODLR_ERR_INVALID, "nmax must be positive");
-  if (p.dprime < -1 || p.dprime > p.ndim - 1) return fail(nullptr, HODLR_ERR_INVALID, "dprime must be in -1..ndim-1");
-  if (!(p.eps_aca > 0.0) || !(p.eps_aca < 1.0))
-    return fail(nullptr, HODLR_ERR_INVALID, "eps_aca must be in (0, 1) (values >= 1 select a fixed rank in the "
-                                            "reference, which this engine does not support)");
-  if (p.precision != HODLR_PREC_FP64 && p.precision != HODLR_PREC_MIXED && p.precision != HODLR_PREC_FP32_FACTORS &&
-      p.precision != HODLR_PREC_BF16_FACTORS)
-    return fail(nullptr, HODLR_ERR_INVALID, "unknown precision");
-  if (p.restart < 0 || p.restart > 1000) return fail(nullptr, HODLR_ERR_INVALID, "restart must be in 0..1000");
-  if (p.ortho < HODLR_ORTHO_AUTO || p.ortho > HODLR_ORTHO_CGS2)
-    return fail(nullptr, HODLR_ERR_INVALID, "unknown orthogonalisation");
-  if (p.relax != HODLR_RELAX_AUTO && p.relax != HODLR_RELAX_OFF && p.relax != HODLR_RELAX_ALWAYS)
-    return fail(nullptr, HODLR_ERR_INVALID, "relax must be HODLR_RELAX_AUTO, _OFF or _ALWAYS");
+  const char* why = params_problem(p);
+  if (why) return fail(nullptr, HODLR_ERR_INVALID, why);
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev == 0)
@@ -1693,6 +1711,7 @@ int hodlr_solve_device(hodlr_op* op, const double* d_b, double* d_x, int64_t nrh
     check_stream_waits(op, st);
     info->rel_residual = worst;
     info->converged = all_conv ? 1 : 0;
+    info->stop_tol = one.stop_tol;
     return all_conv ? HODLR_OK : fail(op->ctx, HODLR_ERR_NOT_CONVERGED, "GMRES did not reach the tolerance");
   });
 }
@@ -2070,7 +2089,7 @@ int hodlr_batch_destroy(hodlr_batch* b) {
 // takes the far field from the file instead of running ACA.
 namespace {
 constexpr char kOpMagic[8] = {'H', 'O', 'D', 'L', 'R', 'G', 'B', 0};
-constexpr uint32_t kOpVersion = 1;
+constexpr uint32_t kOpVersion = 2;  // 2: hodlr_params with stored_margin
 
 struct OpFile {
   std::FILE* f = nullptr;
@@ -2155,8 +2174,11 @@ int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out) {
     op->p.device = ctx->p.device;
     op->mem.budget = ctx->p.device_budget_bytes;
     const int d = op->p.ndim;
-    if (d < 1 || d > kMaxDim || op->n < 1 || op->n > (int64_t(1) << 31) - 1)
-      throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: corrupt header: ") + path};
+    const char* why = params_problem(op->p);
+    if (why || op->n < 1 || op->n > (int64_t(1) << 31) - 1 || op->kd.kind < HODLR_KERNEL_INV_R ||
+        op->kd.kind > HODLR_KERNEL_EXP_NEG_R || !std::isfinite(op->kd.scale) || !std::isfinite(op->kd.diag))
+      throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: corrupt header (") +
+                                      (why ? why : "point count or kernel out of range") + "): " + path};
     std::memset(&op->st, 0, sizeof(op->st));
     std::vector<double> pts(size_t(op->n) * size_t(d)), lo(static_cast<size_t>(d)), hi(static_cast<size_t>(d));
     get(pts.data(), sizeof(double) * pts.size());

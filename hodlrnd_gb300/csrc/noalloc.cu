@@ -54,27 +54,52 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(Scratch)
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_addr[kMaxDevices] = {};
+void* g_ctx[kMaxDevices] = {};  // the context the address belongs to
 
 int fail(int code, const std::string& msg) {
   hodlr::set_thread_error(msg);
   return code;
 }
 
-// Device address of the scratch array on the current device; looked up once
-// per device (the first call on a device, which must not happen inside a
-// stream capture).
+// The current context of the calling thread (driver cuCtxGetCurrent, reached
+// through the runtime so that the library needs no link to libcuda); null
+// when it cannot be queried.
+void* current_context() {
+  using GetCtx = int (*)(void**);
+  static GetCtx fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<GetCtx>(f);
+  }();
+  void* c = nullptr;
+  if (!fn || fn(&c) != 0) return nullptr;
+  return c;
+}
+
+// Device address of the scratch array on the current device.  It is looked
+// up (cudaGetSymbolAddress) by the first call on a device and again whenever
+// the device's context has changed since (after cudaDeviceReset the module is
+// loaded anew, possibly elsewhere); a lookup must not happen inside a stream
+// capture.
 int scratch_address(Scratch** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return fail(HODLR_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return fail(HODLR_ERR_INVALID, "device ordinal beyond the supported range");
+  // null before the runtime has made the device's context current: the
+  // lookup below does that, and the context is read again after it
+  void* ctx = current_context();
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  if (!g_addr[dev] || !ctx || ctx != g_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
       return fail(HODLR_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     g_addr[dev] = p;
+    g_ctx[dev] = current_context();
   }
   *out = static_cast<Scratch*>(g_addr[dev]);
   return HODLR_OK;

@@ -75,7 +75,8 @@ def _bind():
 
 
 def make_params(ndim, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0, precision="fp64", restart=100, tol=None,
-                max_iter=0, inner_tol=0.0, max_outer=0, ortho="auto", relax=True, relax_below=0.0):
+                max_iter=0, inner_tol=0.0, max_outer=0, ortho="auto", relax=True, relax_below=0.0,
+                stored_margin=0.0):
     L = _lib.lib()
     p = _lib.HodlrParams()
     L.hodlr_params_default(ctypes.byref(p))
@@ -94,6 +95,7 @@ def make_params(ndim, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0, precis
     p.ortho = {"auto": _lib.HODLR_ORTHO_AUTO, "mgs": _lib.HODLR_ORTHO_MGS, "cgs2": _lib.HODLR_ORTHO_CGS2}[ortho]
     p.relax = _lib.relax_code(relax)
     p.relax_below = float(relax_below)
+    p.stored_margin = float(stored_margin)
     return p
 
 

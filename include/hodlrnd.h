@@ -39,7 +39,10 @@ extern "C" {
 #define HODLR_ERR_NOT_CONVERGED 5 /* GMRES stopped at max_iter (result still written) */
 #define HODLR_ERR_TREE 6          /* tree would exceed the node limit (degenerate input) */
 #define HODLR_ERR_STATE 7         /* call out of order (e.g. matvec before build) */
-#define HODLR_ERR_DEVICE 8        /* a device-side check failed (index or size out of range) */
+#define HODLR_ERR_DEVICE 8        /* a device-side check failed (index or size out of range), or a
+                                     streaming kernel gave up waiting (2 s) for its bulk copies.  The
+                                     give-up count is kept per device: after one, the next matvec or
+                                     solve of every operator on that device reports this code once */
 #define HODLR_ERR_IO 9            /* a file could not be read or written, or is malformed */
 #define HODLR_ERR_TIMEOUT 10      /* hodlr_server_wait: the request has not finished within the timeout */
 
@@ -90,6 +93,12 @@ typedef struct hodlr_params {
   int32_t relax;     /* FP32_FACTORS, BF16_FACTORS: HODLR_RELAX_AUTO, _OFF or _ALWAYS */
   double relax_below; /* FP32_FACTORS, BF16_FACTORS: relative residual estimate below which products
                          are relaxed (<= 0: the default, tol * 1e5) */
+  double stored_margin; /* the solve ends when the true residual with the stored operator is at most
+                           tol * stored_margin (<= 0: the default, 0.5 for FP32_FACTORS and MIXED, 1 for
+                           FP64 and BF16_FACTORS).  FP32-stored factors differ from the FP64 operator by
+                           their rounding (about 5e-9 relative at eps_aca 1e-8); the margin keeps the
+                           residual against the FP64 operator at most tol as well.  BF16's rounding
+                           (about 1e-3) is beyond any margin.  No counterpart in the reference. */
 } hodlr_params;
 
 /* FP32_FACTORS and BF16_FACTORS solves: once GMRES's residual estimate is
@@ -163,9 +172,10 @@ typedef struct hodlr_solve_info {
   int64_t iterations;       /* total inner GMRES iterations (the reference's return value, GMRES.hpp:267,294,302) */
   int64_t outer_iterations; /* iterative-refinement sweeps (1 for FP64) */
   double rel_residual;      /* |b - A x| / |b| with A the stored operator, FP64 */
-  int32_t converged;
+  int32_t converged;         /* rel_residual <= stop_tol */
   int32_t reserved;
   double seconds;
+  double stop_tol;          /* the stored-operator residual the solve stopped at: tol * stored_margin */
 } hodlr_solve_info;
 
 /* Solve A x = b (HODLRdD_matrix::solve, include/HDD_matrix.hpp:51-62 ->
@@ -272,11 +282,14 @@ uint64_t hodlr_kernel_launches(void);
  *            (rank reached min(m,n) - 1; the factors are then not a
  *            representation), bit 1 = cap columns were not enough.
  * m and n above HODLR_NOALLOC_MAX_POINTS, or cap above HODLR_NOALLOC_MAX_RANK,
- * are rejected with HODLR_ERR_INVALID.  The first call on a device looks the
- * static array up (cudaGetSymbolAddress) and must come before any stream
- * capture on that device.  All calls share the array: calls whose GPU work
- * overlaps (other streams or threads) race and must be serialised.  Blocks
- * until the result is known (synchronises `stream`). */
+ * are rejected with HODLR_ERR_INVALID.  Every index in d_rows and d_cols must
+ * be below ld (they address d_points; the device does not check them).  The
+ * first call on a device (and the first after that device's context was
+ * reset) looks the static array up with cudaGetSymbolAddress; that call should
+ * come before any stream capture on the device.  All calls share the array:
+ * calls whose GPU work overlaps (other streams or threads) race and must be
+ * serialised.  Every call waits for its result: it synchronises `stream` and
+ * copies the rank and flags back to the host. */
 #define HODLR_NOALLOC_MAX_POINTS 16384
 #define HODLR_NOALLOC_MAX_RANK 512
 int hodlr_aca_block_noalloc(const double* d_points, int64_t ld, int32_t ndim, const int32_t* d_rows, int32_t m,
