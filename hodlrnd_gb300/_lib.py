@@ -37,6 +37,9 @@ HODLR_ORTHO_AUTO = 0
 HODLR_ORTHO_MGS = 1
 HODLR_ORTHO_CGS2 = 2
 
+HODLR_FP64_CHECK_AUTO = 0
+HODLR_FP64_CHECK_OFF = 1
+
 HODLR_RELAX_AUTO = 0
 HODLR_RELAX_OFF = 1
 HODLR_RELAX_ALWAYS = 2
@@ -58,6 +61,7 @@ class HodlrParams(ctypes.Structure):
                 ("device_budget_bytes", ctypes.c_uint64), ("rank_cap", ctypes.c_int32),
                 ("max_outer", ctypes.c_int32), ("inner_tol", ctypes.c_double), ("ortho", ctypes.c_int32),
                 ("relax", ctypes.c_int32), ("relax_below", ctypes.c_double),
+                ("fp64_check", ctypes.c_int32), ("aca_workspace_mib", ctypes.c_int32),
                 ("stored_margin", ctypes.c_double)]
 
 
@@ -69,7 +73,8 @@ class HodlrKernelDesc(ctypes.Structure):
 class HodlrSolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int64), ("outer_iterations", ctypes.c_int64),
                 ("rel_residual", ctypes.c_double), ("converged", ctypes.c_int32), ("reserved", ctypes.c_int32),
-                ("seconds", ctypes.c_double), ("stop_tol", ctypes.c_double)]
+                ("seconds", ctypes.c_double), ("stop_tol", ctypes.c_double),
+                ("rel_residual_stored", ctypes.c_double)]
 
 
 class HodlrStats(ctypes.Structure):
@@ -86,9 +91,11 @@ class HodlrStats(ctypes.Structure):
 
 TRACE_KINDS = 16
 # kinds 0-3: launches with FP64 vectors (FP64 factors, or FP32 factors with
-# compensated accumulation); 4-7: FP32 vectors (inner solve of iterative refinement)
+# compensated accumulation); 4-7: FP32 vectors (inner solve of iterative refinement);
+# 8-11: the FP64 operator of a reduced-precision operator's refinement residuals
 TRACE_NAMES = {0: "zgemv_x64", 1: "near_x64", 2: "far_x64", 3: "combine_x64", 4: "zgemv_x32", 5: "near_x32",
-               6: "far_x32", 7: "combine_x32"}
+               6: "far_x32", 7: "combine_x32", 8: "zgemv_ref64", 9: "near_ref64", 10: "far_ref64",
+               11: "combine_ref64"}
 
 
 class HodlrTrace(ctypes.Structure):

@@ -54,7 +54,15 @@ __device__ __forceinline__ int rng_next(uint64_t& s) {
   return int(z >> 33);
 }
 
-template <int D, class Team>
+// Shared memory of one staged team (blocks of at most T rows and columns):
+// U (T x T), V (T x T), the target and source coordinates (D x T each), then
+// the target and source tree positions, the used-row and used-column lists
+// and the two bitmaps.
+__host__ __device__ constexpr int staged_team_bytes(int T, int D) {
+  return (2 * T * T + 2 * D * T) * 8 + (2 * T + 2 * (T + 2) + 2) * 4;
+}
+
+template <int D, class Team, bool S = false>
 struct AcaTeam {
   const AcaArgs& a;
   const AcaBlockDesc& B;
@@ -64,8 +72,12 @@ struct AcaTeam {
   uint32_t *rb, *cb;
   int32_t *rl, *cl;
   KernelDev K;
+  // staged teams: coordinates (target, source; SoA with strides m, n) and tree positions
+  double *xt = nullptr, *xs = nullptr;
+  int32_t *it = nullptr, *is = nullptr;
 
-  __device__ AcaTeam(const AcaArgs& a_, const AcaBlockDesc& B_, Team tm_) : a(a_), B(B_), tm(tm_) {
+  __device__ AcaTeam(const AcaArgs& a_, const AcaBlockDesc& B_, Team tm_, unsigned char* sm = nullptr)
+      : a(a_), B(B_), tm(tm_) {
     K = a.K;
     if (B.kscale != 0.0) K.scale = B.kscale;
     m = B.m;
@@ -73,12 +85,85 @@ struct AcaTeam {
     cap = B.cap;
     nwr = int((m + 31) >> 5);
     nwc = int((n + 31) >> 5);
-    U = a.ws + B.ws;
-    V = U + int64_t(m) * cap;
-    rb = a.bits + B.bits;
-    cb = rb + nwr;
-    rl = a.lists + B.lists;
-    cl = rl + cap + 2;
+    if constexpr (S) {
+      // cap <= min(m, n) <= T: every piece fits the team's share (staged_team_bytes)
+      constexpr int T = Team::kSize;
+      double* d = reinterpret_cast<double*>(sm);
+      U = d;
+      V = U + T * T;
+      xt = V + T * T;
+      xs = xt + D * T;
+      it = reinterpret_cast<int32_t*>(xs + D * T);
+      is = it + T;
+      rl = is + T;
+      cl = rl + T + 2;
+      rb = reinterpret_cast<uint32_t*>(cl + T + 2);
+      cb = rb + 1;
+    } else {
+      U = a.ws + B.ws;
+      V = U + int64_t(m) * cap;
+      rb = a.bits + B.bits;
+      cb = rb + nwr;
+      rl = a.lists + B.lists;
+      cl = rl + cap + 2;
+    }
+  }
+
+  // staged teams: the block's points (tree positions and coordinates) into shared memory
+  __device__ void stage_points() {
+    for (int i = tm.tid(); i < m; i += Team::kSize) {
+      const int32_t p = a.lmap[B.t_map + i];
+      it[i] = p;
+#pragma unroll
+      for (int k = 0; k < D; k++) xt[k * m + i] = a.P.x[k * a.P.ld + p];
+    }
+    for (int j = tm.tid(); j < n; j += Team::kSize) {
+      const int32_t p = a.lmap[B.s_map + j];
+      is[j] = p;
+#pragma unroll
+      for (int k = 0; k < D; k++) xs[k * n + j] = a.P.x[k * a.P.ld + p];
+    }
+    tm.sync();
+  }
+
+  // A larger workspace from the growth arena: 4 x the columns (at most
+  // min(m, n)), the r columns computed so far copied over.  False when there
+  // is no arena or it is full.
+  __device__ bool grow(int r, AcaOut* out) {
+    if (S || !a.arena_used) return false;
+    const int ncap = min(min(m, n), cap * 4);
+    if (ncap <= cap) return false;
+    const uint64_t need = uint64_t(ncap) * uint64_t(m + n);
+    double got = -1.0;  // arena offset (doubles; exact below 2^53), or -1
+    if (tm.tid() == 0) {
+      const unsigned long long off = atomicAdd(a.arena_used, (unsigned long long)need);
+      if (off + need <= a.arena_size) got = double(off);
+    }
+    got = tm.bcast(got);
+    if (got < 0.0) return false;
+    const int64_t ws = a.arena_off + int64_t(got);
+    double* nu = a.ws + ws;
+    double* nv = nu + int64_t(m) * ncap;
+    for (int64_t e = tm.tid(); e < int64_t(m) * r; e += Team::kSize) nu[e] = U[e];
+    for (int64_t e = tm.tid(); e < int64_t(n) * r; e += Team::kSize) nv[e] = V[e];
+    tm.sync();
+    U = nu;
+    V = nv;
+    cap = ncap;
+    if (tm.tid() == 0) {
+      out->cap = ncap;
+      out->ws = ws;
+    }
+    return true;
+  }
+
+  // staged teams: U and V of a low-rank result to the block's workspace
+  // (the layout the compaction reads: U m x cap, then V n x cap, column major)
+  __device__ void write_factors(int r) {
+    double* gu = a.ws + B.ws;
+    double* gv = gu + int64_t(m) * cap;
+    for (int e = tm.tid(); e < m * r; e += Team::kSize) gu[e] = U[e];
+    for (int e = tm.tid(); e < n * r; e += Team::kSize) gv[e] = V[e];
   }
 
   __device__ void init_bits(uint32_t* bits, int nw, int size) {
@@ -165,12 +250,23 @@ struct AcaTeam {
   // Residual row i0 into V[:, r]; argmax over the remaining columns.
   __device__ void gen_row(int i0, int r, int nc, double& mx, int& piv, double& sq) {
     double xi[D];
-    const int64_t pi = a.lmap[B.t_map + i0];
-    load_point<D>(a.P, pi, xi);
+    int64_t pi;
+    if constexpr (S) {
+      pi = it[i0];
+#pragma unroll
+      for (int k = 0; k < D; k++) xi[k] = xt[k * m + i0];
+    } else {
+      pi = a.lmap[B.t_map + i0];
+      load_point<D>(a.P, pi, xi);
+    }
     double ba = -1.0, bv = 0.0, v0 = 0.0, s = 0.0;
     int bi = 0x7fffffff;
     for (int j = tm.tid(); j < n; j += Team::kSize) {
-      double val = kernel_entry<D>(a.P, K, pi, a.lmap[B.s_map + j], xi);
+      double val;
+      if constexpr (S)
+        val = kernel_entry_xy<D>(K, pi == is[j], xi, xs + j, n);
+      else
+        val = kernel_entry<D>(a.P, K, pi, a.lmap[B.s_map + j], xi);
       for (int k = 0; k < r; k++) val = __dsub_rn(val, __dmul_rn(U[i0 + int64_t(k) * m], V[j + int64_t(k) * n]));
       V[j + int64_t(r) * n] = val;
       s += val * val;
@@ -200,14 +296,21 @@ struct AcaTeam {
   __device__ void gen_col(int j0, int r, int nr, double& mx, int& piv, double& sq) {
     double ba = -1.0, bv = 0.0, v0 = 0.0, s = 0.0;
     int bi = 0x7fffffff;
-    const int64_t pj = a.lmap[B.s_map + j0];
+    const int64_t pj = S ? int64_t(is[j0]) : int64_t(a.lmap[B.s_map + j0]);
     for (int i = tm.tid(); i < m; i += Team::kSize) {
       // A(i, j0) with the target point first, as getCol evaluates it
       // (getMatrixEntry(sources[j], k), kernel_function.hpp:32-40).
       double xi[D];
-      const int64_t pi = a.lmap[B.t_map + i];
-      load_point<D>(a.P, pi, xi);
-      double val = kernel_entry<D>(a.P, K, pi, pj, xi);
+      double val;
+      if constexpr (S) {
+#pragma unroll
+        for (int k = 0; k < D; k++) xi[k] = xt[k * m + i];
+        val = kernel_entry_xy<D>(K, it[i] == pj, xi, xs + j0, n);
+      } else {
+        const int64_t pi = a.lmap[B.t_map + i];
+        load_point<D>(a.P, pi, xi);
+        val = kernel_entry<D>(a.P, K, pi, pj, xi);
+      }
       for (int k = 0; k < r; k++) val = __dsub_rn(val, __dmul_rn(V[j0 + int64_t(k) * n], U[i + int64_t(k) * m]));
       U[i + int64_t(r) * m] = val;
       s += val * val;
@@ -235,6 +338,7 @@ struct AcaTeam {
 
   __device__ void run(AcaOut* out) {
     const double tol = a.tol;
+    if constexpr (S) stage_points();
     init_bits(rb, nwr, m);
     init_bits(cb, nwc, n);
     tm.sync();
@@ -246,8 +350,12 @@ struct AcaTeam {
     double mx = 0.0, gamma = 0.0, mnorm = 0.0, row_norm = 0.0, col_norm = 0.0;
     int piv = 0, cur_row = 0, flags = 0;
     const int mn = min(m, n);
+    if (tm.tid() == 0) {
+      out->cap = 0;
+      out->ws = 0;
+    }
     do {
-      if (r >= cap) {
+      if (r >= cap && !grow(r, out)) {
         flags |= kAcaOverflow;
         break;
       }
@@ -334,6 +442,8 @@ struct AcaTeam {
       flags |= kAcaDense;
       rank = mn;
     }
+    if constexpr (S)
+      if (!(flags & (kAcaOverflow | kAcaDense))) write_factors(r);
     if (tm.tid() == 0) {
       out->rank = rank;
       out->flags = flags;
@@ -341,46 +451,116 @@ struct AcaTeam {
   }
 };
 
+// Next list position of a team: its static index (first pass) or, with a
+// work queue, the next value of the kind's counter (blocks are taken in list
+// order, largest first, so teams finish close together).  Team-uniform.
+template <class Team>
+__device__ __forceinline__ int next_item(const AcaArgs& a, int kind, int first, int& pass, const Team& tm) {
+  if (!a.queue) return pass++ == 0 ? first : 0x7fffffff;
+  int v = 0;
+  if (tm.tid() == 0) v = int(atomicAdd(a.queue + kind, 1u));
+  return tm.bcast(v);
+}
+
 template <int D>
 __global__ void __launch_bounds__(128) aca_warp_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
-  const int team = blockIdx.x * 4 + (threadIdx.x >> 5);
-  if (team >= count) return;
-  const int b = list[team];
-  AcaTeam<D, WarpTeam> t(a, a.blocks[b], WarpTeam());
-  t.run(a.out + b);
+  WarpTeam tm;
+  int pass = 0;
+  for (;;) {
+    const int q = next_item(a, kAcaTeamWarp, blockIdx.x * 4 + (threadIdx.x >> 5), pass, tm);
+    if (q >= count) return;
+    const int b = list[q];
+    AcaTeam<D, WarpTeam> t(a, a.blocks[b], tm);
+    t.run(a.out + b);
+  }
 }
 
 template <int D>
 __global__ void __launch_bounds__(256) aca_cta_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
   __shared__ double red[256 / 32 + 1];
   __shared__ int redi[256 / 32 + 1];
-  const int b = list[blockIdx.x];
   CtaTeam<256> tm{red, redi};
-  AcaTeam<D, CtaTeam<256>> t(a, a.blocks[b], tm);
-  t.run(a.out + b);
+  int pass = 0;
+  for (;;) {
+    const int q = next_item(a, kAcaTeamCta, int(blockIdx.x), pass, tm);
+    if (q >= count) return;
+    const int b = list[q];
+    AcaTeam<D, CtaTeam<256>> t(a, a.blocks[b], tm);
+    t.run(a.out + b);
+    tm.sync();
+  }
+}
+
+// Teams of T = 8 or 16 lanes, 128 / T per CTA, each on one block of at most
+// T rows and columns held in shared memory.
+template <int D, int T>
+__global__ void __launch_bounds__(128) aca_sub_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
+  extern __shared__ __align__(16) unsigned char asm_[];
+  constexpr int kTeams = 128 / T;
+  constexpr int kind = T == 8 ? kAcaTeam8 : kAcaTeam16;
+  const int tl = threadIdx.x / T;
+  SubTeam<T> tm;
+  int pass = 0;
+  for (;;) {
+    const int q = next_item(a, kind, blockIdx.x * kTeams + tl, pass, tm);
+    if (q >= count) return;
+    const int b = list[q];
+    AcaTeam<D, SubTeam<T>, true> t(a, a.blocks[b], tm, asm_ + tl * staged_team_bytes(T, D));
+    t.run(a.out + b);
+    tm.sync();  // the team's shared memory is reused by its next block
+  }
+}
+
+// CTAs of a launch: one per team's share of the list, or with work queues
+// at most a.max_ctas (the teams loop over the queue).
+unsigned aca_grid(const AcaArgs& a, int count, int teams_per_cta) {
+  const int need = (count + teams_per_cta - 1) / teams_per_cta;
+  return unsigned(a.queue && a.max_ctas > 0 ? min(need, a.max_ctas) : need);
+}
+
+template <int D, int T>
+void launch_sub(const AcaArgs& a, const int32_t* list, int count, cudaStream_t st) {
+  constexpr int kTeams = 128 / T;
+  constexpr int bytes = kTeams * staged_team_bytes(T, D);
+  static_assert(bytes <= 227 * 1024, "staged ACA teams exceed the shared memory of a CTA");
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(aca_sub_kernel<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  aca_sub_kernel<D, T><<<aca_grid(a, count, kTeams), 128, bytes, st>>>(a, list, count);
 }
 
 template <int D>
-void launch_d(const AcaArgs& a, const int32_t* warp_list, int nwarp, const int32_t* cta_list, int ncta,
-              cudaStream_t st) {
-  if (nwarp > 0) aca_warp_kernel<D><<<unsigned((nwarp + 3) / 4), 128, 0, st>>>(a, warp_list, nwarp);
-  if (ncta > 0) aca_cta_kernel<D><<<unsigned(ncta), 256, 0, st>>>(a, cta_list, ncta);
+void launch_d(const AcaArgs& a, const AcaLists& L, cudaStream_t st) {
+  if (L.n[kAcaTeamCta] > 0)
+    aca_cta_kernel<D><<<aca_grid(a, L.n[kAcaTeamCta], 1), 256, 0, st>>>(a, L.list[kAcaTeamCta], L.n[kAcaTeamCta]);
+  if (L.n[kAcaTeamWarp] > 0)
+    aca_warp_kernel<D><<<aca_grid(a, L.n[kAcaTeamWarp], 4), 128, 0, st>>>(a, L.list[kAcaTeamWarp],
+                                                                          L.n[kAcaTeamWarp]);
+  if (L.n[kAcaTeam16] > 0) launch_sub<D, 16>(a, L.list[kAcaTeam16], L.n[kAcaTeam16], st);
+  if (L.n[kAcaTeam8] > 0) launch_sub<D, 8>(a, L.list[kAcaTeam8], L.n[kAcaTeam8], st);
 }
 
 }  // namespace
 
-cudaError_t launch_aca(int ndim, const AcaArgs& a, const int32_t* warp_list, int nwarp, const int32_t* cta_list,
-                       int ncta, cudaStream_t st) {
-  count_launches(uint64_t(nwarp > 0) + uint64_t(ncta > 0));
+int aca_team(int m, int n) {
+  const int mx = m > n ? m : n;
+  if (mx <= 8) return kAcaTeam8;
+  if (mx <= 16) return kAcaTeam16;
+  if (mx <= 256) return kAcaTeamWarp;
+  return kAcaTeamCta;
+}
+
+cudaError_t launch_aca(int ndim, const AcaArgs& a, const AcaLists& L, cudaStream_t st) {
+  uint64_t k = 0;
+  for (int q = 0; q < kAcaTeamKinds; q++) k += uint64_t(L.n[q] > 0);
+  count_launches(k);
   switch (ndim) {
-    case 1: launch_d<1>(a, warp_list, nwarp, cta_list, ncta, st); break;
-    case 2: launch_d<2>(a, warp_list, nwarp, cta_list, ncta, st); break;
-    case 3: launch_d<3>(a, warp_list, nwarp, cta_list, ncta, st); break;
-    case 4: launch_d<4>(a, warp_list, nwarp, cta_list, ncta, st); break;
-    case 5: launch_d<5>(a, warp_list, nwarp, cta_list, ncta, st); break;
-    case 6: launch_d<6>(a, warp_list, nwarp, cta_list, ncta, st); break;
-    case 7: launch_d<7>(a, warp_list, nwarp, cta_list, ncta, st); break;
-    case 8: launch_d<8>(a, warp_list, nwarp, cta_list, ncta, st); break;
+    case 1: launch_d<1>(a, L, st); break;
+    case 2: launch_d<2>(a, L, st); break;
+    case 3: launch_d<3>(a, L, st); break;
+    case 4: launch_d<4>(a, L, st); break;
+    case 5: launch_d<5>(a, L, st); break;
+    case 6: launch_d<6>(a, L, st); break;
+    case 7: launch_d<7>(a, L, st); break;
+    case 8: launch_d<8>(a, L, st); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -27,6 +27,9 @@ struct AcaBlockDesc {
 struct AcaOut {
   int32_t rank;   // rank, or min(m, n) for a block kept dense
   int32_t flags;  // kAcaDense | kAcaOverflow
+  int32_t cap;    // workspace columns of the result (0: the descriptor's)
+  int32_t pad;
+  int64_t ws;     // offset (doubles, from AcaArgs::ws) of the result's U and V when cap != 0
 };
 
 struct AcaArgs {
@@ -42,11 +45,34 @@ struct AcaArgs {
   uint32_t* bits;
   int32_t* lists;
   AcaOut* out;
+  // Growth arena: a block whose rank reaches its workspace columns takes a
+  // workspace of 4 x the columns (at most min(m, n)) from ws + arena_off on,
+  // bumping *arena_used (doubles); when the arena is full it reports
+  // kAcaOverflow instead.  arena_used == nullptr: no arena (overflow at once).
+  int64_t arena_off;
+  uint64_t arena_size;
+  unsigned long long* arena_used;
+  // Work queues: with queue != nullptr every team takes its next block from
+  // queue[kind] (an atomic counter the caller zeroes) until the list is done,
+  // and a launch has at most max_ctas CTAs.
+  unsigned int* queue;
+  int max_ctas;
 };
 
-// warp_list / cta_list: indices into a.blocks compressed by one warp / one
-// 256-thread CTA each.  Asynchronous on st.
-cudaError_t launch_aca(int ndim, const AcaArgs& a, const int32_t* warp_list, int nwarp, const int32_t* cta_list,
-                       int ncta, cudaStream_t st);
+// Team kinds: 8 or 16 lanes of a warp (blocks of at most 8 or 16 rows and
+// columns, held in shared memory), a warp (at most 256), a 256-thread CTA.
+enum : int { kAcaTeam8 = 0, kAcaTeam16 = 1, kAcaTeamWarp = 2, kAcaTeamCta = 3, kAcaTeamKinds = 4 };
+// The team kind that compresses an m x n block.  The team size sets the
+// order in which the norms of the stopping rule are summed, so every caller
+// that must reproduce hodlr_build's factors picks teams with this.
+int aca_team(int m, int n);
+
+// list[k]: indices into a.blocks compressed by teams of kind k (n[k] of them)
+struct AcaLists {
+  const int32_t* list[kAcaTeamKinds];
+  int n[kAcaTeamKinds];
+};
+// Asynchronous on st.
+cudaError_t launch_aca(int ndim, const AcaArgs& a, const AcaLists& lists, cudaStream_t st);
 
 }  // namespace hodlr

@@ -51,6 +51,26 @@ __device__ __forceinline__ double kernel_entry(const PointsDev& P, const KernelD
   }
 }
 
+// The same entry from two staged coordinate vectors (stride ld between
+// coordinates); same_point: the tree positions are equal (the diagonal).
+template <int D>
+__device__ __forceinline__ double kernel_entry_xy(const KernelDev& K, bool same_point, const double* xi,
+                                                  const double* xj, int ld) {
+  if (same_point) return K.diag;
+  double d2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; k++) {
+    const double t = __dsub_rn(xi[k], xj[k * ld]);
+    d2 = __dadd_rn(d2, __dmul_rn(t, t));
+  }
+  switch (K.kind) {
+    case kInvR: return __ddiv_rn(K.scale, __dsqrt_rn(d2));
+    case kInvR2: return __ddiv_rn(K.scale, d2);
+    case kLogR: return __dmul_rn(K.scale, log(__dsqrt_rn(d2)));
+    default: return __dmul_rn(K.scale, exp(-__dsqrt_rn(d2)));
+  }
+}
+
 template <int D>
 __device__ __forceinline__ void load_point(const PointsDev& P, int64_t i, double* xi) {
 #pragma unroll
@@ -128,6 +148,38 @@ struct WarpTeam {
   }
   __device__ __forceinline__ int bcast(int v) const { return __shfl_sync(0xffffffffu, v, 0); }
   __device__ __forceinline__ double bcast(double v) const { return __shfl_sync(0xffffffffu, v, 0); }
+};
+
+// T lanes of one warp (T = 8 or 16): lanes 0..T-1, T..2T-1, ... each form a
+// team of their own.  Teams of one warp may follow different control flow
+// (their blocks differ); every shuffle names only the team's lanes.
+template <int T>
+struct SubTeam {
+  static constexpr int kSize = T;
+  unsigned mask;
+  __device__ __forceinline__ SubTeam() : mask(((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1))) {}
+  __device__ __forceinline__ int tid() const { return threadIdx.x & (T - 1); }
+  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+  __device__ __forceinline__ double sum(double v) const {
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, T);
+    return v;
+  }
+  __device__ __forceinline__ void argmax(double& a, int& i, double& v) const {
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) {
+      const double a2 = __shfl_xor_sync(mask, a, o, T);
+      const int i2 = __shfl_xor_sync(mask, i, o, T);
+      const double v2 = __shfl_xor_sync(mask, v, o, T);
+      if (a2 > a || (a2 == a && i2 < i)) {
+        a = a2;
+        i = i2;
+        v = v2;
+      }
+    }
+  }
+  __device__ __forceinline__ int bcast(int v) const { return __shfl_sync(mask, v, 0, T); }
+  __device__ __forceinline__ double bcast(double v) const { return __shfl_sync(mask, v, 0, T); }
 };
 
 template <int NT>

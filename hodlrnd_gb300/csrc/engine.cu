@@ -172,6 +172,8 @@ struct Plan {
   PanelFix* pfix_near = nullptr;  // near panels above 32 rows split over items (share ypart with the far ones)
   int npfix_near = 0;
   int64_t nypart_near = 0;
+  // small items stream their segments as one byte run (small_items_contiguous)
+  bool contig_near = false, contig_far = false;
   int64_t nzpart = 0, nypart = 0;  // partial-sum scratch (elements of the vector type)
   void* zpart = nullptr;
   void* ypart = nullptr;
@@ -213,6 +215,11 @@ struct hodlr_op {
   NearList near;
   std::vector<int32_t> rank, dense;
   std::vector<const void*> uptr, vptr;  // stored factors (or dense tile) of each far block
+  // reduced-precision operators with the FP64 check: the FP64 factors of
+  // every far block and the FP64 operator's plan (the refinement residuals)
+  bool has_ref = false;
+  std::vector<const void*> uptr64, vptr64;
+  Plan plan_ref;
   int64_t n = 0, zlen = 0;
   int nslots = 0;
   DevMem mem;
@@ -232,6 +239,8 @@ struct hodlr_op {
   double* d_r64 = nullptr;
   float* d_r32 = nullptr;
   float* d_d32 = nullptr;
+  double* d_rref = nullptr;  // FP64 check: the refinement residual and correction, n each
+  double* d_dref = nullptr;
   double* d_io = nullptr;    // caller-order staging, n
   double* d_io2 = nullptr;
   double* d_hb = nullptr;    // host-API staging of one right-hand side and its solution
@@ -391,6 +400,7 @@ void build_near_plan(hodlr_op* op, const NearTiles& nt, const void* base, Prec a
       }
     }
   }
+  plan.contig_near = small_items_contiguous(panels, segs, small, int(esz));
   plan.pfix_near = upload(op->mem, pfix, st, "near panel fix-ups");
   plan.npfix_near = int(pfix.size());
   plan.nypart_near = nypart * rows_per_item(a);
@@ -502,6 +512,12 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   }
   op->zlen = zoff - op->n;
   plan.a_far = a;
+  // FP64 far factors stay where the ACA batches put them, so whether a panel's
+  // blocks follow one another depends on the batch split (and differs for an
+  // operator read from a file): their panels always take the direct-load
+  // kernel, whose results do not depend on the layout.  FP32 and BF16 factors
+  // are laid out in panel order (relayout_far).
+  plan.contig_far = a != Prec::kD && small_items_contiguous(panels, segs, small, prec_size(a));
   plan.panels_far = upload(op->mem, panels, st, "far panels");
   plan.segs_far = upload(op->mem, segs, st, "far segments");
   plan.small_far = upload(op->mem, small, st, "far items");
@@ -581,6 +597,8 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     op->dense.assign(nb, 0);
     op->uptr.assign(nb, nullptr);
     op->vptr.assign(nb, nullptr);
+    op->uptr64.assign(op->has_ref ? nb : 0, nullptr);
+    op->vptr64.assign(op->has_ref ? nb : 0, nullptr);
     boff[j + 1] = boff[j] + int64_t(nb);
     if (j + 1 < nops) {
       pbase[j + 1] = pbase[j] + op->n;
@@ -616,7 +634,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   // Scratch of one batch: the FP64 workspace is bounded (4 GiB by default);
   // a single block that needs more grows it.  Not counted against the
   // operators' memory: it is freed when the build returns.
-  const size_t max_batch = 1 << 20;
+  const size_t max_batch = size_t(1) << 23;
   struct Scratch {
     void* p = nullptr;
     size_t bytes = 0;
@@ -633,13 +651,28 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       bytes = need;
     }
   };
-  Scratch s_ws, s_bits, s_lists, s_desc, s_out, s_idx, s_cd, s_pts, s_lmap;
-  const uint64_t ws_doubles = uint64_t(1) << 29;
-  const uint64_t bits_room = uint64_t(1) << 26, list_room = uint64_t(1) << 26;
-  s_desc.ensure(max_batch * sizeof(AcaBlockDesc), st, "ACA descriptors");
-  s_out.ensure(max_batch * sizeof(AcaOut), st, "ACA results");
-  s_idx.ensure(max_batch * sizeof(int32_t), st, "ACA team lists");
-  s_cd.ensure(max_batch * sizeof(CompactDesc), st, "compaction descriptors");
+  Scratch s_ws, s_bits, s_lists, s_desc, s_out, s_idx, s_cd, s_pts, s_lmap, s_ctr;
+  // FP64 workspace of one launch: a quarter of the free device memory,
+  // between 4 and 64 GiB, so that most operators are compressed by one
+  // launch per team kind; a growth arena of an eighth of it on top
+  size_t free_b = 0, total_b = 0;
+  check_cuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  const uint64_t ws_doubles =
+      op0->p.aca_workspace_mib > 0
+          ? std::max<uint64_t>(uint64_t(1) << 17, uint64_t(op0->p.aca_workspace_mib) << 17)
+          : std::min<uint64_t>(uint64_t(1) << 33, std::max<uint64_t>(uint64_t(1) << 29, uint64_t(free_b) / 4 / 8));
+  const uint64_t arena_doubles = ws_doubles / 8;
+  const uint64_t bits_room = ws_doubles / 8, list_room = ws_doubles / 8;
+  const size_t nslot = std::min(nb, max_batch);
+  s_desc.ensure(nslot * sizeof(AcaBlockDesc), st, "ACA descriptors");
+  s_out.ensure(nslot * sizeof(AcaOut), st, "ACA results");
+  s_idx.ensure(nslot * sizeof(int32_t), st, "ACA team lists");
+  const size_t max_cd = size_t(1) << 20;  // compaction descriptors per launch
+  s_cd.ensure(std::min(nslot, max_cd) * sizeof(CompactDesc), st, "compaction descriptors");
+  // the work-queue counters of the team kinds and the growth arena's counter
+  s_ctr.ensure(64, st, "ACA counters");
+  int sms = 0;
+  check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op0->p.device), "cudaDeviceGetAttribute");
   AcaBlockDesc* d_desc = static_cast<AcaBlockDesc*>(s_desc.p);
   AcaOut* d_out = static_cast<AcaOut*>(s_out.p);
   int32_t* d_lists_idx = static_cast<int32_t*>(s_idx.p);
@@ -677,7 +710,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   std::vector<size_t> retry;
   std::vector<AcaBlockDesc> desc;
   std::vector<AcaOut> out;
-  std::vector<int32_t> warp_list, cta_list;
+  std::vector<std::vector<int32_t>> team_list(kAcaTeamKinds);
   std::vector<CompactDesc> cds;
   while (pos < todo.size() || !retry.empty()) {
     // next batch
@@ -704,8 +737,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       while (pos < todo.size() && take(todo[pos])) pos++;
     }
     desc.resize(batch.size());
-    warp_list.clear();
-    cta_list.clear();
+    for (auto& l : team_list) l.clear();
     uint64_t ow = 0, ob = 0, ol = 0;
     for (size_t q = 0; q < batch.size(); q++) {
       const size_t g = batch[q];
@@ -726,11 +758,17 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       ow += ws_need(g);
       ob += uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32);
       ol += uint64_t(2 * (cap[g] + 2));
-      (std::max(mm[g], nn[g]) <= 256 ? warp_list : cta_list).push_back(int32_t(q));
+      team_list[size_t(aca_team(mm[g], nn[g]))].push_back(int32_t(q));
     }
-    std::vector<int32_t> lst(cta_list);
-    lst.insert(lst.end(), warp_list.begin(), warp_list.end());
-    s_ws.ensure(std::max<uint64_t>(ow, 1) * 8, st, "ACA workspace");
+    // one index array, the team kinds one after another (largest blocks first)
+    std::vector<int32_t> lst;
+    AcaLists al;
+    size_t lpos[kAcaTeamKinds];
+    for (int k = kAcaTeamKinds - 1; k >= 0; k--) {
+      lpos[k] = lst.size();
+      lst.insert(lst.end(), team_list[size_t(k)].begin(), team_list[size_t(k)].end());
+    }
+    s_ws.ensure((ow + arena_doubles) * 8, st, "ACA workspace");
     s_bits.ensure(std::max<uint64_t>(ob, 1) * 4, st, "ACA bitmaps");
     s_lists.ensure(std::max<uint64_t>(ol, 1) * 4, st, "ACA index lists");
     double* ws = static_cast<double*>(s_ws.p);
@@ -746,8 +784,19 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     a.bits = static_cast<uint32_t*>(s_bits.p);
     a.lists = static_cast<int32_t*>(s_lists.p);
     a.out = d_out;
-    CK(launch_aca(ndim, a, d_lists_idx + cta_list.size(), int(warp_list.size()), d_lists_idx, int(cta_list.size()),
-                  st));
+    // one persistent launch per team kind: teams take their blocks from a
+    // work queue; blocks whose rank outgrows their columns continue in the arena
+    CK(cudaMemsetAsync(s_ctr.p, 0, 64, st));
+    a.queue = static_cast<unsigned int*>(s_ctr.p);
+    a.arena_used = reinterpret_cast<unsigned long long*>(static_cast<char*>(s_ctr.p) + 32);
+    a.arena_off = int64_t(ow);
+    a.arena_size = arena_doubles;
+    a.max_ctas = sms * 16;
+    for (int k = 0; k < kAcaTeamKinds; k++) {
+      al.list[k] = d_lists_idx + lpos[k];
+      al.n[k] = int(team_list[size_t(k)].size());
+    }
+    CK(launch_aca(ndim, a, al, st));
     out.resize(batch.size());
     CK(cudaMemcpyAsync(out.data(), d_out, out.size() * sizeof(AcaOut), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -787,7 +836,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       c.s_begin = sb[g];
       c.t_map = desc[q].t_map;
       c.s_map = desc[q].s_map;
-      c.ws = desc[q].ws;
+      c.ws = out[q].cap ? out[q].ws : desc[q].ws;
       const int32_t rk = std::max(op->rank[b], 0);
       c.u_dst = ch + off[q];
       c.v_dst = ch + off[q] + far_u_bytes(mm[g], nn[g], rk, op->dense[b], fp);
@@ -800,17 +849,76 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       c.n = nn[g];
       c.rank = op->rank[b];
       c.dense = op->dense[b];
-      c.cap = desc[q].cap;
+      c.cap = out[q].cap ? out[q].cap : desc[q].cap;
       c.pad = 0;
       c.kscale = desc[q].kscale;
       op->uptr[b] = c.u_dst;
       op->vptr[b] = c.v_dst;
       if (op->dense[b] || op->rank[b] > 0) cds.push_back(c);
     }
-    if (!cds.empty()) {
-      CK(cudaMemcpyAsync(d_cd, cds.data(), cds.size() * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
-      CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(cds.size()), fp, st));
+    for (size_t b0 = 0; b0 < cds.size(); b0 += max_cd) {
+      const size_t k = std::min(max_cd, cds.size() - b0);
+      CK(cudaMemcpyAsync(d_cd, cds.data() + b0, k * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
+      CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(k), fp, st));
       CK(cudaStreamSynchronize(st));
+    }
+    // the FP64 factors of the same blocks, for operators that keep them
+    if (fp != Prec::kD) {
+      std::vector<uint64_t> bytes64(nops, 0), off64(batch.size(), 0);
+      for (size_t q = 0; q < batch.size(); q++) {
+        const size_t g = batch[q];
+        hodlr_op* op = ops[size_t(job[g])];
+        if (!op->has_ref || (out[q].flags & kAcaOverflow)) continue;
+        const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
+        off64[q] = bytes64[size_t(job[g])];
+        const int64_t r = op->rank[b];
+        bytes64[size_t(job[g])] += far_u_bytes(mm[g], nn[g], r, op->dense[b], Prec::kD) +
+                                   far_v_bytes(nn[g], r, op->dense[b], Prec::kD);
+      }
+      std::vector<char*> chunk64(nops, nullptr);
+      bool any = false;
+      for (size_t j = 0; j < nops; j++)
+        if (bytes64[j] > 0) {
+          chunk64[j] = static_cast<char*>(ops[j]->mem.alloc(bytes64[j], "far-field factors (FP64 reference)"));
+          CK(cudaMemsetAsync(chunk64[j], 0, bytes64[j], st));
+          any = true;
+        }
+      if (any) {
+        std::vector<CompactDesc> cd64;
+        for (size_t q = 0; q < batch.size(); q++) {
+          const size_t g = batch[q];
+          hodlr_op* op = ops[size_t(job[g])];
+          if (!op->has_ref || (out[q].flags & kAcaOverflow)) continue;
+          const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
+          if (!op->dense[b] && op->rank[b] <= 0) continue;
+          char* ch = chunk64[size_t(job[g])];
+          CompactDesc c;
+          c.t_begin = tb[g];
+          c.s_begin = sb[g];
+          c.t_map = desc[q].t_map;
+          c.s_map = desc[q].s_map;
+          c.ws = out[q].cap ? out[q].ws : desc[q].ws;
+          c.u_dst = ch + off64[q];
+          c.v_dst = ch + off64[q] + far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD);
+          c.s_dst = nullptr;
+          c.m = mm[g];
+          c.n = nn[g];
+          c.rank = op->rank[b];
+          c.dense = op->dense[b];
+          c.cap = out[q].cap ? out[q].cap : desc[q].cap;
+          c.pad = 0;
+          c.kscale = desc[q].kscale;
+          op->uptr64[b] = c.u_dst;
+          op->vptr64[b] = c.v_dst;
+          cd64.push_back(c);
+        }
+        for (size_t b0 = 0; b0 < cd64.size(); b0 += max_cd) {
+          const size_t k = std::min(max_cd, cd64.size() - b0);
+          CK(cudaMemcpyAsync(d_cd, cd64.data() + b0, k * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
+          CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(k), Prec::kD, st));
+          CK(cudaStreamSynchronize(st));
+        }
+      }
     }
   }
 }
@@ -880,6 +988,13 @@ void compute_stats(hodlr_op* op) {
                            N * (slots - 1.0) * sx;
     op->tr.bytes[kb + 3] = N * slots * sx + N * sx;
   }
+  if (op->has_ref) {  // the FP64 operator of the refinement residuals
+    const int kb = HODLR_TRACE_ZGEMV_REF;
+    op->tr.bytes[kb + 0] = lr_cols * 8.0 + zsum * 8.0 + N * 8.0;
+    op->tr.bytes[kb + 1] = s.near_entries * 8.0 + 2.0 * N * 8.0;
+    op->tr.bytes[kb + 2] = (lr_rows + s.dense_far_entries) * 8.0 + zsum * 8.0 + N * 8.0 + N * (slots - 1.0) * 8.0;
+    op->tr.bytes[kb + 3] = N * slots * 8.0 + N * 8.0;
+  }
 }
 
 // ---------------------------------------------------------------- apply
@@ -907,7 +1022,9 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
     if (e != cudaSuccess) return e;
   }
   const Prec px = PrecOf<T>::v;
-  const int kb = px == Prec::kD ? HODLR_TRACE_ZGEMV_FP64 : HODLR_TRACE_ZGEMV_FP32;
+  const int kb = &plan == &op->plan_ref ? HODLR_TRACE_ZGEMV_REF
+                 : px == Prec::kD       ? HODLR_TRACE_ZGEMV_FP64
+                                        : HODLR_TRACE_ZGEMV_FP32;
   Tracer& tr = op->tr;
   if (plan.nzb > 0) tr.start(kb + 0, st);
   // FP32 or BF16 factors with FP64 vectors: compensated (or, while the solver
@@ -928,14 +1045,14 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   tr.start(kb + 1, st);
   if ((e = launch_panels(plan.a_near, px, plan.panels_near, plan.segs_near, plan.small_near, plan.nsmall_near,
                          plan.big_near, plan.nbig_near, plan.pfix_near, plan.npfix_near, plan.ypart, in, ldin, yslots, n,
-                         op->nslots, 1, st)) != cudaSuccess)
+                         op->nslots, 1, st, Accum::kByType, plan.contig_near)) != cudaSuccess)
     return e;
   tr.stop(st);
   const bool far = plan.nsmall_far + plan.nbig_far > 0;
   if (far) tr.start(kb + 2, st);
   if ((e = launch_panels(plan.a_far, px, plan.panels_far, plan.segs_far, plan.small_far, plan.nsmall_far, plan.big_far,
                          plan.nbig_far, plan.pfix_far, plan.npfix_far, plan.ypart, fin, ldin, yslots, n, op->nslots, 1,
-                         st, acc)) != cudaSuccess)
+                         st, acc, plan.contig_far)) != cudaSuccess)
     return e;
   if (far) tr.stop(st);
   tr.start(kb + 3, st);
@@ -943,6 +1060,11 @@ cudaError_t apply_tree(hodlr_op* op, const Plan& plan, const T* x, T* y, T* in, 
   tr.stop(st);
   if (tr.used > 8192) tr.harvest();
   return e;
+}
+
+__global__ void axpy_d_kernel(double* x, const double* d, int64_t n) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    x[i] = x[i] + d[i];
 }
 
 __global__ void axpy_f2d_kernel(double* x, const float* d, int64_t n) {
@@ -960,81 +1082,135 @@ Ortho ortho_of(const hodlr_params& p) {
 }
 
 // Solve in tree order on device buffers b, x (one right-hand side).
-// The stored-operator residual a solve stops at, as a fraction of tol: FP32
-// factors differ from the FP64 operator by their rounding (about 5e-9 relative
-// at eps_aca 1e-8, measured at N = 262144), so their solves stop at half of
-// tol to keep the residual against the FP64 operator below tol too.
-double stored_margin(const hodlr_params& p) {
-  if (p.stored_margin > 0) return p.stored_margin;
-  return (p.precision == HODLR_PREC_FP32_FACTORS || p.precision == HODLR_PREC_MIXED) ? 0.5 : 1.0;
+// Reduced-precision operators keep the FP64 far field unless the FP64 check is off.
+bool wants_ref(const hodlr_params& p) {
+  return p.precision != HODLR_PREC_FP64 && p.fp64_check != HODLR_FP64_CHECK_OFF;
 }
+
+// |b - A x| / |b| with the FP64-vector operator of `plan` (plan64: the stored
+// operator, compensated products unless relaxed ones are forced; plan_ref:
+// the FP64 operator); the residual vector is left in op->d_r64.  Tree order.
+double true_residual(hodlr_op* op, const Plan& plan, const double* b, const double* x, cudaStream_t st) {
+  CK(apply_tree<double>(op, plan, x, op->d_io2, op->d_in64, op->d_y64, st));
+  CK(vec_sub_norm2<double>(b, op->d_io2, op->d_r64, op->n, op->d_part, op->d_scal + 1, st));
+  CK(vec_norm2<double>(b, op->n, op->d_part, op->d_scal + 2, st));
+  CK(cudaMemcpyAsync(op->h_scal, op->d_scal, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return op->h_scal[1] / (op->h_scal[2] == 0.0 ? 1.0 : op->h_scal[2]);
+}
+
+// Iterative refinement with the FP64 operator around solves with the stored
+// one: while |b - A64 x| / |b| > tol, solve A_stored d = r (r = b - A64 x,
+// from d = 0, to a relative residual that leaves a 0.3 margin below tol)
+// and x += d.  Each sweep multiplies the FP64 residual by about
+// max(its inner tolerance, |A_stored^-1 (A64 - A_stored)|): far below 1 for
+// FP32 factors (one sweep), about 1e-3 x the conditioning for BF16.
+// `inner` runs the stored-operator solve of A d = r into d; returns the
+// FP64 residual, counts sweeps and inner iterations.
+double refine(hodlr_op* op, const double* b, double* x, double tol, int max_sweeps, int64_t max_iter, cudaStream_t st,
+              const std::function<int64_t(const double* r, double* d, double sweep_tol, int64_t its_left)>& inner,
+              int* sweeps, int64_t* its) {
+  double res = true_residual(op, op->plan_ref, b, x, st);
+  while (res > tol && *sweeps < max_sweeps && *its < max_iter) {
+    // the correction's own stopping point, relative to |r|
+    const double sweep_tol = std::min(0.5, 0.3 * tol / res);
+    CK(cudaMemcpyAsync(op->d_rref, op->d_r64, sizeof(double) * size_t(op->n), cudaMemcpyDeviceToDevice, st));
+    *its += inner(op->d_rref, op->d_dref, sweep_tol, max_iter - *its);
+    axpy_d_kernel<<<kVecCtas, 256, 0, st>>>(x, op->d_dref, op->n);
+    CK(cudaGetLastError());
+    (*sweeps)++;
+    res = true_residual(op, op->plan_ref, b, x, st);
+  }
+  return res;
+}
+
+// The stored-operator residual a solve without the FP64 check stops at.
+double stored_stop(const hodlr_params& p, double tol) { return tol * (p.stored_margin > 0 ? p.stored_margin : 1.0); }
 
 void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr_solve_info* info) {
   const hodlr_params& p = op->p;
-  const double tol_req = p.tol > 0 ? p.tol : p.eps_aca;
-  const double tol = tol_req * stored_margin(p);
-  info->stop_tol = tol;
+  const double tol = p.tol > 0 ? p.tol : p.eps_aca;
   const int64_t max_iter = p.max_iter > 0 ? p.max_iter : op->n;
   const int restart = p.restart > 0 ? p.restart : 100;
+  const int max_outer = p.max_outer > 0 ? p.max_outer : 10;
   const double t0 = now_s();
+  const bool ref = op->has_ref;
+  double stop = ref ? tol : stored_stop(p, tol);
   if (p.precision != HODLR_PREC_MIXED) {
     // HODLRdD_matrix::solve: x0 = b, iterSolver(100, N, eps_ACA) (HDD_matrix.hpp:51-62);
-    // with FP32 factors the same FP64 GMRES runs on the FP32-stored operator
+    // with FP32 or BF16 factors the same FP64 GMRES runs on the stored operator
     CK(cudaMemcpyAsync(x, b, sizeof(double) * size_t(op->n), cudaMemcpyDeviceToDevice, st));
     TreeMatvec<double> A = [op, st](const double* xi, double* yo) {
       return apply_tree<double>(op, op->plan64, xi, yo, op->d_in64, op->d_y64, st);
     };
-    GmresResult r;
     // FP32 or BF16 factors: relaxed accumulation once the residual estimate is below
     // relax_below (tol * 1e5) -- an inexact Krylov method may take products with relative
     // error up to about tol / |r_k| (Simoncini and Szyld, SIAM J. Sci.
     // Comput. 25 (2003); Bouras and Fraysse, SIAM J. Matrix Anal. Appl. 26
     // (2005)), and relaxed products are accurate to about 1e-6 -- then the
-    // true residual with compensated products decides, and GMRES continues
-    // from x with compensated products while it is above tol.
-    const bool relax = (p.precision == HODLR_PREC_FP32_FACTORS || p.precision == HODLR_PREC_BF16_FACTORS) &&
-                       p.relax != HODLR_RELAX_OFF;
-    const double relax_at = p.relax_below > 0 ? p.relax_below : std::min(1.0, tol_req * kRelaxFactor);
+    // true residual decides (with the FP64 operator, or with compensated
+    // products on the stored one), and GMRES continues while it is above tol.
+    const bool reduced = p.precision != HODLR_PREC_FP64;
+    const bool relax = reduced && p.relax != HODLR_RELAX_OFF;
+    const double relax_at = p.relax_below > 0 ? p.relax_below : std::min(1.0, tol * kRelaxFactor);
     std::function<void(double)> progress;
     if (relax) progress = [op, relax_at](double res) { op->relaxed = res < relax_at; };
+    // The first solve's target on the stored operator: tol (FP32 factors, whose
+    // rounding is about tol at eps_aca 1e-8), or inner_tol for BF16 factors
+    // (about 1e-3 from the FP64 operator: refinement sweeps take it from there).
+    const double first_tol = !ref || p.precision != HODLR_PREC_BF16_FACTORS
+                                 ? stop
+                                 : std::max(stop, p.inner_tol > 0 ? p.inner_tol : 1e-4);
     op->relaxed = false;
-    const cudaError_t ge = gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter, tol, st, &r, ortho_of(p),
-                                               progress);
+    GmresResult r;
+    const cudaError_t ge =
+        gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter, first_tol, st, &r, ortho_of(p), progress);
     op->relaxed = false;
     CK(ge);
     int64_t its = r.iterations;
     int sweeps = 1;
-    double res = r.resid;
+    double res = r.resid, res_stored = r.resid;
     bool conv = r.converged;
-    if (relax && conv) {
+    if (reduced && !ref && conv) {
+      // no FP64 operator: the stored operator's true residual with compensated products
       for (;;) {
-        // |b - A x| / |b| with compensated products
-        CK(apply_tree<double>(op, op->plan64, x, op->d_io2, op->d_in64, op->d_y64, st));
-        CK(vec_sub_norm2<double>(b, op->d_io2, op->d_r64, op->n, op->d_part, op->d_scal + 1, st));
-        CK(vec_norm2<double>(b, op->n, op->d_part, op->d_scal + 2, st));
-        CK(cudaMemcpyAsync(op->h_scal, op->d_scal, sizeof(double) * 3, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        res = op->h_scal[1] / (op->h_scal[2] == 0.0 ? 1.0 : op->h_scal[2]);
-        if (res <= tol || sweeps >= 4 || its >= max_iter) break;
+        res = res_stored = true_residual(op, op->plan64, b, x, st);
+        if (res <= stop || sweeps >= 4 || its >= max_iter) break;
         GmresResult r2;
-        CK(gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter - its, tol, st, &r2, ortho_of(p)));
+        CK(gmres_solve<double>(op->g64, A, b, x, false, restart, max_iter - its, stop, st, &r2, ortho_of(p)));
         its += r2.iterations;
         sweeps++;
       }
-      conv = res <= tol;
+      conv = res <= stop;
+    } else if (ref) {
+      res_stored = true_residual(op, op->plan64, b, x, st);
+      auto inner = [&](const double* rr, double* d, double sweep_tol, int64_t left) -> int64_t {
+        GmresResult r2;
+        op->relaxed = false;
+        const cudaError_t e =
+            gmres_solve<double>(op->g64, A, rr, d, true, restart, left, sweep_tol, st, &r2, ortho_of(p), progress);
+        op->relaxed = false;
+        CK(e);
+        return r2.iterations;
+      };
+      res = refine(op, b, x, stop, max_outer + 1, max_iter, st, inner, &sweeps, &its);
+      conv = res <= stop;
     }
     CK(cudaStreamSynchronize(st));
     info->iterations = its;
     info->outer_iterations = sweeps;
     info->rel_residual = res;
+    info->rel_residual_stored = reduced ? res_stored : res;
     info->converged = conv ? 1 : 0;
   } else {
-    // FP64 iterative refinement around FP32 GMRES on the FP32 operator
-    const int max_outer = p.max_outer > 0 ? p.max_outer : 10;
+    // FP64 iterative refinement around FP32 GMRES on the FP32 operator; the
+    // refinement residual with the FP64 operator (FP64 check) or with the
+    // FP64-vector stored operator (FP64 near field, FP32 far factors)
     const double inner_tol = p.inner_tol > 0 ? p.inner_tol : 1e-4;
     TreeMatvec<float> A32 = [op, st](const float* xi, float* yo) {
       return apply_tree<float>(op, op->plan32, xi, yo, op->d_in32, op->d_y32, st);
     };
+    const Plan& R = ref ? op->plan_ref : op->plan64;
     const int64_t n = op->n;
     CK(cudaMemsetAsync(x, 0, sizeof(double) * size_t(n), st));
     CK(cudaMemcpyAsync(op->d_r64, b, sizeof(double) * size_t(n), cudaMemcpyDeviceToDevice, st));
@@ -1046,34 +1222,38 @@ void solve_tree(hodlr_op* op, const double* b, double* x, cudaStream_t st, hodlr
     double rel = op->h_scal[1] / normb;
     int64_t inner_total = 0;
     int outer = 0;
-    while (rel > tol && outer < max_outer && inner_total < max_iter) {
+    while (rel > stop && outer < max_outer && inner_total < max_iter) {
       CK(launch_gather(op->d_r64, Prec::kD, n, nullptr, n, 1, op->d_r32, Prec::kF, n, st));
       GmresResult r;
       // The first sweep stops at inner_tol; a later sweep aims below what the
-      // remaining reduction needs (tol |b| / |r|, with a 0.3 margin) so that
-      // it ends the solve instead of leaving a residual just above tol.
+      // remaining reduction needs (stop |b| / |r|, with a 0.3 margin) so that
+      // it ends the solve instead of leaving a residual just above the target.
       double sweep_tol = inner_tol;
-      if (outer > 0) sweep_tol = std::min(inner_tol, 0.3 * tol / rel);
+      if (outer > 0) sweep_tol = std::min(inner_tol, 0.3 * stop / rel);
       CK(gmres_solve<float>(op->g32, A32, op->d_r32, op->d_d32, true, restart, max_iter - inner_total,
-                            std::max(sweep_tol, tol), st, &r, ortho_of(p)));
+                            std::max(sweep_tol, stop), st, &r, ortho_of(p)));
       inner_total += r.iterations;
       axpy_f2d_kernel<<<kVecCtas, 256, 0, st>>>(x, op->d_d32, n);
       CK(cudaGetLastError());
-      // true residual with the FP64-vector operator (FP64 near field, FP32-stored far factors)
-      CK(apply_tree<double>(op, op->plan64, x, op->d_io2, op->d_in64, op->d_y64, st));
-      CK(vec_sub_norm2<double>(b, op->d_io2, op->d_r64, n, op->d_part, op->d_scal + 1, st));
-      CK(cudaMemcpyAsync(op->h_scal, op->d_scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
-      CK(cudaStreamSynchronize(st));
-      rel = op->h_scal[1] / normb;
+      rel = true_residual(op, R, b, x, st);
       outer++;
     }
     info->iterations = inner_total;
     info->outer_iterations = outer;
     info->rel_residual = rel;
-    info->converged = rel <= tol ? 1 : 0;
+    info->rel_residual_stored = ref ? true_residual(op, op->plan64, b, x, st) : rel;
+    info->converged = rel <= stop ? 1 : 0;
   }
+  info->stop_tol = stop;
   info->seconds = now_s() - t0;
 }
+
+}  // namespace
+
+// The stream of a context (the request loop times its requests' GPU work on it).
+cudaStream_t ctx_stream(const hodlr_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
+
+namespace {
 
 int guarded(hodlr_ctx* ctx, const std::function<int()>& f) {
   try {
@@ -1218,6 +1398,7 @@ void build_finish(hodlr_op* op, BuildState& bs, cudaStream_t st) {
   if (op->p.precision == HODLR_PREC_MIXED) {
     build_near_plan(op, bs.nt32, bs.near32, Prec::kF, op->plan32, st);
     op->plan32.a_far = Prec::kF;
+    op->plan32.contig_far = op->plan64.contig_far;
     op->plan32.panels_far = op->plan64.panels_far;
     op->plan32.segs_far = op->plan64.segs_far;
     op->plan32.small_far = op->plan64.small_far;
@@ -1240,6 +1421,27 @@ void build_finish(hodlr_op* op, BuildState& bs, cudaStream_t st) {
   op->plan64.nypart = std::max(op->plan64.nypart, op->plan64.nypart_near);
   op->plan64.zpart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nzpart, 1)) * 8, "z partial sums");
   op->plan64.ypart = op->mem.alloc(size_t(std::max<int64_t>(op->plan64.nypart, 1)) * 8, "row partial sums");
+  if (op->has_ref) {
+    // the FP64 operator: the FP64 near field of plan64, the FP64 far factors
+    Plan& r = op->plan_ref;
+    const int64_t zlen = op->zlen;
+    build_far_plan(op, op->uptr64, op->vptr64, Prec::kD, r, st);
+    if (op->zlen != zlen) throw Failure{HODLR_ERR_DEVICE, "the FP64 far field has other ranks than the stored one"};
+    r.a_near = op->plan64.a_near;
+    r.panels_near = op->plan64.panels_near;
+    r.segs_near = op->plan64.segs_near;
+    r.small_near = op->plan64.small_near;
+    r.big_near = op->plan64.big_near;
+    r.nsmall_near = op->plan64.nsmall_near;
+    r.nbig_near = op->plan64.nbig_near;
+    r.pfix_near = op->plan64.pfix_near;
+    r.npfix_near = op->plan64.npfix_near;
+    r.nypart_near = op->plan64.nypart_near;
+    r.contig_near = op->plan64.contig_near;
+    r.nypart = std::max(r.nypart, r.nypart_near);
+    r.zpart = op->mem.alloc(size_t(std::max<int64_t>(r.nzpart, 1)) * 8, "z partial sums (FP64 reference)");
+    r.ypart = op->mem.alloc(size_t(std::max<int64_t>(r.nypart, 1)) * 8, "row partial sums (FP64 reference)");
+  }
   // work vectors; the input buffers [x | z] end in 16 bytes of padding,
   // which the streaming V^T x stage copies may read (a run of inputs is
   // copied from the 16-byte boundary below it to the one above it)
@@ -1252,6 +1454,10 @@ void build_finish(hodlr_op* op, BuildState& bs, cudaStream_t st) {
   op->d_x64 = op->mem.alloc_n<double>(size_t(n), "solution");
   op->d_r64 = op->mem.alloc_n<double>(size_t(n), "residual");
   op->d_io = op->mem.alloc_n<double>(size_t(n), "staging");
+  if (op->has_ref) {
+    op->d_rref = op->mem.alloc_n<double>(size_t(n), "refinement residual");
+    op->d_dref = op->mem.alloc_n<double>(size_t(n), "refinement correction");
+  }
   op->d_io2 = op->mem.alloc_n<double>(size_t(n), "staging");
   op->d_hb = op->mem.alloc_n<double>(size_t(n), "host staging");
   op->d_hx = op->mem.alloc_n<double>(size_t(n), "host staging");
@@ -1437,6 +1643,8 @@ void build_batch_plan(hodlr_batch& b, cudaStream_t st) {
   p.pfix_near = upload(b.mem, h.pfix_near, st, "batch near fix-ups");
   p.npfix_near = int(h.pfix_near.size());
   p.panels_far = upload(b.mem, h.panels_far, st, "batch far panels");
+  p.contig_near = small_items_contiguous(h.panels_near, h.segs_near, h.small_near, prec_size(p.a_near));
+  p.contig_far = p.a_far != Prec::kD && small_items_contiguous(h.panels_far, h.segs_far, h.small_far, prec_size(p.a_far));
   p.segs_far = upload(b.mem, h.segs_far, st, "batch far segments");
   p.small_far = upload(b.mem, h.small_far, st, "batch far items");
   p.big_far = upload(b.mem, h.big_far, st, "batch far items");
@@ -1477,9 +1685,10 @@ void batch_apply(hodlr_batch& b, const void* x, void* y, cudaStream_t st) {
   }
   CK(launch_zgemv(p.a_far, b.vec, p.zb, p.zitems, p.nzitems, p.zfix, p.nzfix, p.zpart, fin, b.ld_in, 1, st, acc));
   CK(launch_panels(p.a_near, b.vec, p.panels_near, p.segs_near, p.small_near, p.nsmall_near, p.big_near, p.nbig_near,
-                   p.pfix_near, p.npfix_near, p.ypart, b.d_in, b.ld_in, b.d_y, b.ycol, 1, 1, st));
+                   p.pfix_near, p.npfix_near, p.ypart, b.d_in, b.ld_in, b.d_y, b.ycol, 1, 1, st, Accum::kByType,
+                   p.contig_near));
   CK(launch_panels(p.a_far, b.vec, p.panels_far, p.segs_far, p.small_far, p.nsmall_far, p.big_far, p.nbig_far,
-                   p.pfix_far, p.npfix_far, p.ypart, fin, b.ld_in, b.d_y, b.ycol, 1, 1, st, acc));
+                   p.pfix_far, p.npfix_far, p.ypart, fin, b.ld_in, b.d_y, b.ycol, 1, 1, st, acc, p.contig_far));
   CK(launch_batch_combine(b.vec, b.d_inst, int(b.ops.size()), b.max_n, b.d_y, y, st));
 }
 
@@ -1535,6 +1744,9 @@ const char* params_problem(const hodlr_params& p) {
   if (p.ortho < HODLR_ORTHO_AUTO || p.ortho > HODLR_ORTHO_CGS2) return "unknown orthogonalisation";
   if (p.relax != HODLR_RELAX_AUTO && p.relax != HODLR_RELAX_OFF && p.relax != HODLR_RELAX_ALWAYS)
     return "relax must be HODLR_RELAX_AUTO, _OFF or _ALWAYS";
+  if (p.fp64_check != HODLR_FP64_CHECK_AUTO && p.fp64_check != HODLR_FP64_CHECK_OFF)
+    return "fp64_check must be HODLR_FP64_CHECK_AUTO or _OFF";
+  if (p.aca_workspace_mib < 0) return "aca_workspace_mib must not be negative";
   return nullptr;
 }
 
@@ -1604,6 +1816,7 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
   std::unique_ptr<hodlr_op> op(new hodlr_op());
   op->ctx = ctx;
   op->p = ctx->p;
+  op->has_ref = wants_ref(op->p);
   op->kd = *kernel;
   op->n = n;
   op->mem.budget = ctx->p.device_budget_bytes;
@@ -1712,6 +1925,7 @@ int hodlr_solve_device(hodlr_op* op, const double* d_b, double* d_x, int64_t nrh
     info->rel_residual = worst;
     info->converged = all_conv ? 1 : 0;
     info->stop_tol = one.stop_tol;
+    info->rel_residual_stored = std::max(info->rel_residual_stored, one.rel_residual_stored);
     return all_conv ? HODLR_OK : fail(op->ctx, HODLR_ERR_NOT_CONVERGED, "GMRES did not reach the tolerance");
   });
 }
@@ -1992,6 +2206,7 @@ int hodlr_build_batch(hodlr_ctx* ctx, int32_t count, const double* const* points
       b->ops.push_back(op);
       op->ctx = ctx;
       op->p = ctx->p;
+      op->has_ref = wants_ref(op->p);
       op->kd = kernels[i];
       op->n = n[i];
       op->keep_host_plans = true;
@@ -2089,7 +2304,7 @@ int hodlr_batch_destroy(hodlr_batch* b) {
 // takes the far field from the file instead of running ACA.
 namespace {
 constexpr char kOpMagic[8] = {'H', 'O', 'D', 'L', 'R', 'G', 'B', 0};
-constexpr uint32_t kOpVersion = 2;  // 2: hodlr_params with stored_margin
+constexpr uint32_t kOpVersion = 2;  // 2: hodlr_params with fp64_check, the FP64 factors of the check
 
 struct OpFile {
   std::FILE* f = nullptr;
@@ -2142,6 +2357,18 @@ int hodlr_op_save(const hodlr_op* op, const double* points, const char* path) {
       if (bv) CK(cudaMemcpy(buf.data() + bu, op->vptr[size_t(q)], bv, cudaMemcpyDeviceToHost));
       put(buf.data(), bu + bv);
     }
+    if (op->has_ref)  // the FP64 factors of the FP64 check, in the same order
+      for (int64_t q = 0; q < nb; q++) {
+        const FarBlock& fb = op->far[size_t(q)];
+        const int64_t m = t.count[size_t(t.gid(fb.level, fb.t))], n = t.count[size_t(t.gid(fb.level, fb.s))];
+        const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
+        if (!dn && r <= 0) continue;
+        const uint64_t bu = block_u_bytes(m, n, r, dn, Prec::kD), bv = block_v_bytes(n, r, dn, Prec::kD);
+        buf.resize(bu + bv);
+        CK(cudaMemcpy(buf.data(), op->uptr64[size_t(q)], bu, cudaMemcpyDeviceToHost));
+        if (bv) CK(cudaMemcpy(buf.data() + bu, op->vptr64[size_t(q)], bv, cudaMemcpyDeviceToHost));
+        put(buf.data(), bu + bv);
+      }
     if (std::fflush(fh.f) != 0) throw Failure{HODLR_ERR_IO, std::string("hodlr_op_save: write failed: ") + path};
     return HODLR_OK;
   });
@@ -2226,11 +2453,40 @@ int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out) {
       op->uptr[size_t(q)] = chunk + off[size_t(q)];
       op->vptr[size_t(q)] = dn ? nullptr : chunk + vo;
     }
+    CK(cudaMemcpyAsync(chunk, host.data(), std::max<uint64_t>(total, 16), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    op->has_ref = wants_ref(op->p);
+    if (op->has_ref) {  // the FP64 factors of the FP64 check
+      uint64_t total64 = 0;
+      std::vector<uint64_t> off64(size_t(nb), 0);
+      for (int64_t q = 0; q < nb; q++) {
+        const FarBlock& fb = op->far[size_t(q)];
+        const int64_t m = t.count[size_t(t.gid(fb.level, fb.t))], n = t.count[size_t(t.gid(fb.level, fb.s))];
+        const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
+        off64[size_t(q)] = total64;
+        if (!dn && r <= 0) continue;
+        total64 += block_u_bytes(m, n, r, dn, Prec::kD) + block_v_bytes(n, r, dn, Prec::kD);
+      }
+      std::vector<char> h64(std::max<uint64_t>(total64, 16), 0);
+      char* c64 = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(total64, 16), "far-field factors (FP64 reference)"));
+      op->uptr64.assign(size_t(nb), nullptr);
+      op->vptr64.assign(size_t(nb), nullptr);
+      for (int64_t q = 0; q < nb; q++) {
+        const FarBlock& fb = op->far[size_t(q)];
+        const int64_t m = t.count[size_t(t.gid(fb.level, fb.t))], n = t.count[size_t(t.gid(fb.level, fb.s))];
+        const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
+        if (!dn && r <= 0) continue;
+        const uint64_t bu = block_u_bytes(m, n, r, dn, Prec::kD), bv = block_v_bytes(n, r, dn, Prec::kD);
+        get(h64.data() + off64[size_t(q)], bu + bv);
+        op->uptr64[size_t(q)] = c64 + off64[size_t(q)];
+        op->vptr64[size_t(q)] = dn ? nullptr : c64 + off64[size_t(q)] + bu;
+      }
+      CK(cudaMemcpyAsync(c64, h64.data(), std::max<uint64_t>(total64, 16), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+    }
     char extra;
     if (std::fread(&extra, 1, 1, fh.f) == 1)
       throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: trailing bytes: ") + path};
-    CK(cudaMemcpyAsync(chunk, host.data(), std::max<uint64_t>(total, 16), cudaMemcpyHostToDevice, st));
-    CK(cudaStreamSynchronize(st));
     op->st.t_aca_s = 0.0;
     build_finish(op.get(), bs, st);
     *out = op.release();

@@ -52,6 +52,19 @@ __global__ void __launch_bounds__(kThreads) dot_partial_kernel(const T* a, const
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// partials of |sum_{s = s0}^{s1 - 1} y[s * n + i]|^2 over i
+template <typename T>
+__global__ void __launch_bounds__(kThreads) slots_partial_kernel(const T* y, int64_t n, int s0, int s1, double* part) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * int64_t(kThreads) + threadIdx.x; i < n; i += int64_t(kVecCtas) * kThreads) {
+    double v = 0.0;
+    for (int s = s0; s < s1; s++) v += to_d(y[int64_t(s) * n + i]);
+    acc += v * v;
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
 // h = <w, v_k> from part_in; w -= h v_k; part_out = partials of <w, next>.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -373,6 +386,15 @@ cudaError_t vec_norm2(const T* a, int64_t n, double* part, double* dst, cudaStre
 }
 
 template <typename T>
+cudaError_t slots_norm2(const T* y, int64_t n, int s0, int s1, double* part, double* dst, cudaStream_t st) {
+  count_launches(1);
+  slots_partial_kernel<T><<<kVecCtas, kThreads, 0, st>>>(y, n, s0, s1, part);
+  count_launches(1);
+  finish_norm_kernel<<<1, kThreads, 0, st>>>(part, dst);
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t gmres_solve(GmresWork<T>& W, const TreeMatvec<T>& A, const T* b, T* x, bool x0_zero, int restart,
                         int64_t max_iter, double tol, cudaStream_t st, GmresResult* res, Ortho ortho,
                         const std::function<void(double)>& progress) {
@@ -495,6 +517,7 @@ template cudaError_t vec_sub_norm2<double>(const double*, const double*, double*
                                            cudaStream_t);
 template cudaError_t vec_sub_norm2<float>(const float*, const float*, float*, int64_t, double*, double*, cudaStream_t);
 template cudaError_t vec_norm2<double>(const double*, int64_t, double*, double*, cudaStream_t);
+template cudaError_t slots_norm2<double>(const double*, int64_t, int, int, double*, double*, cudaStream_t);
 template cudaError_t vec_norm2<float>(const float*, int64_t, double*, double*, cudaStream_t);
 
 }  // namespace hodlr

@@ -78,5 +78,8 @@ template <typename T>
 cudaError_t vec_sub_norm2(const T* a, const T* b, T* c, int64_t n, double* part, double* dst, cudaStream_t st);
 template <typename T>
 cudaError_t vec_norm2(const T* a, int64_t n, double* part, double* dst, cudaStream_t st);
+// *dst = || sum_{s = s0}^{s1 - 1} y[s * n .. s * n + n) || (output slots of a matvec)
+template <typename T>
+cudaError_t slots_norm2(const T* y, int64_t n, int s0, int s1, double* part, double* dst, cudaStream_t st);
 
 }  // namespace hodlr

@@ -666,6 +666,267 @@ __global__ void __launch_bounds__(kSWarps * 32, HODLR_TUNE_S_MINB)
   }
 }
 
+// Phase 2, panels of at most 32 rows, when the segments of every item lie
+// in memory in segment order (the far field after its relayout in panel
+// order, the near field as assembled).  All segments of a panel have its m
+// rows, so an item's factors form one run of m-row columns (with up to 15
+// bytes of padding after each segment).  The run is streamed through a
+// per-warp ring of kLStages stages; a stage is the bytes of a run of whole
+// columns -- at most kLStageBytes, at most kLCols columns -- fetched by ONE
+// bulk copy (from the 16-byte boundary at or below its first column), and
+// the input values of those columns, gathered into the stage by the lanes
+// with 4- or 8-byte asynchronous copies (cp.async) that complete on the
+// stage's mbarrier.  Both are issued kLStages - 1 stages ahead of the
+// products, so neither the factor bytes nor the scattered inputs (read from
+// L2: x and z are small) are waited for in the loop.
+//
+// The warp plans each stage together: lane k reads the record of the k-th
+// next segment (one coalesced load per 32 segments), a warp scan places each
+// segment's columns in the stage, and every lane then fills the stage's
+// column table (the element offset of each column in the stage buffer; for
+// BF16 dense tiles its input scale) and starts the gathers of columns lane,
+// lane + 32, ...  The products then read only shared memory: lanes form
+// slices of mpad lanes (one lane per row), slice sl takes the stage's
+// columns sl, sl + slices, ..., column parity picks the accumulator.
+#ifndef HODLR_TUNE_L_STAGES
+#define HODLR_TUNE_L_STAGES 2
+#endif
+#ifndef HODLR_TUNE_L_BYTES
+#define HODLR_TUNE_L_BYTES 4096
+#endif
+#ifndef HODLR_TUNE_L_COLS
+#define HODLR_TUNE_L_COLS 128
+#endif
+#ifndef HODLR_TUNE_L_MINB
+#define HODLR_TUNE_L_MINB 5
+#endif
+constexpr int kLWarps = 4;
+constexpr int kLStages = HODLR_TUNE_L_STAGES;
+constexpr int kLStageBytes = HODLR_TUNE_L_BYTES;  // factor bytes per stage at most
+constexpr int kLCols = HODLR_TUNE_L_COLS;         // columns per stage at most
+constexpr int kLHead = 64;                        // barriers and stage descriptors
+static_assert(kLStages >= 2 && kLStages <= 4, "leaf ring: 2 to 4 stages");
+static_assert(kLStageBytes % 16 == 0 && kLStageBytes >= 512 && kLStageBytes <= 65536,
+              "leaf stage: a multiple of 16 bytes in 512 .. 65536 (column offsets are 16-bit)");
+static_assert(kLCols % 32 == 0 && kLCols <= 1024, "leaf stage columns: a multiple of 32");
+static_assert(32 + kLStages * 8 <= kLHead, "leaf ring header too small");
+// stage: factor bytes | inputs (kLCols x TX) | column offsets (kLCols x u16) | BF16 scales (kLCols x f32)
+template <typename TA, typename TX>
+__host__ __device__ constexpr int l_stage_smem() {
+  return kLStageBytes + kLCols * int(sizeof(TX)) + kLCols * 2 + (sizeof(TA) == 2 ? kLCols * 4 : 0);
+}
+template <typename TA, typename TX>
+__host__ __device__ constexpr int l_warp_smem() { return kLHead + kLStages * l_stage_smem<TA, TX>(); }
+
+__device__ __forceinline__ void cp_async_gather(void* dst, const void* src, int bytes) {
+  if (bytes == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+// the stage's mbarrier also waits for this thread's earlier cp.async copies
+// (its pending count is raised now and lowered when they land)
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.shared.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <typename TA, typename TACC>
+__global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
+    panel_leaf_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
+                      int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
+                      typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots,
+                      typename IO<TACC>::TY* __restrict__ ypart) {
+  using TX = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
+  using AC = Acc<TACC>;
+  constexpr int esz = int(sizeof(TA));
+  constexpr bool kScaled = esz == 2;
+  constexpr int kStage = l_stage_smem<TA, TX>(), kWarpSmem = l_warp_smem<TA, TX>();
+  constexpr int kXOff = kLStageBytes, kOOff = kXOff + kLCols * int(sizeof(TX)), kSOff = kOOff + kLCols * 2;
+  extern __shared__ __align__(16) unsigned char lsm[];
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int w = blockIdx.x * kLWarps + wid;
+  if (w >= nitems) return;
+  const Item it = items[w];
+  const Panel P = panels[it.panel];
+  const int m = P.m;
+  const int colb = m * esz;  // bytes per column
+  const TX* inc = in + blockIdx.y * ld_in;
+  TY* yo = y + int64_t(blockIdx.y) * nslots * ld_y + P.yoff;
+  int mpad = 1;
+  while (mpad < m) mpad <<= 1;
+  const int slices = 32 / mpad;
+  const int i = lane & (mpad - 1), sl = lane / mpad;
+  unsigned char* base = lsm + wid * kWarpSmem;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(base);
+  int2* meta = reinterpret_cast<int2*>(base + 32);  // per stage: column count, unused
+  unsigned char* ring = base + kLHead;
+  const int32_t qe = it.seg_e;
+  const char* a0 = static_cast<const char*>(segs[it.seg_b].A);  // 16-byte aligned: every segment starts on 16 bytes
+  if (lane == 0) {
+#pragma unroll
+    for (int s = 0; s < kLStages; s++) mbar_init(bar + s, 1u);
+    fence_mbar_init();
+  }
+  __syncwarp();
+
+  // next column to stage (the same in every lane): segment pq, column pj
+  int32_t pq = it.seg_b, pj = 0;
+  // Plans the stage from (pq, pj) into slot st and issues its copies; false
+  // when every column is staged.  Warp-uniform.
+  auto issue = [&](int st) -> bool {
+    if (pq >= qe) return false;
+    unsigned char* su = ring + st * kStage;
+    TX* xs = reinterpret_cast<TX*>(su + kXOff);
+    uint16_t* co = reinterpret_cast<uint16_t*>(su + kOOff);
+    float* sc = reinterpret_cast<float*>(su + kSOff);
+    int32_t sbase = 0, cols = 0, end = 0;
+    bool first = true, more = true;
+    while (more) {
+      // lane k: segment pq + k, its first column to stage (pj for k = 0)
+      const int32_t q = pq + lane;
+      int32_t K = 0, so = 0;
+      int64_t ino = 0;
+      const float* cs = nullptr;
+      if (q < qe) {
+        const Seg S = segs[q];
+        K = S.K;
+        so = int32_t(static_cast<const char*>(S.A) - a0);
+        ino = S.in_off;
+        cs = S.cscale;
+      }
+      const int32_t j0 = lane == 0 ? pj : 0;
+      const int32_t avail = max(K - j0, 0);
+      if (first) sbase = (__shfl_sync(0xffffffffu, so + j0 * colb, 0)) & ~15;
+      first = false;
+      // columns of this segment whose end stays within the stage's bytes
+      const int32_t room = sbase + kLStageBytes - so;
+      int32_t fit = room >= colb * (j0 + 1) ? room / colb - j0 : 0;
+      int32_t take = min(avail, fit);
+      // segments after the first one that is not taken whole take nothing
+      const unsigned part = __ballot_sync(0xffffffffu, take < avail || q >= qe);
+      const int stop_at = part ? __ffs(part) - 1 : 32;  // first lane not taken whole
+      if (lane > stop_at) take = 0;
+      // the column cap: exclusive prefix sum of the takes
+      int32_t pre = take;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t v = __shfl_up_sync(0xffffffffu, pre, o);
+        if (lane >= o) pre += v;
+      }
+      pre -= take;
+      take = max(0, min(take, kLCols - cols - pre));
+      // column table and gathers for this window: the taken columns in order
+      int32_t incl = pre + take;  // columns before the end of this lane's share
+      const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+      const int32_t wcols = min(total, kLCols - cols);
+      for (int c0 = 0; c0 < wcols; c0 += 32) {  // every lane takes part in the shuffles
+        const int c = c0 + lane;
+        // the lane k whose share holds column c: the last with pre_k <= c
+        int k = 0;
+#pragma unroll
+        for (int b = 16; b > 0; b >>= 1) {
+          const int32_t pk = __shfl_sync(0xffffffffu, pre, k + b);  // k + b <= 31
+          if (pk <= c) k += b;
+        }
+        const int32_t pk = __shfl_sync(0xffffffffu, pre, k);
+        const int32_t jk = __shfl_sync(0xffffffffu, j0, k) + (c - pk);
+        const int32_t sok = __shfl_sync(0xffffffffu, so, k);
+        const int64_t ink = __shfl_sync(0xffffffffu, ino, k);
+        unsigned long long csk = 0;
+        if constexpr (kScaled) csk = __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(cs), k);
+        if (c < wcols) {
+          co[cols + c] = uint16_t((sok + jk * colb - sbase) / esz);
+          cp_async_gather(xs + cols + c, inc + ink + jk, int(sizeof(TX)));
+          if constexpr (kScaled) sc[cols + c] = csk ? __ldg(reinterpret_cast<const float*>(csk) + jk) : 1.f;
+        }
+      }
+      // the last lane with columns ends the stage's bytes and moves the cursor
+      const unsigned has = __ballot_sync(0xffffffffu, take > 0);
+      if (has) {
+        const int kl = 31 - __clz(has);
+        const int32_t e = __shfl_sync(0xffffffffu, so + (j0 + take) * colb, kl);
+        const int32_t tk = __shfl_sync(0xffffffffu, take, kl), ak = __shfl_sync(0xffffffffu, avail, kl);
+        const int32_t jl = __shfl_sync(0xffffffffu, j0, kl);
+        end = e;
+        if (tk < ak) {
+          pq += kl;
+          pj = jl + tk;
+        } else {
+          pq += kl + 1;
+          pj = 0;
+        }
+      }
+      cols += wcols;
+      // another window of 32 segments only when all 32 were taken whole
+      more = has == 0xffffffffu && stop_at == 32 && cols < kLCols && pq < qe;
+    }
+    cp_async_arrive(bar + st);
+    if (lane == 0) meta[st] = make_int2(cols, 0);
+    __syncwarp();
+    if (lane == 0) {
+      // end rounded up to 16 bytes stays inside the last segment's storage
+      // (every segment occupies a multiple of 16 bytes), and end - sbase <= kLStageBytes
+      const uint32_t bytes = uint32_t(((end + 15) & ~15) - sbase);
+      fence_proxy_async();
+      mbar_expect_tx(bar + st, bytes);
+      bulk_g2s(su, a0 + sbase, bytes, bar + st);
+    }
+    return true;
+  };
+
+  int nissued = 0;
+  for (int s = 0; s < kLStages; s++) {
+    if (!issue(s)) break;
+    nissued++;
+  }
+  typename AC::A a0acc = AC::zero(), a1acc = AC::zero();
+  for (int k = 0; k < nissued; k++) {
+    const int st = k % kLStages;
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(bar + st, uint32_t(k / kLStages) & 1u));
+    if (!ok) {
+      if (lane == 0) atomicAdd(&g_stream_timeouts, 1u);
+      for (int t = k; t < nissued; t++) mbar_wait(bar + t % kLStages, uint32_t(t / kLStages) & 1u);
+      cp_async_wait_all();
+      return;
+    }
+    const int C = meta[st].x;
+    const unsigned char* sb = ring + st * kStage;
+    const TA* su = reinterpret_cast<const TA*>(sb);
+    const TX* xs = reinterpret_cast<const TX*>(sb + kXOff);
+    const uint16_t* co = reinterpret_cast<const uint16_t*>(sb + kOOff);
+    const float* sc = reinterpret_cast<const float*>(sb + kSOff);
+    if (i < m) {
+      int c = sl;
+      for (; c + slices < C; c += 2 * slices) {
+        typename AC::X x0 = AC::in(xs[c]), x1 = AC::in(xs[c + slices]);
+        if constexpr (kScaled) {
+          x0 = AC::xscale(x0, sc[c]);
+          x1 = AC::xscale(x1, sc[c + slices]);
+        }
+        AC::fma(a0acc, su[co[c] + i], x0);
+        AC::fma(a1acc, su[co[c + slices] + i], x1);
+      }
+      if (c < C) {
+        typename AC::X x0 = AC::in(xs[c]);
+        if constexpr (kScaled) x0 = AC::xscale(x0, sc[c]);
+        AC::fma(a0acc, su[co[c] + i], x0);
+      }
+    }
+    __syncwarp();  // stage k's slot is refilled for stage k + kLStages
+    if (issue(st)) nissued++;
+  }
+  typename AC::A acc = AC::add(a0acc, a1acc);
+  for (int o = mpad; o < 32; o <<= 1) acc = AC::add(acc, AC::shfl_xor(acc, o));
+  if (sl == 0 && i < m) {
+    if (it.part < 0)
+      yo[i] = TY(AC::value(acc));
+    else
+      ypart[int64_t(it.part) * tile_rows(int(sizeof(TA))) + i] = TY(AC::value(acc));
+  }
+}
+
 // Phase 2, panels of more than 32 rows: item chunk = row tile t of the
 // panel (T = 512 / sizeof(TA) rows, lane l owns rows t*T + l*RPL ..).  Every
 // segment's tile is h x K, column major with column stride h (h = the tile's
@@ -1209,9 +1470,22 @@ cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, i
 
 // FP32 and BF16 storage: the bulk-copy staged kernels
 template <typename TA, typename TACC>
+static void panels_leaf(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const void* in,
+                        int64_t ld_in, void* ypart, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st) {
+  using TI = typename IO<TACC>::TI;
+  using TY = typename IO<TACC>::TY;
+  dim3 g(unsigned((nsmall + kLWarps - 1) / kLWarps), unsigned(nrhs));
+  cudaFuncSetAttribute(panel_leaf_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       kLWarps * l_warp_smem<TA, TI>());
+  panel_leaf_kernel<TA, TACC><<<g, kLWarps * 32, kLWarps * l_warp_smem<TA, TI>(), st>>>(
+      panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots,
+      static_cast<TY*>(ypart));
+}
+
+template <typename TA, typename TACC>
 static void panels_staged(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big,
                           int nbig, const void* in, int64_t ld_in, void* ypart, void* y, int64_t ld_y, int nslots,
-                          int nrhs, cudaStream_t st) {
+                          int nrhs, cudaStream_t st, bool contig) {
   using TI = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
   if (nbig > 0) {
@@ -1224,7 +1498,9 @@ static void panels_staged(const Panel* panels, const Seg* segs, const Item* smal
         panels, segs, big, nbig, static_cast<TY*>(ypart), static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y,
         nslots);
   }
-  if (nsmall > 0) {
+  if (nsmall > 0 && contig) {
+    panels_leaf<TA, TACC>(panels, segs, small, nsmall, in, ld_in, ypart, y, ld_y, nslots, nrhs, st);
+  } else if (nsmall > 0) {
     dim3 g(unsigned((nsmall + kSWarps - 1) / kSWarps), unsigned(nrhs));
     cudaFuncSetAttribute(panel_small_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kSWarps * s_warp_smem<TA>());
@@ -1237,7 +1513,7 @@ static void panels_staged(const Panel* panels, const Seg* segs, const Item* smal
 template <typename TA, typename TACC>
 static void panels_t(const Panel* panels, const Seg* segs, const Item* small, int nsmall, const Item* big, int nbig,
                      const PanelFix* fix, int nfix, void* ypart, const void* in, int64_t ld_in, void* y, int64_t ld_y,
-                     int nslots, int nrhs, cudaStream_t st) {
+                     int nslots, int nrhs, cudaStream_t st, bool contig) {
   using TI = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
   if constexpr (sizeof(TA) == 8) {  // FP64 storage: direct loads
@@ -1247,14 +1523,17 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
                                                             static_cast<const TI*>(in), ld_in, static_cast<TY*>(y),
                                                             ld_y, nslots);
     }
-    if (nsmall > 0) {
+    if (nsmall > 0 && contig) {
+      panels_leaf<TA, TACC>(panels, segs, small, nsmall, in, ld_in, ypart, y, ld_y, nslots, nrhs, st);
+    } else if (nsmall > 0) {
       dim3 g(warps_grid(nsmall), unsigned(nrhs));
       panel_small_direct_kernel<TA, TACC><<<g, 256, 0, st>>>(panels, segs, small, nsmall, static_cast<const TI*>(in),
                                                              ld_in, static_cast<TY*>(y), ld_y, nslots,
                                                              static_cast<TY*>(ypart));
     }
   } else {
-    panels_staged<TA, TACC>(panels, segs, small, nsmall, big, nbig, in, ld_in, ypart, y, ld_y, nslots, nrhs, st);
+    panels_staged<TA, TACC>(panels, segs, small, nsmall, big, nbig, in, ld_in, ypart, y, ld_y, nslots, nrhs, st,
+                            contig);
   }
   if (nfix > 0) {
     const int rows = int(tile_rows(int(sizeof(TA))));
@@ -1265,29 +1544,49 @@ static void panels_t(const Panel* panels, const Seg* segs, const Item* small, in
 }
 
 
+bool small_items_contiguous(const std::vector<Panel>& panels, const std::vector<Seg>& segs,
+                            const std::vector<Item>& small, int esz) {
+  for (const Item& it : small) {
+    const int64_t m = panels[size_t(it.panel)].m;
+    if (m < 1 || m > 32) return false;
+    const char* a0 = static_cast<const char*>(segs[size_t(it.seg_b)].A);
+    if (reinterpret_cast<uintptr_t>(a0) % 16 != 0) return false;
+    const char* next = a0;  // end of the previous segment's columns
+    for (int32_t q = it.seg_b; q < it.seg_e; q++) {
+      const char* a = static_cast<const char*>(segs[size_t(q)].A);
+      // each segment starts on 16 bytes after the previous one's data; offsets
+      // from the item's first segment stay far below 2^31
+      if (a < next || reinterpret_cast<uintptr_t>(a) % 16 != 0 || a - a0 > (int64_t(1) << 30)) return false;
+      next = a + m * int64_t(segs[size_t(q)].K) * esz;
+    }
+  }
+  return true;
+}
+
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
-                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st, Accum acc) {
+                          int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st, Accum acc,
+                          bool contig) {
   if (nsmall + nbig <= 0) return cudaSuccess;
   count_launches(uint64_t(nbig > 0) + uint64_t(nsmall > 0) + uint64_t(nfix > 0));
   if (a == Prec::kD && x == Prec::kD)
     panels_t<double, double>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots,
-                             nrhs, st);
+                             nrhs, st, contig);
   else if (a == Prec::kF && x == Prec::kD && acc == Accum::kCompensated)
     panels_t<float, DF>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
-                        st);
+                        st, contig);
   else if (a == Prec::kF && x == Prec::kD && acc == Accum::kRelaxed)
     panels_t<float, FH>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
-                        st);
+                        st, contig);
   else if (a == Prec::kB && x == Prec::kD && acc == Accum::kRelaxed)
     panels_t<bf16, FH>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
-                       st);
+                       st, contig);
   else if (a == Prec::kB && x == Prec::kD)
     panels_t<bf16, DF>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
-                       st);
+                       st, contig);
   else if (a == Prec::kF && x == Prec::kF)
     panels_t<float, float>(panels, segs, small, nsmall, big, nbig, fix, nfix, ypart, in, ld_in, y, ld_y, nslots, nrhs,
-                           st);
+                           st, contig);
   else
     return cudaErrorInvalidValue;
   return cudaGetLastError();

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "device.cuh"
 
 namespace hodlr {
@@ -167,10 +169,17 @@ cudaError_t launch_zgemv(Prec a, Prec x, const ZBlock* zb, const ZItem* items, i
                          void* zpart, void* in, int64_t ld_in, int nrhs, cudaStream_t st,
                          Accum acc = Accum::kByType);
 // `small` items belong to panels of at most 32 rows, `big` ones to larger panels.
+// contig: every small item's segments lie in memory in segment order, each
+// after the end of the previous one (small_items_contiguous), so that the
+// item's factors can be streamed as one byte run.
 cudaError_t launch_panels(Prec a, Prec x, const Panel* panels, const Seg* segs, const Item* small, int nsmall,
                           const Item* big, int nbig, const PanelFix* fix, int nfix, void* ypart, const void* in,
                           int64_t ld_in, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st,
-                          Accum acc = Accum::kByType);
+                          Accum acc = Accum::kByType, bool contig = false);
+// Whether the segments of every small item (panels of at most 32 rows) with
+// esz-byte elements follow one another in memory, as launch_panels' contig asks.
+bool small_items_contiguous(const std::vector<Panel>& panels, const std::vector<Seg>& segs,
+                            const std::vector<Item>& small, int esz);
 // Copy of `bytes` (a multiple of 16) from src to dst, both 16-byte aligned.
 struct CopyDesc {
   const void* src;

@@ -160,8 +160,20 @@ extern "C" int hodlr_aca_block_noalloc(const double* d_points, int64_t ld, int32
   a.bits = s->bits;
   a.lists = s->lists;
   a.out = &s->out;
-  const bool small = (m > n ? m : n) <= 256;
-  e = hodlr::launch_aca(ndim, a, s->team, small ? 1 : 0, s->team, small ? 0 : 1, st);
+  a.arena_off = 0;
+  a.arena_size = 0;
+  a.arena_used = nullptr;  // no growth: a block that needs more than cap columns reports it
+  a.queue = nullptr;
+  a.max_ctas = 0;
+  // the team hodlr_build gives a block of this size (the team size sets the
+  // summation order of the stopping rule's norms)
+  hodlr::AcaLists al;
+  for (int k = 0; k < hodlr::kAcaTeamKinds; k++) {
+    al.list[k] = s->team;
+    al.n[k] = 0;
+  }
+  al.n[hodlr::aca_team(m, n)] = 1;
+  e = hodlr::launch_aca(ndim, a, al, st);
   if (e != cudaSuccess)
     return fail(HODLR_ERR_CUDA, std::string("hodlr_aca_block_noalloc: launch: ") + cudaGetErrorString(e));
   AcaOut out;

@@ -33,12 +33,15 @@
 #include <unordered_map>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/hodlrnd.h"
 #include "tree.hpp"
 
 namespace hodlr {
 void set_thread_error(const std::string& msg);  // engine.cu: hodlr_last_error(NULL)
 }
+cudaStream_t ctx_stream(const hodlr_ctx* ctx);  // engine.cu: the context's stream
 
 namespace {
 
@@ -66,6 +69,10 @@ double prior_rank(int ndim, double eps, int64_t k) {
   return std::min(double(k), std::ceil(r));
 }
 
+// ACA workspace of a build in the request loop (MiB): builds run side by
+// side, so each keeps its transient workspace small.
+constexpr int kServerAcaMiB = 4096;
+
 struct Prediction {
   uint64_t near_bytes = 0, far_bytes = 0, vector_bytes = 0, build_bytes = 0;
   int64_t far_blocks = 0;
@@ -91,7 +98,9 @@ int predict(const hodlr_params& p, const double* pts, int64_t n, const double* l
   for (int64_t k = 0; k + 1 < int64_t(nl.leaf_ptr.size()); k++)
     for (int64_t q = nl.leaf_ptr[size_t(k)]; q < nl.leaf_ptr[size_t(k + 1)]; q++)
       near_entries += double(t.count[size_t(t.gid(L, k))]) * double(t.count[size_t(t.gid(L, nl.src[size_t(q)]))]);
-  const double fesz = p.precision == HODLR_PREC_FP64 ? 8.0 : p.precision == HODLR_PREC_BF16_FACTORS ? 2.0 : 4.0;
+  // stored factors, plus the FP64 factors a reduced-precision operator keeps for its FP64 check
+  const double fesz = (p.precision == HODLR_PREC_FP64 ? 8.0 : p.precision == HODLR_PREC_BF16_FACTORS ? 2.0 : 4.0) +
+                      (p.precision != HODLR_PREC_FP64 && p.fp64_check != HODLR_FP64_CHECK_OFF ? 8.0 : 0.0);
   double far_entries = 0, sum_mn = 0;
   for (const hodlr::FarBlock& b : far) {
     const double m = double(t.count[size_t(t.gid(b.level, b.t))]);
@@ -111,9 +120,11 @@ int predict(const hodlr_params& p, const double* pts, int64_t n, const double* l
   const double nd = double(n);
   pr.vector_bytes = uint64_t(nd * (2 * 8 + 8 * double(t.levels) + 7 * 8) + (restart + 1) * nd * vb +
                              nd * (8.0 * p.ndim + 8 + 4.0 * t.levels) + double(pr.far_blocks) * 96.0);
-  // ACA workspace during the build: FP64 factors of the blocks of one batch
-  // (bounded by the engine's 4 GiB batches)
-  pr.build_bytes = uint64_t(std::min(4294967296.0, 8.0 * (far_entries + 0.25 * sum_mn)));
+  // ACA workspace during the build: FP64 factors of the blocks of one launch,
+  // bounded by kServerAcaMiB (the server's builds set aca_workspace_mib), and
+  // the growth arena of an eighth of that
+  const double ws_cap = double(kServerAcaMiB) * 1048576.0;
+  pr.build_bytes = uint64_t(std::min(ws_cap, 8.0 * (far_entries + 0.25 * sum_mn)) + ws_cap / 8);
   *out = pr;
   return HODLR_OK;
 }
@@ -167,6 +178,7 @@ struct hodlr_server {
   std::set<uint64_t> building;      // keys whose build is running
   hodlr_server_stats st{};
   std::vector<std::thread> workers;
+  cudaEvent_t t0_event = nullptr;   // recorded at creation: the origin of the requests' device times
 
   double scale_for(int ndim, int kind) {
     auto it = far_scale.find(ndim * 16 + kind);
@@ -299,10 +311,20 @@ void execute(hodlr_server* s, Admitted& a, Done& d, std::unique_ptr<Geometry>& b
   Job& j = *a.job;
   hodlr_result& r = d.res;
   r.t_queue_s = t_admit;
-  r.predicted_bytes = a.geo ? 0 : a.reserved;
+  r.predicted_bytes = a.geo ? 0 : a.reserved - solve_extra_bytes(j) - j.pred.build_bytes;
+  r.predicted_build_bytes = a.geo ? 0 : j.pred.build_bytes;
   d.x.assign(size_t(j.n * j.nrhs), 0.0);
   Geometry* g = a.geo;
   const auto t0 = Clock::now();
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  auto mark = [&](int k) {  // event k on the geometry's stream (device times of the request)
+    if (s->p.simulate || !s->t0_event || !g || !g->ctx) return;
+    if (cudaSetDevice(s->p.device) != cudaSuccess || cudaEventCreate(&ev[k]) != cudaSuccess) {
+      ev[k] = nullptr;
+      return;
+    }
+    cudaEventRecord(ev[k], ctx_stream(g->ctx));
+  };
   if (!g) {
     built.reset(new Geometry());
     g = built.get();
@@ -317,7 +339,9 @@ void execute(hodlr_server* s, Admitted& a, Done& d, std::unique_ptr<Geometry>& b
       hodlr_params p = j.params;
       p.device = s->p.device;
       p.device_budget_bytes = 0;  // admission already accounted for it
+      if (p.aca_workspace_mib == 0) p.aca_workspace_mib = kServerAcaMiB;
       int rc = hodlr_ctx_create(&p, &g->ctx);
+      if (rc == HODLR_OK) mark(0);
       if (rc == HODLR_OK)
         rc = hodlr_build(g->ctx, j.points.data(), j.n, j.lo.data(), j.hi.data(), &j.kernel, &g->op);
       if (rc != HODLR_OK) {
@@ -335,6 +359,7 @@ void execute(hodlr_server* s, Admitted& a, Done& d, std::unique_ptr<Geometry>& b
     r.actual_bytes = g->bytes;
   } else {
     r.actual_bytes = g->bytes;
+    mark(0);
   }
   const auto t1 = Clock::now();
   r.t_build_s = std::chrono::duration<double>(t1 - t0).count();
@@ -350,6 +375,17 @@ void execute(hodlr_server* s, Admitted& a, Done& d, std::unique_ptr<Geometry>& b
     r.iterations = info.iterations;
     r.rel_residual = info.rel_residual;
     if (rc != HODLR_OK) std::strncpy(r.message, hodlr_last_error(g->ctx), sizeof(r.message) - 1);
+    mark(1);
+    if (ev[0] && ev[1] && cudaEventSynchronize(ev[1]) == cudaSuccess) {
+      float a0 = 0.f, a1 = 0.f;
+      if (cudaEventElapsedTime(&a0, s->t0_event, ev[0]) == cudaSuccess &&
+          cudaEventElapsedTime(&a1, s->t0_event, ev[1]) == cudaSuccess) {
+        r.t_device_start_s = 1e-3 * double(a0);
+        r.t_device_end_s = 1e-3 * double(a1);
+      }
+    }
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
   }
   r.t_solve_s = seconds_since(t1);
   r.t_total_s = seconds_since(j.t_submit);
@@ -450,6 +486,17 @@ int hodlr_server_create(const hodlr_server_params* params, hodlr_server** out) {
   s->p = *params;
   if (s->p.slots == 0) s->p.slots = 4;
   if (s->p.memory_budget_bytes == 0) s->p.memory_budget_bytes = uint64_t(150) << 30;
+  if (!s->p.simulate) {
+    cudaError_t e = cudaSetDevice(s->p.device);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->t0_event);
+    if (e == cudaSuccess) e = cudaEventRecord(s->t0_event, nullptr);
+    if (e == cudaSuccess) e = cudaEventSynchronize(s->t0_event);
+    if (e != cudaSuccess) {
+      if (s->t0_event) cudaEventDestroy(s->t0_event);
+      delete s;
+      return fail(HODLR_ERR_CUDA, std::string("hodlr_server_create: ") + cudaGetErrorString(e));
+    }
+  }
   for (int i = 0; i < s->p.slots; i++) s->workers.emplace_back(worker, s);
   *out = s;
   return HODLR_OK;
@@ -543,6 +590,7 @@ int hodlr_server_destroy(hodlr_server* s) {
   }
   for (auto& t : s->workers) t.join();
   for (auto& kv : s->resident) destroy_geometry(kv.second.get());
+  if (s->t0_event) cudaEventDestroy(s->t0_event);
   delete s;
   return HODLR_OK;
 }

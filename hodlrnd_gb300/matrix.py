@@ -28,7 +28,8 @@ def _dp(a):
 class HODLRdD_matrix:
     def __init__(self, userkernel, gridPoints, x1, x2, *, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0,
                  precision="fp64", restart=100, tol=None, max_iter=0, device=0, device_budget_bytes=0, rank_cap=0,
-                 inner_tol=0.0, max_outer=0, ortho="auto", relax=True, relax_below=0.0, stored_margin=0.0):
+                 inner_tol=0.0, max_outer=0, ortho="auto", relax=True, relax_below=0.0, stored_margin=0.0,
+                 fp64_check=True):
         self.kernel = userkernel
         self.points = np.ascontiguousarray(gridPoints, dtype=np.float64)
         if self.points.ndim != 2:
@@ -60,6 +61,7 @@ class HODLRdD_matrix:
         p.relax = _lib.relax_code(relax)
         p.relax_below = float(relax_below)
         p.stored_margin = float(stored_margin)
+        p.fp64_check = _lib.HODLR_FP64_CHECK_AUTO if fp64_check else _lib.HODLR_FP64_CHECK_OFF
         self.params = p
         self._ctx = None
         self._op = None

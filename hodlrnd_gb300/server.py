@@ -34,7 +34,8 @@ class HodlrResult(ctypes.Structure):
                 ("rel_residual", ctypes.c_double), ("t_queue_s", ctypes.c_double), ("t_build_s", ctypes.c_double),
                 ("t_solve_s", ctypes.c_double), ("t_total_s", ctypes.c_double),
                 ("predicted_bytes", ctypes.c_uint64), ("actual_bytes", ctypes.c_uint64),
-                ("message", ctypes.c_char * 128)]
+                ("predicted_build_bytes", ctypes.c_uint64), ("t_device_start_s", ctypes.c_double),
+                ("t_device_end_s", ctypes.c_double), ("message", ctypes.c_char * 128)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "message"}
@@ -76,7 +77,7 @@ def _bind():
 
 def make_params(ndim, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0, precision="fp64", restart=100, tol=None,
                 max_iter=0, inner_tol=0.0, max_outer=0, ortho="auto", relax=True, relax_below=0.0,
-                stored_margin=0.0):
+                stored_margin=0.0, fp64_check=True):
     L = _lib.lib()
     p = _lib.HodlrParams()
     L.hodlr_params_default(ctypes.byref(p))
@@ -96,6 +97,7 @@ def make_params(ndim, Nmax=64, eps_ACA=1e-10, INTERACTION_TYPE_ALLOWED=0, precis
     p.relax = _lib.relax_code(relax)
     p.relax_below = float(relax_below)
     p.stored_margin = float(stored_margin)
+    p.fp64_check = _lib.HODLR_FP64_CHECK_AUTO if fp64_check else _lib.HODLR_FP64_CHECK_OFF
     return p
 
 

@@ -93,12 +93,12 @@ typedef struct hodlr_params {
   int32_t relax;     /* FP32_FACTORS, BF16_FACTORS: HODLR_RELAX_AUTO, _OFF or _ALWAYS */
   double relax_below; /* FP32_FACTORS, BF16_FACTORS: relative residual estimate below which products
                          are relaxed (<= 0: the default, tol * 1e5) */
-  double stored_margin; /* the solve ends when the true residual with the stored operator is at most
-                           tol * stored_margin (<= 0: the default, 0.5 for FP32_FACTORS and MIXED, 1 for
-                           FP64 and BF16_FACTORS).  FP32-stored factors differ from the FP64 operator by
-                           their rounding (about 5e-9 relative at eps_aca 1e-8); the margin keeps the
-                           residual against the FP64 operator at most tol as well.  BF16's rounding
-                           (about 1e-3) is beyond any margin.  No counterpart in the reference. */
+  int32_t fp64_check; /* FP32_FACTORS, BF16_FACTORS, MIXED: HODLR_FP64_CHECK_AUTO (on) or _OFF */
+  int32_t aca_workspace_mib; /* FP64 workspace of one ACA launch, MiB (0: a quarter of the free device
+                                memory, 4 to 64 GiB); blocks beyond it go to further launches.  Freed
+                                when the build returns.  No counterpart in the reference. */
+  double stored_margin; /* with the FP64 check off: a solve ends when the true residual with the stored
+                           operator is at most tol * stored_margin (<= 0: 1) */
 } hodlr_params;
 
 /* FP32_FACTORS and BF16_FACTORS solves: once GMRES's residual estimate is
@@ -112,6 +112,20 @@ typedef struct hodlr_params {
 #define HODLR_RELAX_AUTO 0
 #define HODLR_RELAX_OFF 1
 #define HODLR_RELAX_ALWAYS 2
+
+/* Reduced-precision operators (FP32_FACTORS, BF16_FACTORS, MIXED) store
+ * rounded far-field factors; rounding moves the stored operator away from the
+ * FP64 one (about 1e-8 relative for FP32 factors at eps_aca 1e-8 and
+ * N = 262144, about 1e-3 for BF16), so a stored-operator residual of tol says
+ * little about the FP64 operator's.  With the FP64 check (the default) the
+ * build also keeps the FP64 far factors (their bytes count in device_bytes),
+ * and a solve is FP64 iterative refinement: GMRES on the stored operator,
+ * then residuals b - A x with the FP64 operator, each followed by a stored-
+ * operator GMRES solve of the correction, until the FP64 operator's residual
+ * is at most tol.  HODLR_FP64_CHECK_OFF keeps only the stored factors and
+ * ends on the stored operator's residual (see stored_margin). */
+#define HODLR_FP64_CHECK_AUTO 0
+#define HODLR_FP64_CHECK_OFF 1
 
 /* GMRES orthogonalisation.  MGS is the reference's (include/GMRES.hpp:236-240)
  * and needs i + 2 kernel launches at Arnoldi step i; CGS2 (classical
@@ -171,11 +185,13 @@ int hodlr_matvec_device(hodlr_op* op, const double* d_x, double* d_y, int64_t nr
 typedef struct hodlr_solve_info {
   int64_t iterations;       /* total inner GMRES iterations (the reference's return value, GMRES.hpp:267,294,302) */
   int64_t outer_iterations; /* iterative-refinement sweeps (1 for FP64) */
-  double rel_residual;      /* |b - A x| / |b| with A the stored operator, FP64 */
+  double rel_residual;      /* |b - A x| / |b| in FP64, with the FP64 operator (FP64, or reduced precision
+                               with the FP64 check), else with the stored operator */
   int32_t converged;         /* rel_residual <= stop_tol */
   int32_t reserved;
   double seconds;
-  double stop_tol;          /* the stored-operator residual the solve stopped at: tol * stored_margin */
+  double stop_tol;          /* the residual the solve had to reach (tol, or tol * stored_margin) */
+  double rel_residual_stored; /* reduced precision: |b - A x| / |b| with the stored operator */
 } hodlr_solve_info;
 
 /* Solve A x = b (HODLRdD_matrix::solve, include/HDD_matrix.hpp:51-62 ->
@@ -247,6 +263,11 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
 #define HODLR_TRACE_NEAR_FP32 5
 #define HODLR_TRACE_FAR_FP32 6
 #define HODLR_TRACE_COMBINE_FP32 7
+#define HODLR_TRACE_ZGEMV_REF 8    /* the same four for the FP64 operator kept by reduced-precision
+                                      operators (the refinement residuals of the FP64 check) */
+#define HODLR_TRACE_NEAR_REF 9
+#define HODLR_TRACE_FAR_REF 10
+#define HODLR_TRACE_COMBINE_REF 11
 
 typedef struct hodlr_trace {
   uint64_t launches[HODLR_TRACE_KINDS];
@@ -375,8 +396,11 @@ typedef struct hodlr_result {
   double t_build_s;          /* operator build (0 when resident) */
   double t_solve_s;          /* all right-hand sides, host copies included */
   double t_total_s;          /* submit -> completion */
-  uint64_t predicted_bytes;  /* reserved at admission for a build */
+  uint64_t predicted_bytes;  /* predicted footprint of the operator it built (0 when resident) */
   uint64_t actual_bytes;     /* the operator's device footprint */
+  uint64_t predicted_build_bytes; /* transient build workspace reserved at admission beside it */
+  double t_device_start_s;   /* the request's GPU work: first and last event on its geometry's stream, */
+  double t_device_end_s;     /* seconds from the server's creation (0 with simulate) */
   char message[128];         /* failure message, empty on success */
 } hodlr_result;
 

@@ -81,10 +81,21 @@ def test_bf16_solve_backward_error():
     x64 = M64.solve(f["b"])
     xb = Mb.solve(f["b"])
     info = Mb.last_solve
+    # FP64 iterative refinement around the BF16-operator solves: the residual
+    # with the FP64 operator reaches tol, although the stored BF16 operator
+    # is about 1e-3 away from it
     assert info["converged"] == 1 and info["rel_residual"] <= c["eps"]
+    assert info["outer_iterations"] >= 2
     nb = np.linalg.norm(f["b"])
-    assert np.linalg.norm(f["b"] - M64 * xb) <= 5e-3 * nb
-    assert np.linalg.norm(xb - x64) <= 0.1 * np.linalg.norm(x64)
+    assert np.linalg.norm(f["b"] - M64 * xb) <= c["eps"] * nb
+    assert np.linalg.norm(xb - x64) <= 1e-5 * np.linalg.norm(x64)
+    # without the check: the stored operator's residual, about 1e-3 from the FP64 one
+    Mo = build(c, f["points"], precision="bf16_factors", max_iter=400, fp64_check=False)
+    xo = Mo.solve(f["b"])
+    assert Mo.last_solve["converged"] == 1 and Mo.last_solve["rel_residual"] <= c["eps"]
+    assert np.linalg.norm(f["b"] - M64 * xo) <= 5e-3 * nb
+    assert Mo.statistics()["device_bytes"] < Mb.statistics()["device_bytes"]
+    Mo.close()
     M64.close()
     Mb.close()
 

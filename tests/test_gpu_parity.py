@@ -151,11 +151,12 @@ def test_fp32_factor_solve_reaches_tolerance():
     it64 = M64.last_solve["iterations"]
     x32 = M32.solve(f["b"])
     info = M32.last_solve
+    # the FP64 check: the solve ends on the FP64 operator's residual
     assert info["converged"] == 1 and info["rel_residual"] <= c["eps"]
-    assert abs(info["iterations"] - it64) <= 3
+    assert info["iterations"] <= it64 + 15
     assert rel(x32, x64) < 1e-5
     r = f["b"] - M64 * x32
-    assert np.linalg.norm(r) / np.linalg.norm(f["b"]) < 1e-6
+    assert np.linalg.norm(r) / np.linalg.norm(f["b"]) <= c["eps"]
     M64.close()
     M32.close()
 
@@ -236,22 +237,28 @@ def test_cgs2_orthogonalisation_matches_mgs():
 
 def test_relaxed_products_keep_the_true_residual():
     """FP32 factors: plain-FP32 products once the residual estimate allows it
-    (inexact GMRES), compensated products for the final true residual."""
+    (inexact GMRES); the true residual decides -- with the FP64 operator
+    (the FP64 check), or without the check with compensated products on the
+    stored operator."""
     c = cases.REF_CASES["hodlr3d_n4096"]
     f = dict(np.load(os.path.join(GOLDEN, "ref_hodlr3d_n4096.npz")))
+    M64 = build(c, f["points"])
     Mr = build(c, f["points"], precision="fp32_factors")
     Mc = build(c, f["points"], precision="fp32_factors", relax=False)
-    xr = Mr.solve(f["b"])
-    xc = Mc.solve(f["b"])
-    ir, ic = Mr.last_solve, Mc.last_solve
-    assert ir["converged"] == 1 and ir["rel_residual"] <= c["eps"]
-    assert ic["converged"] == 1 and ic["rel_residual"] <= c["eps"]
-    # the true residual with compensated products, recomputed here
-    r = f["b"] - Mc * xr
-    assert np.linalg.norm(r) / np.linalg.norm(f["b"]) <= c["eps"]
+    Ms = build(c, f["points"], precision="fp32_factors", fp64_check=False)
+    xr, xc, xs = Mr.solve(f["b"]), Mc.solve(f["b"]), Ms.solve(f["b"])
+    ir, ic, is_ = Mr.last_solve, Mc.last_solve, Ms.last_solve
+    nb = np.linalg.norm(f["b"])
+    for x, info in ((xr, ir), (xc, ic)):
+        assert info["converged"] == 1 and info["rel_residual"] <= c["eps"]
+        # the FP64 operator's residual, recomputed here
+        assert np.linalg.norm(f["b"] - M64 * x) <= c["eps"] * nb
     assert rel(xr, xc) < 1e-6
-    Mr.close()
-    Mc.close()
+    # no check: the stored operator's true residual, with compensated products
+    assert is_["converged"] == 1 and is_["rel_residual"] <= c["eps"]
+    assert np.linalg.norm(f["b"] - Mc * xs) <= c["eps"] * nb
+    for M in (M64, Mr, Mc, Ms):
+        M.close()
 
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32_factors", "mixed", "bf16_factors"])

@@ -34,8 +34,12 @@ def test_predict_bytes_is_monotone_and_tracks_precision():
     big = predict_bytes(cloud(16000, 3, 1), BOX3, Nmax=64, eps_ACA=1e-8)
     assert 0 < small < big
     f64 = predict_bytes(cloud(16000, 3, 1), BOX3, Nmax=64, eps_ACA=1e-8, precision="fp64")
-    f32 = predict_bytes(cloud(16000, 3, 1), BOX3, Nmax=64, eps_ACA=1e-8, precision="fp32_factors")
+    f32 = predict_bytes(cloud(16000, 3, 1), BOX3, Nmax=64, eps_ACA=1e-8, precision="fp32_factors",
+                        fp64_check=False)
     assert f32 < f64
+    # with the FP64 check the FP64 factors are kept beside the FP32 ones
+    f32c = predict_bytes(cloud(16000, 3, 1), BOX3, Nmax=64, eps_ACA=1e-8, precision="fp32_factors")
+    assert f64 < f32c
     loose = predict_bytes(cloud(16000, 3, 1), BOX3, Nmax=64, eps_ACA=1e-4)
     assert loose <= f64
 

@@ -56,6 +56,11 @@ def test_alone_and_in_the_mix_give_the_same_solutions():
     st = mix.stats()
     mix.close()
     assert st["builds"] == len(reqs) and st["resident_hits"] == len(reqs)
+    # the requests' GPU work overlapped: the device intervals (events on each
+    # geometry's stream) of at least two concurrent requests intersect
+    iv = [(info["t_device_start_s"], info["t_device_end_s"]) for _, info in xs_mix]
+    assert all(0.0 < a < b for a, b in iv)
+    assert any(iv[p][0] < iv[q][1] and iv[q][0] < iv[p][1] for p in range(len(iv)) for q in range(p + 1, len(iv)))
     for k in range(len(reqs)):
         assert np.array_equal(xs_alone[k], ref[k])
         assert np.array_equal(xs_mix[k][0], ref[k])
@@ -69,5 +74,7 @@ def test_prediction_tracks_the_measured_footprint():
     res = [srv.wait(srv.submit(r["points"], r["b"], r["kernel"], box=r["box"], **r["params"]))[1] for r in reqs]
     srv.close()
     for r in res:
-        # the reservation covers the operator (it also holds the build's workspace)
-        assert r["actual_bytes"] > 0 and r["predicted_bytes"] >= r["actual_bytes"]
+        # the reservation (predicted operator + the build's transient workspace) covers the operator
+        assert r["actual_bytes"] > 0 and r["predicted_bytes"] + r["predicted_build_bytes"] >= r["actual_bytes"]
+        # and the operator's own prediction is within a factor of 2.5 of what it holds
+        assert 0.4 <= r["predicted_bytes"] / r["actual_bytes"] <= 2.5
