@@ -105,7 +105,7 @@ struct AcaTeam {
       rb = a.bits + B.bits;
       cb = rb + nwr;
       rl = a.lists + B.lists;
-      cl = rl + cap + 2;
+      cl = rl + (B.lcap > 0 ? B.lcap : cap) + 2;  // room for the rank the block may grow to
     }
   }
 

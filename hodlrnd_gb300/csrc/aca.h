@@ -15,10 +15,11 @@ struct AcaBlockDesc {
   int64_t t_map, s_map;      // offsets into AcaArgs::lmap of the target (rows) and source (columns) node
   int32_t m, n;              // rows, columns
   int32_t cap;               // workspace columns
-  int32_t pad;
+  int32_t lcap;              // the largest rank the pivot lists hold (0: cap); a block that may grow into
+                             // the arena needs min(m, n)
   int64_t ws;                // offset (doubles) of U (m x cap) followed by V (n x cap)
   int64_t bits;              // offset (words) of the row bitmap followed by the column bitmap
-  int64_t lists;             // offset (int32) of the used-row list (cap+2) then the used-column list (cap+2)
+  int64_t lists;             // offset (int32) of the used-row list (lcap+2) then the used-column list (lcap+2)
   uint64_t seed;             // restart-heuristic generator seed
   double kscale;             // kernel scale of this block's operator; 0: AcaArgs::K.scale (batched builds
                              // run blocks of several operators in one launch)

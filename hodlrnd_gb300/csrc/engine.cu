@@ -718,7 +718,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     uint64_t acc_w = 0, acc_b = 0, acc_l = 0;
     auto take = [&](size_t g) {
       const uint64_t w = ws_need(g), bw = uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32),
-                     lw = uint64_t(2 * (cap[g] + 2));
+                     lw = uint64_t(2 * (std::min(mm[g], nn[g]) + 2));
       if (!batch.empty() && (acc_w + w > ws_doubles || acc_b + bw > bits_room || acc_l + lw > list_room ||
                              batch.size() >= max_batch))
         return false;
@@ -749,7 +749,8 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       d.m = mm[g];
       d.n = nn[g];
       d.cap = cap[g];
-      d.pad = 0;
+      // the pivot lists hold every rank the block can reach, also after it grows into the arena
+      d.lcap = std::min(mm[g], nn[g]);
       d.ws = int64_t(ow);
       d.bits = int64_t(ob);
       d.lists = int64_t(ol);
@@ -757,7 +758,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       d.kscale = joint ? op->kd.scale : 0.0;
       ow += ws_need(g);
       ob += uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32);
-      ol += uint64_t(2 * (cap[g] + 2));
+      ol += uint64_t(2 * (std::min(mm[g], nn[g]) + 2));
       team_list[size_t(aca_team(mm[g], nn[g]))].push_back(int32_t(q));
     }
     // one index array, the team kinds one after another (largest blocks first)
