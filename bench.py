@@ -266,7 +266,8 @@ def run_gb300(args):
     pts, scale = workload(n, rank)
     kern = h.Kernel("inv_r", scale, 1.0)
     box = ([0.0] * NDIM, [1.0] * NDIM)
-    common = dict(Nmax=NMAX, eps_ACA=EPS, INTERACTION_TYPE_ALLOWED=DPRIME, tol=EPS, device=local)
+    common = dict(Nmax=NMAX, eps_ACA=EPS, INTERACTION_TYPE_ALLOWED=DPRIME, tol=EPS, device=local,
+                  fp64_check=not args.no_fp64_check)
     t0 = time.perf_counter()
     M = h.HODLRdD_matrix(kern, pts, *box, precision=args.precision, **common).Assemble_matrix_operators()
     build_s = time.perf_counter() - t0
@@ -316,7 +317,8 @@ def run_gb300(args):
         engines[prec] = {"value": round(k2 / (ms / 1e3), 3), "unit": "solves/s", "steps": k2,
                          "inner_iterations": [i["iterations"] for i in inf],
                          "outer_iterations": [i["outer_iterations"] for i in inf],
-                         "rel_residual": max(i["rel_residual"] for i in inf)}
+                         "rel_residual": max(i["rel_residual"] for i in inf),
+                         "rel_residual_stored_operator": max(i["rel_residual_stored"] for i in inf)}
         if "fp64" in others and prec != "fp64":
             b0 = B[0].cpu().numpy()
             engines[prec]["rel_residual_fp64_operator"] = float(
@@ -373,12 +375,17 @@ def run_gb300(args):
                           "p99": round(float(np.percentile(step_ms, 99)), 3)},
            "solve": dict({"engine": args.precision, "inner_iterations": [i["iterations"] for i in infos],
                           "outer_iterations": [i["outer_iterations"] for i in infos],
-                          "rel_residual_stored_operator": max(i["rel_residual"] for i in infos),
-                          "stop_tol_stored_operator": infos[0]["stop_tol"], "target_rel_error": EPS}, **acc),
+                          "rel_residual_engine": max(i["rel_residual"] for i in infos),
+                          "rel_residual_stored_operator": max(i["rel_residual_stored"] for i in infos),
+                          "stop_tol": infos[0]["stop_tol"], "target_rel_error": EPS,
+                          "accuracy_check": "FP64 operator (iterative refinement with the FP64 far field)"}, **acc),
            "engines": engines,
            "matvec": matvec,
            "build": {"s": round(build_s, 3), "tree_s": round(stats["t_tree_s"], 3),
-                     "aca_s": round(stats["t_aca_s"], 3), "near_s": round(stats["t_near_s"], 3),
+                     "aca_s": round(stats["t_aca_s"], 3), "aca_kernel_s": round(stats["t_aca_kernel_s"], 3),
+                     "compact_s": round(stats["t_compact_s"], 3), "aca_entries": stats["aca_entries"],
+                     "aca_entries_per_s": round(stats["aca_entries"] / max(stats["t_aca_kernel_s"], 1e-9), 1),
+                     "near_s": round(stats["t_near_s"], 3),
                      "far_blocks": stats["n_far_blocks"], "dense_far_blocks": stats["n_dense_far_blocks"],
                      "max_rank": stats["max_rank"], "far_bytes": stats["far_bytes"],
                      "near_bytes": stats["near_bytes"], "device_bytes": stats["device_bytes"],
@@ -710,6 +717,8 @@ def run_c4(args):
                                   "FP32 factors; 1 and 64 RHS"}, "cases": {}}
     x = torch.randn(n, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(SEED))
     y = torch.empty_like(x)
+    X = torch.randn((64, n), dtype=torch.float32, device="cuda", generator=torch.Generator(device="cuda").manual_seed(SEED))
+    x0 = X[0].to(torch.float64)  # column 0 of the 64-RHS inputs, for single-RHS comparisons
     reps = max(args.steps, 3)
     engines = (("bf16_factors", 1e-4, "always"), ("fp32_factors", 1e-8, True), ("fp64", 1e-8, True))
     if args.c4_engine != "all":  # one engine alone (a small case for profiling)
@@ -723,6 +732,26 @@ def run_c4(args):
             t_build = time.perf_counter() - t0
             r = matvec_rate(M, x, y, st)
             ys[prec] = y.cpu().numpy().copy()
+            M.matvec_device(x0.data_ptr(), y.data_ptr(), 1, st.cuda_stream)
+            ys[prec + "_x0"] = y.cpu().numpy().copy()
+            tc = None
+            if prec == "bf16_factors":
+                # 64 right-hand sides on the tensor cores (tcgen05, BF16 operands, FP32 accumulation)
+                Y = torch.empty_like(X)
+                for _ in range(3):
+                    M.matvec_tc_device(X.data_ptr(), Y.data_ptr(), 64, st.cuda_stream)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record(st)
+                for _ in range(reps):
+                    M.matvec_tc_device(X.data_ptr(), Y.data_ptr(), 64, st.cuda_stream)
+                e1.record(st)
+                torch.cuda.synchronize()
+                tms = e0.elapsed_time(e1) / reps
+                ys["tc_x0"] = Y[0].double().cpu().numpy().copy()
+                tc = {"ms": round(tms, 3), "rhs_matvecs_per_s": round(64 / (tms / 1e3), 1),
+                      "operands": "BF16 factors as stored, right-hand sides split into BF16 high and low parts, "
+                                  "FP64 near field in three BF16 terms; FP32 accumulation in tensor memory"}
             s = M.statistics()
             res[prec] = {"eps_ACA": eps, "accumulation": "fp32" if relax == "always" else
                          ("fp64" if prec == "fp64" else "compensated fp32"),
@@ -731,6 +760,8 @@ def run_c4(args):
                          "far_blocks": s["n_far_blocks"], "dense_far_blocks": s["n_dense_far_blocks"],
                          "max_rank": s["max_rank"], "far_bytes": s["far_bytes"], "near_bytes": s["near_bytes"],
                          "device_bytes": s["device_bytes"]}
+            if tc is not None:
+                res[prec]["rhs64_tensor_cores"] = tc
             M.close()
         if args.c4_engine != "all":
             out["cases"][f"dprime={dp}"] = res
@@ -738,9 +769,14 @@ def run_c4(args):
         y64 = ys["fp64"]
         for prec in ("bf16_factors", "fp32_factors"):
             res[prec]["rel_diff_vs_fp64_operator"] = float(np.linalg.norm(ys[prec] - y64) / np.linalg.norm(y64))
+        if "tc_x0" in ys:
+            t0v, b0v, f0v = ys["tc_x0"], ys["bf16_factors_x0"], ys["fp64_x0"]
+            tcr = res["bf16_factors"]["rhs64_tensor_cores"]
+            tcr["rel_diff_vs_fp64_operator"] = float(np.linalg.norm(t0v - f0v) / np.linalg.norm(f0v))
+            tcr["single_rhs_bf16_rel_diff_vs_fp64_operator"] = float(np.linalg.norm(b0v - f0v) / np.linalg.norm(f0v))
+            tcr["rel_diff_vs_single_rhs_bf16"] = float(np.linalg.norm(t0v - b0v) / np.linalg.norm(b0v))
         B = HODLRdD_batch([kern], [pts], [box], Nmax=128, eps_ACA=1e-8, INTERACTION_TYPE_ALLOWED=dp,
                           precision="mixed")
-        X = torch.randn((64, n), dtype=torch.float32, device="cuda")
         Y = torch.empty_like(X)
         for _ in range(3):
             B.matvec_device(X.data_ptr(), Y.data_ptr(), 64, st.cuda_stream)
@@ -775,6 +811,8 @@ def main():
     ap.add_argument("--other-steps", type=int, default=3)
     ap.add_argument("--headline-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true",
+                    help="reduced-precision engines without the FP64 far field (stop on the stored operator)")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--workload", choices=["solve", "serving", "batch", "c4"], default="solve",
                     help="serving: replay the request trace through the request loop (its own JSON line)")

@@ -83,7 +83,8 @@ class HodlrStats(ctypes.Structure):
                [(k, ctypes.c_double) for k in ("n_flop", "memory_gb", "compression_ratio")] + \
                [(k, ctypes.c_uint64) for k in ("near_bytes", "far_bytes", "device_bytes")] + \
                [(k, ctypes.c_double) for k in ("t_tree_s", "t_aca_s", "t_near_s", "t_build_s", "t_matvec_s",
-                                               "far_entries", "dense_far_entries", "near_entries")]
+                                               "far_entries", "dense_far_entries", "near_entries",
+                                               "t_aca_kernel_s", "t_compact_s", "aca_entries")]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -152,6 +153,10 @@ def lib():
     L.hodlr_op_load.argtypes = [P, ctypes.c_char_p, ctypes.POINTER(P)]
     L.hodlr_vec_load.argtypes = [ctypes.c_char_p, D, ctypes.c_int64, I64]
     L.hodlr_vec_save.argtypes = [ctypes.c_char_p, D, ctypes.c_int64]
+    L.hodlr_matvec_tc_device.argtypes = [P, P, P, ctypes.c_int64, P]
+    L.hodlr_matvec_tc_device.restype = ctypes.c_int
+    L.hodlr_tc_selftest.argtypes = [P, P, ctypes.c_int32, ctypes.c_int32, P]
+    L.hodlr_tc_selftest.restype = ctypes.c_int
     for f in ("hodlr_op_save", "hodlr_op_load", "hodlr_set_relax", "hodlr_vec_load", "hodlr_vec_save", "hodlr_ctx_create", "hodlr_ctx_destroy", "hodlr_build", "hodlr_op_destroy", "hodlr_matvec",
               "hodlr_matvec_device", "hodlr_solve", "hodlr_solve_device", "hodlr_stats_get",
               "hodlr_get_permutation", "hodlr_get_blocks", "hodlr_tree_build", "hodlr_tree_sizes",

@@ -17,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhodlrnd_gb300.so")
-SOURCES = ["tree.cpp", "aca.cu", "matvec.cu", "gmres.cu", "engine.cu", "noalloc.cu", "vecio.cpp", "server.cpp"]
+SOURCES = ["tree.cpp", "aca.cu", "matvec.cu", "gmres.cu", "engine.cu", "noalloc.cu", "vecio.cpp", "server.cpp",
+           "tcgen05.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = "-fPIC,-fopenmp,-ffp-contract=off,-O2"
 

@@ -16,6 +16,7 @@
 #include "aca.h"
 #include "gmres.h"
 #include "matvec.h"
+#include "tc.h"
 #include "tree.hpp"
 
 using namespace hodlr;
@@ -220,6 +221,21 @@ struct hodlr_op {
   bool has_ref = false;
   std::vector<const void*> uptr64, vptr64;
   Plan plan_ref;
+  // tensor-core products for 64 right-hand sides (BF16 factors; built on first use)
+  struct TcPlan {
+    bool built = false;
+    Item *near_small = nullptr, *near_big = nullptr, *far_small = nullptr, *far_big = nullptr;
+    int n_near_small = 0, n_near_big = 0, n_far_small = 0, n_far_big = 0;
+    int max_near_small = 0, max_near_big = 0, max_far_small = 0, max_far_big = 0;  // rows of the largest item
+    PanelFix *fix_near = nullptr, *fix_far = nullptr;
+    int nfix_near = 0, nfix_far = 0;
+    TcZGroup* zg = nullptr;
+    TcZEntry* ze = nullptr;
+    int nzg = 0, max_zg = 0;
+    float *in = nullptr, *y = nullptr, *part_near = nullptr, *part_far = nullptr;
+    unsigned int* status = nullptr;
+    unsigned int* h_status = nullptr;
+  } tc;
   int64_t n = 0, zlen = 0;
   int nslots = 0;
   DevMem mem;
@@ -257,6 +273,7 @@ struct hodlr_op {
     gmres_free(g32);
     if (h_scal) cudaFreeHost(h_scal);
     if (h_waits) cudaFreeHost(h_waits);
+    if (tc.h_status) cudaFreeHost(tc.h_status);
     mem.release_all();
   }
 };
@@ -706,6 +723,28 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   });
 
   KernelDev K{op0->kd.kind, op0->kd.scale, op0->kd.diag};
+  struct Events {
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    ~Events() {
+      for (cudaEvent_t x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } evs;
+  check_cuda(cudaEventCreate(&evs.e[0]), "cudaEventCreate");
+  check_cuda(cudaEventCreate(&evs.e[1]), "cudaEventCreate");
+  cudaEvent_t ev_a0 = evs.e[0], ev_a1 = evs.e[1];
+  double t_kernel = 0.0, t_compact = 0.0;
+  // device times shared by every operator of the launch
+  struct Report {
+    const std::vector<hodlr_op*>& ops;
+    double &tk, &tc;
+    ~Report() {
+      for (hodlr_op* op : ops) {
+        op->st.t_aca_kernel_s = tk;
+        op->st.t_compact_s = tc;
+      }
+    }
+  } report{ops, t_kernel, t_compact};
   size_t pos = 0;
   std::vector<size_t> retry;
   std::vector<AcaBlockDesc> desc;
@@ -797,10 +836,17 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       al.list[k] = d_lists_idx + lpos[k];
       al.n[k] = int(team_list[size_t(k)].size());
     }
+    CK(cudaEventRecord(ev_a0, st));
     CK(launch_aca(ndim, a, al, st));
+    CK(cudaEventRecord(ev_a1, st));
     out.resize(batch.size());
     CK(cudaMemcpyAsync(out.data(), d_out, out.size() * sizeof(AcaOut), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
+      t_kernel += 1e-3 * double(ms);
+    }
     // compaction of the finished blocks: one chunk per operator and batch
     cds.clear();
     std::vector<uint64_t> bytes(nops, 0), off(batch.size(), 0);
@@ -860,8 +906,13 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     for (size_t b0 = 0; b0 < cds.size(); b0 += max_cd) {
       const size_t k = std::min(max_cd, cds.size() - b0);
       CK(cudaMemcpyAsync(d_cd, cds.data() + b0, k * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
+      CK(cudaEventRecord(ev_a0, st));
       CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(k), fp, st));
+      CK(cudaEventRecord(ev_a1, st));
       CK(cudaStreamSynchronize(st));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
+      t_compact += 1e-3 * double(ms);
     }
     // the FP64 factors of the same blocks, for operators that keep them
     if (fp != Prec::kD) {
@@ -916,8 +967,13 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
         for (size_t b0 = 0; b0 < cd64.size(); b0 += max_cd) {
           const size_t k = std::min(max_cd, cd64.size() - b0);
           CK(cudaMemcpyAsync(d_cd, cd64.data() + b0, k * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
+          CK(cudaEventRecord(ev_a0, st));
           CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(k), Prec::kD, st));
+          CK(cudaEventRecord(ev_a1, st));
           CK(cudaStreamSynchronize(st));
+          float ms = 0.f;
+          CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
+          t_compact += 1e-3 * double(ms);
         }
       }
     }
@@ -935,6 +991,7 @@ void compute_stats(hodlr_op* op) {
   s.n_dense_far_blocks = 0;
   s.max_rank = 0;
   s.far_entries = s.dense_far_entries = s.near_entries = 0;
+  s.aca_entries = 0;
   double flop = 0.0;
   const int L = t.levels - 1;
   for (int64_t k = 0; k < t.level_size[size_t(L)]; k++) {
@@ -950,6 +1007,8 @@ void compute_stats(hodlr_op* op) {
     const double m = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].t))]);
     const double n = double(t.count[size_t(t.gid(op->far[b].level, op->far[b].s))]);
     flop += double(op->rank[b]) * (m + n);
+    // the ACA generates one residual row and column per step, one more for the stopping step
+    s.aca_entries += double(op->rank[b] + 1) * (m + n);
     s.max_rank = std::max<int64_t>(s.max_rank, op->rank[b]);
     if (op->dense[b]) {
       s.n_dense_far_blocks++;
@@ -1729,6 +1788,152 @@ void batch_apply_mr(hodlr_batch& b, const float* x, float* y, int64_t nrhs, cuda
   CK(launch_batch_combine_mr(b.d_inst, count, b.max_n, b.d_y_mr, b.ycol, y, b.total_n, int(nrhs), nch, st));
 }
 
+// ---- tensor-core products for 64 right-hand sides ---------------------------
+
+// Items of the tensor-core panel kernels for one family of panels: per panel,
+// its row tiles (one for panels of at most 32 rows) times runs of at most
+// kTcSegsPerItem segments (runs after the first write partial row blocks that
+// a fix-up adds in order).
+constexpr int kTcSegsPerItem = 1024;
+static_assert(kTcSegsPerItem < kTcMaxSegs, "the tensor-core kernels hold the column starts of an item's segments");
+void tc_panel_items(const std::vector<Panel>& panels, int tile_rows, std::vector<Item>& small, std::vector<Item>& big,
+                    int& max_small, int& max_big, std::vector<PanelFix>& fix, int& nparts) {
+  for (size_t pi = 0; pi < panels.size(); pi++) {
+    const Panel& P = panels[pi];
+    const int64_t ns = P.seg_end - P.seg_begin;
+    if (ns <= 0 || P.m <= 0) continue;
+    const int runs = int((ns + kTcSegsPerItem - 1) / kTcSegsPerItem);
+    const bool is_big = P.m > 32;
+    const int tiles = is_big ? int((P.m + tile_rows - 1) / tile_rows) : 1;
+    for (int tl = 0; tl < tiles; tl++) {
+      const int rows = is_big ? std::min<int>(tile_rows, P.m - tl * tile_rows) : P.m;
+      (is_big ? max_big : max_small) = std::max(is_big ? max_big : max_small, rows);
+      if (runs > 1) fix.push_back({int32_t(pi), tl, nparts, runs});
+      for (int q = 0; q < runs; q++) {
+        Item it;
+        it.panel = int32_t(pi);
+        it.chunk = tl;
+        it.seg_b = int32_t(P.seg_begin + int64_t(q) * kTcSegsPerItem);
+        it.seg_e = int32_t(std::min<int64_t>(P.seg_end, P.seg_begin + int64_t(q + 1) * kTcSegsPerItem));
+        it.part = runs > 1 ? nparts++ : -1;
+        (is_big ? big : small).push_back(it);
+      }
+    }
+  }
+}
+
+void build_tc_plan(hodlr_op* op, cudaStream_t st) {
+  hodlr_op::TcPlan& T = op->tc;
+  if (T.built) return;
+  if (!op->plan64.host) throw Failure{HODLR_ERR_STATE, "the operator keeps no host plan for the tensor-core path"};
+  const Plan::Host& h = *op->plan64.host;
+  std::vector<Item> ns, nb, fs, fb;
+  std::vector<PanelFix> fxn, fxf;
+  int pn = 0, pf = 0;
+  tc_panel_items(h.panels_near, int(tile_rows(8)), ns, nb, T.max_near_small, T.max_near_big, fxn, pn);
+  tc_panel_items(h.panels_far, int(tile_rows(2)), fs, fb, T.max_far_small, T.max_far_big, fxf, pf);
+  // z groups: the low-rank blocks by source node (consecutive in the sorted
+  // order), at most 256 rows per group
+  std::vector<int32_t> order(h.zb.size());
+  for (size_t q = 0; q < order.size(); q++) order[q] = int32_t(q);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t x, int32_t y) { return h.zb[size_t(x)].x_off < h.zb[size_t(y)].x_off; });
+  std::vector<TcZGroup> zg;
+  std::vector<TcZEntry> ze;
+  for (size_t q = 0; q < order.size();) {
+    const ZBlock& z0 = h.zb[size_t(order[q])];
+    TcZGroup g{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0};
+    while (q < order.size() && h.zb[size_t(order[q])].x_off == z0.x_off) {
+      const ZBlock& z = h.zb[size_t(order[q])];
+      for (int32_t k0 = 0; k0 < z.r;) {
+        const int32_t take = std::min(z.r - k0, 256 - g.rows);
+        ze.push_back({order[q], k0, take});
+        g.rows += take;
+        k0 += take;
+        if (g.rows == 256) {  // close the group, continue with a new one on the same source
+          g.e_end = int32_t(ze.size());
+          T.max_zg = std::max(T.max_zg, g.rows);
+          zg.push_back(g);
+          g = TcZGroup{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0};
+        }
+      }
+      q++;
+    }
+    if (g.rows > 0) {
+      g.e_end = int32_t(ze.size());
+      T.max_zg = std::max(T.max_zg, g.rows);
+      zg.push_back(g);
+    }
+  }
+  T.near_small = upload(op->mem, ns, st, "tensor-core near items");
+  T.near_big = upload(op->mem, nb, st, "tensor-core near items");
+  T.far_small = upload(op->mem, fs, st, "tensor-core far items");
+  T.far_big = upload(op->mem, fb, st, "tensor-core far items");
+  T.n_near_small = int(ns.size());
+  T.n_near_big = int(nb.size());
+  T.n_far_small = int(fs.size());
+  T.n_far_big = int(fb.size());
+  T.fix_near = upload(op->mem, fxn, st, "tensor-core near fix-ups");
+  T.fix_far = upload(op->mem, fxf, st, "tensor-core far fix-ups");
+  T.nfix_near = int(fxn.size());
+  T.nfix_far = int(fxf.size());
+  T.zg = upload(op->mem, zg, st, "tensor-core z groups");
+  T.ze = upload(op->mem, ze, st, "tensor-core z entries");
+  T.nzg = int(zg.size());
+  const int64_t n = op->n;
+  T.in = op->mem.alloc_n<float>(size_t(n + op->zlen) * kTcRhs, "tensor-core input (64 right-hand sides)");
+  T.y = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots) * kTcRhs, "tensor-core output slots");
+  T.part_near = op->mem.alloc_n<float>(size_t(std::max(pn, 1)) * tile_rows(8) * kTcRhs, "tensor-core partial rows");
+  T.part_far = op->mem.alloc_n<float>(size_t(std::max(pf, 1)) * tile_rows(2) * kTcRhs, "tensor-core partial rows");
+  T.status = op->mem.alloc_n<unsigned int>(1, "tensor-core status");
+  CK(cudaMemsetAsync(T.status, 0, sizeof(unsigned int), st));
+  CK(cudaMallocHost(&T.h_status, sizeof(unsigned int)));
+  CK(cudaStreamSynchronize(st));
+  T.built = true;
+}
+
+// Y = A X for up to 64 columns of X (caller order, column major, FP32).
+void apply_tc(hodlr_op* op, const float* x, int64_t ldx, float* y, int64_t ldy, int nrhs, cudaStream_t st) {
+  hodlr_op::TcPlan& T = op->tc;
+  const Plan& P = op->plan64;
+  const int64_t n = op->n;
+  CK(launch_tc_gather(x, ldx, nrhs, op->d_perm, n, T.in, st));
+  CK(cudaMemsetAsync(T.y, 0, sizeof(float) * size_t(n) * size_t(op->nslots) * kTcRhs, st));
+  TcLaunch a{};
+  a.in = T.in;
+  a.y = T.y;
+  a.n = n;
+  a.status = T.status;
+  // z = V^T x, grouped by source node
+  a.zb = P.zb;
+  a.zgroups = T.zg;
+  a.zentries = T.ze;
+  a.nz = T.nzg;
+  a.nmax = T.max_zg;
+  CK(launch_tc(kTcZ, a, st));
+  a.nz = 0;
+  // near field (FP64 tiles, three BF16 terms), then the far field (BF16)
+  a.panels = P.panels_near;
+  a.segs = P.segs_near;
+  a.part = T.part_near;
+  a.tile_rows = int(tile_rows(8));
+  a.items = T.near_small, a.nitems = T.n_near_small, a.big = 0, a.nmax = T.max_near_small;
+  CK(launch_tc(kTcNear, a, st));
+  a.items = T.near_big, a.nitems = T.n_near_big, a.big = 1, a.nmax = T.max_near_big;
+  CK(launch_tc(kTcNear, a, st));
+  CK(launch_tc_fix(P.panels_near, T.fix_near, T.nfix_near, int(tile_rows(8)), T.part_near, T.y, n, st));
+  a.panels = P.panels_far;
+  a.segs = P.segs_far;
+  a.part = T.part_far;
+  a.tile_rows = int(tile_rows(2));
+  a.items = T.far_small, a.nitems = T.n_far_small, a.big = 0, a.nmax = T.max_far_small;
+  CK(launch_tc(kTcFar, a, st));
+  a.items = T.far_big, a.nitems = T.n_far_big, a.big = 1, a.nmax = T.max_far_big;
+  CK(launch_tc(kTcFar, a, st));
+  CK(launch_tc_fix(P.panels_far, T.fix_far, T.nfix_far, int(tile_rows(2)), T.part_far, T.y, n, st));
+  CK(launch_tc_combine(T.y, op->nslots, n, op->d_perm, y, ldy, nrhs, st));
+}
+
 // Why the parameters cannot be used (null when they can): the checks of
 // hodlr_ctx_create, applied again to the parameters read from an operator file.
 const char* params_problem(const hodlr_params& p) {
@@ -1818,6 +2023,7 @@ int hodlr_build(hodlr_ctx* ctx, const double* points, int64_t n, const double* b
   op->ctx = ctx;
   op->p = ctx->p;
   op->has_ref = wants_ref(op->p);
+  op->keep_host_plans = op->p.precision == HODLR_PREC_BF16_FACTORS;  // the tensor-core plan is built from them
   op->kd = *kernel;
   op->n = n;
   op->mem.budget = ctx->p.device_budget_bytes;
@@ -1953,6 +2159,30 @@ int hodlr_solve(hodlr_op* op, const double* b, double* x, int64_t nrhs, hodlr_so
       op->mem.release(dx);
     }
     return rc;
+  });
+}
+
+int hodlr_matvec_tc_device(hodlr_op* op, const float* d_x, float* d_y, int64_t nrhs, void* stream) {
+  if (!op || !d_x || !d_y) return fail(op ? op->ctx : nullptr, HODLR_ERR_INVALID, "hodlr_matvec_tc_device: null argument");
+  if (nrhs < 1) return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_matvec_tc_device: nrhs must be positive");
+  if (op->p.precision != HODLR_PREC_BF16_FACTORS)
+    return fail(op->ctx, HODLR_ERR_INVALID, "hodlr_matvec_tc_device: the operator must store BF16 factors");
+  return guarded(op->ctx, [&]() -> int {
+    CK(cudaSetDevice(op->p.device));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    build_tc_plan(op, st);
+    const int64_t n = op->n;
+    for (int64_t c = 0; c < nrhs; c += kTcRhs) {
+      const int k = int(std::min<int64_t>(kTcRhs, nrhs - c));
+      apply_tc(op, d_x + c * n, n, d_y + c * n, n, k, st);
+    }
+    CK(cudaMemcpyAsync(op->tc.h_status, op->tc.status, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (*op->tc.h_status != 0) {
+      CK(cudaMemsetAsync(op->tc.status, 0, sizeof(unsigned int), st));
+      throw Failure{HODLR_ERR_DEVICE, "a tensor-core kernel gave up waiting for its MMAs; the results are invalid"};
+    }
+    return HODLR_OK;
   });
 }
 
@@ -2407,6 +2637,7 @@ int hodlr_op_load(hodlr_ctx* ctx, const char* path, hodlr_op** out) {
         op->kd.kind > HODLR_KERNEL_EXP_NEG_R || !std::isfinite(op->kd.scale) || !std::isfinite(op->kd.diag))
       throw Failure{HODLR_ERR_IO, std::string("hodlr_op_load: corrupt header (") +
                                       (why ? why : "point count or kernel out of range") + "): " + path};
+    op->keep_host_plans = op->p.precision == HODLR_PREC_BF16_FACTORS;  // for the tensor-core plan
     std::memset(&op->st, 0, sizeof(op->st));
     std::vector<double> pts(size_t(op->n) * size_t(d)), lo(static_cast<size_t>(d)), hi(static_cast<size_t>(d));
     get(pts.data(), sizeof(double) * pts.size());

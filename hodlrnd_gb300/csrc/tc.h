@@ -1,0 +1,77 @@
+// Tensor-core products of the HODLR operator for 64 right-hand sides at once
+// (tcgen05.cu).
+//
+// Vectors are "point major": entry p of a 64-column block sits at
+// v[p * 64 .. p * 64 + 63] (FP32), for the inputs [x | z] (tree positions,
+// then the z values of the low-rank blocks) and for the output slots.  Each
+// product is D (128 x N) = A (128 x K) B^T on the tensor cores: A holds the 64
+// right-hand sides split into BF16 high and low parts (rows 0-63 and 64-127,
+// x = hi + lo to about 2^-17 relative), B the factor columns (N output rows,
+// K input columns in steps of 16), D the FP32 accumulator in tensor memory;
+// the result is D_hi + D_lo.  BF16 factors are taken as they are stored; FP64
+// near-field entries are split into three BF16 terms (about 2^-24 relative).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "matvec.h"
+
+namespace hodlr {
+
+constexpr int kTcRhs = 64;     // right-hand sides per block
+constexpr int kTcMaxSegs = 2048;  // segments of one panel item (the host splits longer items)
+
+// kind of product: z = V^T x (one item per low-rank block), near-field panels
+// (FP64 tiles), far-field panels (BF16 dense tiles and U factors)
+enum TcKind { kTcZ = 0, kTcNear = 1, kTcFar = 2 };
+
+// z = V^T x for the low-rank blocks with one source node, grouped: the
+// group's rows are rows k0 .. k0 + nk - 1 of z_b for each of its entries
+// (at most 256 rows in all), and its columns the source node's points.
+struct TcZEntry {
+  int32_t zb;      // index into the z blocks
+  int32_t k0, nk;  // rows (columns of V) of z_b in this group
+};
+struct TcZGroup {
+  int64_t x_off;   // first point of the source node
+  int32_t n;       // points of the source node (the columns)
+  int32_t e_begin, e_end;  // entries
+  int32_t rows;    // sum of nk
+};
+
+struct TcLaunch {
+  float* in;        // [x | z], point major
+  float* y;         // output slots, point major: slot s of row p at (s * n + p) * 64
+  float* part;      // partial row blocks of split panels: (part * rows_per_item + i) * 64
+  int64_t n;        // points (rows of one slot)
+  unsigned int* status;  // wait give-ups
+  // panels (near, far)
+  const Panel* panels;
+  const Seg* segs;
+  const Item* items;
+  int nitems;
+  int big;          // items are row tiles of panels above 32 rows
+  int tile_rows;    // rows of one tile of the stored precision (big items)
+  // z products: blocks, groups by source node, group entries
+  const ZBlock* zb;
+  const TcZGroup* zgroups;
+  const TcZEntry* zentries;
+  int nz;           // groups
+  int nmax;         // largest output row count of the launch's items (N before padding)
+};
+
+// One launch per kind (and small / big items); asynchronous on st.
+cudaError_t launch_tc(TcKind kind, const TcLaunch& a, cudaStream_t st);
+// in[p * 64 + r] = x[perm[p] + r * ld_x] (x in caller order, column major FP32), p < n, r < nrhs (<= 64);
+// columns r >= nrhs are zero
+cudaError_t launch_tc_gather(const float* x, int64_t ld_x, int nrhs, const int64_t* perm, int64_t n, float* in,
+                             cudaStream_t st);
+// y_out[perm[p] + r * ld_out] = sum over slots s of y[(s * n + p) * 64 + r], r < nrhs
+cudaError_t launch_tc_combine(const float* y, int nslots, int64_t n, const int64_t* perm, float* out,
+                              int64_t ld_out, int nrhs, cudaStream_t st);
+// adds split panels' partial row blocks into their output rows (fix-up, as panel_fix_kernel)
+cudaError_t launch_tc_fix(const Panel* panels, const PanelFix* fix, int nfix, int rows_per_item, const float* part,
+                          float* y, int64_t n, cudaStream_t st);
+
+}  // namespace hodlr

@@ -166,6 +166,13 @@ class HODLRdD_matrix:
         _lib.check(_lib.lib().hodlr_matvec_device(self._op, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), nrhs,
                                                   ctypes.c_void_p(stream)), self._ctx)
 
+    def matvec_tc_device(self, x_ptr, y_ptr, nrhs, stream=0):
+        """Y = A X on the tensor cores (hodlr_matvec_tc_device): BF16 factors,
+        FP32 n x nrhs column-major device arrays; synchronises `stream`."""
+        self._need_op()
+        _lib.check(_lib.lib().hodlr_matvec_tc_device(self._op, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr),
+                                                     int(nrhs), ctypes.c_void_p(stream)), self._ctx)
+
     def solve(self, b, *, out=None, raise_on_stall=False):
         """x with A x = b (HODLRdD_matrix::solve): FP64 GMRES with x0 = b, or
         FP64 iterative refinement around FP32 GMRES in mixed precision.

@@ -225,6 +225,9 @@ typedef struct hodlr_stats {
   double far_entries;       /* sum over low-rank blocks of r (m + n) */
   double dense_far_entries; /* sum over dense far blocks of m n */
   double near_entries;      /* sum over near blocks of m n */
+  double t_aca_kernel_s;    /* device time of the ACA launches (inside t_aca_s) */
+  double t_compact_s;       /* device time of the factor compaction launches (inside t_aca_s) */
+  double aca_entries;       /* kernel entries the ACA generated: sum over blocks of (r + 1)(m + n) */
 } hodlr_stats;
 
 /* print_matrix_statistics figures (include/HDD_matrix.hpp:69-85) plus byte counts. */
@@ -317,6 +320,27 @@ int hodlr_aca_block_noalloc(const double* d_points, int64_t ld, int32_t ndim, co
                             const int32_t* d_cols, int32_t n, const hodlr_kernel_desc* kernel, double eps_aca,
                             uint64_t seed, int32_t cap, double* d_factors, int32_t* rank, int32_t* flags,
                             void* stream);
+
+/* Y = A X for several right-hand sides on the tensor cores: an operator with
+ * BF16 far-field factors (HODLR_PREC_BF16_FACTORS), X and Y device arrays of
+ * n x nrhs FP32, column major, caller's point order.  Blocks of 64 columns
+ * go through tcgen05 MMAs (BF16 operands, FP32 accumulation in tensor
+ * memory): every right-hand side split into BF16 high and low parts (to about
+ * 2^-17 relative), the BF16 factors as stored, the FP64 near field in three
+ * BF16 terms -- the product differs from the stored operator's FP32 product
+ * by about 1e-5 relative, far below the BF16 storage itself (about 1e-3).
+ * The first call builds the tensor-core plan and buffers (about n + sum of
+ * ranks times 256 bytes).  Synchronises `stream`.  Replaces the mat-mat use
+ * of HODLRdD_matrix::operator* (include/HDD_matrix.hpp:42-47). */
+int hodlr_matvec_tc_device(hodlr_op* op, const float* d_x, float* d_y, int64_t nrhs, void* stream);
+
+/* ---- tensor cores ---------------------------------------------------------
+ * Self-test of the fifth-generation tensor-core path (tcgen05) the multi-RHS
+ * products use: D = A B^T with A (128 x k) and B (n x k) BF16, row major,
+ * given as their 16-bit patterns, D (128 x n) FP32 row major, accumulated in
+ * tensor memory.  n a multiple of 16 in 16..256, k a multiple of 16 in 16..128.
+ * Host pointers; synchronous.  No counterpart in the reference. */
+int hodlr_tc_selftest(const uint16_t* A, const uint16_t* B, int32_t n, int32_t k, float* D);
 
 /* ---- batches of independent operators ---------------------------------- */
 /* No counterpart in the reference (one HODLRdD_matrix per caller,
