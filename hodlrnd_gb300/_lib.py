@@ -145,6 +145,8 @@ def lib():
     L.hodlr_kernel_launches.argtypes = []
     L.hodlr_kernel_launches.restype = ctypes.c_uint64
     L.hodlr_tree_build.argtypes = [ctypes.POINTER(HodlrParams), D, ctypes.c_int64, D, D, ctypes.POINTER(P)]
+    L.hodlr_tree_build_device.argtypes = [ctypes.POINTER(HodlrParams), D, ctypes.c_int64, D, D, ctypes.POINTER(P)]
+    L.hodlr_tree_build_device.restype = ctypes.c_int
     L.hodlr_tree_sizes.argtypes = [P, I64]
     L.hodlr_tree_get.argtypes = [P, I64, I64, I64, I64, I64, I64, I64]
     L.hodlr_tree_destroy.argtypes = [P]

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhodlrnd_gb300.so")
 SOURCES = ["tree.cpp", "aca.cu", "matvec.cu", "gmres.cu", "engine.cu", "noalloc.cu", "vecio.cpp", "server.cpp",
-           "tcgen05.cu"]
+           "tcgen05.cu", "dtree.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = "-fPIC,-fopenmp,-ffp-contract=off,-O2"
 

@@ -14,6 +14,7 @@
 
 #include "../../include/hodlrnd.h"
 #include "aca.h"
+#include "dtree.h"
 #include "gmres.h"
 #include "matvec.h"
 #include "tc.h"
@@ -1351,23 +1352,23 @@ void build_prepare(hodlr_op* op, const double* points, const double* box_lo, con
   tp.ndim = op->p.ndim;
   tp.nmax = op->p.nmax;
   tp.dprime = op->p.dprime;
-  const std::string terr = build_tree(tp, points, n, box_lo, box_hi, op->tree);
-  if (!terr.empty())
-    throw Failure{terr.find("exceeds") != std::string::npos ? HODLR_ERR_TREE : HODLR_ERR_INVALID,
-                  "hodlr_build: " + terr};
+  // the tree, its lists, the points in tree order, the permutation and the
+  // reference-order maps, built on the device
+  const int d = op->p.ndim;
+  op->d_pts = op->mem.alloc_n<double>(size_t(n) * size_t(d), "points");
+  op->d_perm = op->mem.alloc_n<int64_t>(size_t(n), "permutation");
+  DeviceTreeOut dto;
+  dto.d_pts = op->d_pts;
+  dto.d_perm = op->d_perm;
+  dto.alloc_lmap = [op](size_t k) { return op->mem.alloc_n<int32_t>(k, "reference-order map"); };
+  const DeviceTreeStatus ds = build_tree_device(tp, points, n, box_lo, box_hi, op->tree, dto, st);
+  if (ds.code != 0) throw Failure{ds.code, "hodlr_build: " + ds.msg};
+  op->d_lmap = dto.d_lmap;
   op->far = far_blocks(op->tree);
   op->near = near_blocks(op->tree);
   op->nslots = op->tree.levels;
   const double t1 = now_s();
   op->st.t_tree_s = t1 - t0;
-  // points in tree order, structure of arrays
-  const int d = op->p.ndim;
-  std::vector<double> soa(size_t(n) * size_t(d));
-  for (int64_t i = 0; i < n; i++)
-    for (int k = 0; k < d; k++) soa[size_t(k) * size_t(n) + size_t(i)] = points[size_t(op->tree.perm[size_t(i)]) * d + k];
-  op->d_pts = upload(op->mem, soa, st, "points");
-  op->d_perm = upload(op->mem, op->tree.perm, st, "permutation");
-  op->d_lmap = upload(op->mem, reference_order_map(op->tree), st, "reference-order map");
   // near field
   bs.nt = near_tiles(op->tree, op->near, 8);
   const NearTiles& nt = bs.nt;
@@ -2370,6 +2371,38 @@ int hodlr_tree_build(const hodlr_params* params, const double* points, int64_t n
     *out = tr.release();
     return HODLR_OK;
   } catch (const std::exception& e) {
+    return fail(nullptr, HODLR_ERR_INVALID, e.what());
+  }
+}
+
+int hodlr_tree_build_device(const hodlr_params* params, const double* points, int64_t n, const double* box_lo,
+                            const double* box_hi, hodlr_tree** out) {
+  if (!params || !points || !box_lo || !box_hi || !out)
+    return fail(nullptr, HODLR_ERR_INVALID, "hodlr_tree_build_device: null argument");
+  *out = nullptr;
+  cudaStream_t st = nullptr;
+  try {
+    check_cuda(cudaSetDevice(params->device), "cudaSetDevice");
+    check_cuda(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "cudaStreamCreate");
+    std::unique_ptr<hodlr_tree> tr(new hodlr_tree());
+    TreeParams tp;
+    tp.ndim = params->ndim;
+    tp.nmax = params->nmax;
+    tp.dprime = params->dprime;
+    DeviceTreeOut dto;  // the host arrays only
+    const DeviceTreeStatus ds = build_tree_device(tp, points, n, box_lo, box_hi, tr->t, dto, st);
+    cudaStreamDestroy(st);
+    st = nullptr;
+    if (ds.code != 0) return fail(nullptr, ds.code, "hodlr_tree_build_device: " + ds.msg);
+    tr->far = far_blocks(tr->t);
+    tr->near = near_blocks(tr->t);
+    *out = tr.release();
+    return HODLR_OK;
+  } catch (const Failure& f) {
+    if (st) cudaStreamDestroy(st);
+    return fail(nullptr, f.code, "hodlr_tree_build_device: " + f.msg);
+  } catch (const std::exception& e) {
+    if (st) cudaStreamDestroy(st);
     return fail(nullptr, HODLR_ERR_INVALID, e.what());
   }
 }

@@ -234,16 +234,31 @@ class HODLRdD_matrix:
         print(f"Time to Initialize (in s) : {s['t_build_s']}")
         print(f"Matrix-Vector time (in s) : {s['t_matvec_s']}")
 
-    def tree_structure(self):
+    def tree_structure(self, device=False):
+        """Tree and lists as arrays.  device=True builds them again on the GPU
+        (hodlr_tree_build_device, the path hodlr_build takes) instead of
+        returning the host build's."""
+        L = _lib.lib()
+        if device:
+            tree = ctypes.c_void_p()
+            _lib.check(L.hodlr_tree_build_device(ctypes.byref(self.params), _dp(self.points), self.N, _dp(self.x1),
+                                                 _dp(self.x2), ctypes.byref(tree)))
+            try:
+                return self._structure(tree)
+            finally:
+                L.hodlr_tree_destroy(tree)
+        return self._structure(self._tree)
+
+    def _structure(self, tree):
         L = _lib.lib()
         sz = np.zeros(6, np.int64)
-        _lib.check(L.hodlr_tree_sizes(self._tree, sz.ctypes.data_as(_I64)))
+        _lib.check(L.hodlr_tree_sizes(tree, sz.ctypes.data_as(_I64)))
         levels, nodes = int(sz[0]), int(sz[1])
         out = dict(level_sizes=np.zeros(levels, np.int64), node_counts=np.zeros(nodes, np.int64),
                    nbr_ptr=np.zeros(nodes + 1, np.int64), nbr=np.zeros(max(int(sz[2]), 1), np.int64),
                    intr_ptr=np.zeros(nodes + 1, np.int64), intr=np.zeros(max(int(sz[3]), 1), np.int64),
                    leaf_perm=np.zeros(self.N, np.int64))
-        _lib.check(L.hodlr_tree_get(self._tree, *[out[k].ctypes.data_as(_I64) for k in
+        _lib.check(L.hodlr_tree_get(tree, *[out[k].ctypes.data_as(_I64) for k in
                                                  ("level_sizes", "node_counts", "nbr_ptr", "nbr", "intr_ptr",
                                                   "intr", "leaf_perm")]))
         out["nbr"] = out["nbr"][:int(sz[2])]

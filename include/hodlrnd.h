@@ -469,6 +469,12 @@ typedef struct hodlr_tree hodlr_tree;
 /* Tree and lists only (include/HDD_tree.hpp:23-74, include/HDD_node.hpp:150-180). */
 int hodlr_tree_build(const hodlr_params* params, const double* points, int64_t n, const double* box_lo,
                      const double* box_hi, hodlr_tree** out);
+/* The same tree and lists built on the GPU params->device (what hodlr_build
+ * uses): the points' stable partition among the children, the child boxes and
+ * the admissibility tests run on the device with the host's rounding, so the
+ * arrays equal hodlr_tree_build's bit for bit.  Errors: hodlr_last_error(NULL). */
+int hodlr_tree_build_device(const hodlr_params* params, const double* points, int64_t n, const double* box_lo,
+                            const double* box_hi, hodlr_tree** out);
 /* sizes[0..5] = levels, nodes (all levels), neighbour entries, interaction entries,
  * far blocks (both nodes non-empty), near blocks (self + non-empty neighbours of non-empty leaves) */
 int hodlr_tree_sizes(const hodlr_tree* tree, int64_t* sizes);
