@@ -1834,17 +1834,21 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   tc_panel_items(h.panels_near, int(tile_rows(8)), ns, nb, T.max_near_small, T.max_near_big, fxn, pn);
   tc_panel_items(h.panels_far, int(tile_rows(2)), fs, fb, T.max_far_small, T.max_far_big, fxf, pf);
   // z groups: the low-rank blocks by source node (consecutive in the sorted
-  // order), at most 256 rows per group
+  // order), at most 256 rows per group.  A node is its first point and its
+  // size: a node and its first child start at the same point.
   std::vector<int32_t> order(h.zb.size());
   for (size_t q = 0; q < order.size(); q++) order[q] = int32_t(q);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int32_t x, int32_t y) { return h.zb[size_t(x)].x_off < h.zb[size_t(y)].x_off; });
+  auto same_source = [&](const ZBlock& a, const ZBlock& b) { return a.x_off == b.x_off && a.n == b.n; };
+  std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+    const ZBlock &a = h.zb[size_t(x)], &b = h.zb[size_t(y)];
+    return a.x_off != b.x_off ? a.x_off < b.x_off : a.n < b.n;
+  });
   std::vector<TcZGroup> zg;
   std::vector<TcZEntry> ze;
   for (size_t q = 0; q < order.size();) {
     const ZBlock& z0 = h.zb[size_t(order[q])];
     TcZGroup g{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0};
-    while (q < order.size() && h.zb[size_t(order[q])].x_off == z0.x_off) {
+    while (q < order.size() && same_source(h.zb[size_t(order[q])], z0)) {
       const ZBlock& z = h.zb[size_t(order[q])];
       for (int32_t k0 = 0; k0 < z.r;) {
         const int32_t take = std::min(z.r - k0, 256 - g.rows);

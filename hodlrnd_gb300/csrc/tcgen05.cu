@@ -485,12 +485,14 @@ static cudaError_t launch_tc_k(const TcLaunch& a, cudaStream_t st) {
   const int smem = tc_smem_bytes<KIND>(npad);
   cudaError_t e = cudaFuncSetAttribute(tc_kernel<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_kernel<KIND>, kTcThreads, size_t(smem));
-  // tensor memory: 512 columns per SM shared by the resident CTAs
-  per_sm = std::max(1, std::min(per_sm, int(512 / tcols)));
+  int dev = 0, sms = 0, smem_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+      (e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+    return e;
+  // resident CTAs per SM: threads (2048 / 128), shared memory (1 KB reserved
+  // per CTA), and tensor memory (512 columns per SM shared by the CTAs)
+  const int per_sm = std::max(1, std::min({2048 / kTcThreads, smem_sm / (smem + 1024), int(512 / tcols)}));
   const int grid = std::min(nitems, sms * per_sm);
   count_launches(1);
   tc_kernel<KIND><<<grid, kTcThreads, smem, st>>>(a, npad, tcols);
