@@ -224,15 +224,18 @@ struct hodlr_op {
   Plan plan_ref;
   // tensor-core products for 64 right-hand sides (BF16 factors; built on first use)
   struct TcPlan {
+    // one launch per (family, small / big, rows bucket): items of at most
+    // `rows` output rows, so each launch holds just the tensor memory and
+    // shared memory its items need
+    struct Run {
+      const void* items;  // Item (panels) or TcZGroup (z)
+      int n, rows, big;
+    };
     bool built = false;
-    Item *near_small = nullptr, *near_big = nullptr, *far_small = nullptr, *far_big = nullptr;
-    int n_near_small = 0, n_near_big = 0, n_far_small = 0, n_far_big = 0;
-    int max_near_small = 0, max_near_big = 0, max_far_small = 0, max_far_big = 0;  // rows of the largest item
+    std::vector<Run> near, far, z;
     PanelFix *fix_near = nullptr, *fix_far = nullptr;
     int nfix_near = 0, nfix_far = 0;
-    TcZGroup* zg = nullptr;
     TcZEntry* ze = nullptr;
-    int nzg = 0, max_zg = 0;
     float *in = nullptr, *y = nullptr, *part_near = nullptr, *part_far = nullptr;
     unsigned int* status = nullptr;
     unsigned int* h_status = nullptr;
@@ -1791,36 +1794,53 @@ void batch_apply_mr(hodlr_batch& b, const float* x, float* y, int64_t nrhs, cuda
 
 // ---- tensor-core products for 64 right-hand sides ---------------------------
 
+// Rows buckets of the tensor-core launches: 16, 32, 64, 128, 256.
+int tc_bucket(int rows) {
+  int b = 16;
+  while (b < rows) b <<= 1;
+  return b;
+}
+
 // Items of the tensor-core panel kernels for one family of panels: per panel,
 // its row tiles (one for panels of at most 32 rows) times runs of at most
 // kTcSegsPerItem segments (runs after the first write partial row blocks that
-// a fix-up adds in order).
-constexpr int kTcSegsPerItem = 1024;
-static_assert(kTcSegsPerItem < kTcMaxSegs, "the tensor-core kernels hold the column starts of an item's segments");
-void tc_panel_items(const std::vector<Panel>& panels, int tile_rows, std::vector<Item>& small, std::vector<Item>& big,
-                    int& max_small, int& max_big, std::vector<PanelFix>& fix, int& nparts) {
+// a fix-up adds in order).  Items are listed by launch: small then big panels,
+// each by rows bucket; runs[] gets one entry per non-empty launch (offsets
+// into the items until the array is uploaded).
+constexpr int kTcSegsPerItem = kTcMaxSegs;  // the kernels hold an item's segment records in shared memory
+void tc_panel_items(const std::vector<Panel>& panels, int tile_rows, std::vector<Item>& items,
+                    std::vector<hodlr_op::TcPlan::Run>& runs, std::vector<PanelFix>& fix, int& nparts) {
+  std::vector<Item> by[2][5];  // [big][bucket]
   for (size_t pi = 0; pi < panels.size(); pi++) {
     const Panel& P = panels[pi];
     const int64_t ns = P.seg_end - P.seg_begin;
     if (ns <= 0 || P.m <= 0) continue;
-    const int runs = int((ns + kTcSegsPerItem - 1) / kTcSegsPerItem);
+    const int nruns = int((ns + kTcSegsPerItem - 1) / kTcSegsPerItem);
     const bool is_big = P.m > 32;
     const int tiles = is_big ? int((P.m + tile_rows - 1) / tile_rows) : 1;
     for (int tl = 0; tl < tiles; tl++) {
       const int rows = is_big ? std::min<int>(tile_rows, P.m - tl * tile_rows) : P.m;
-      (is_big ? max_big : max_small) = std::max(is_big ? max_big : max_small, rows);
-      if (runs > 1) fix.push_back({int32_t(pi), tl, nparts, runs});
-      for (int q = 0; q < runs; q++) {
+      int bk = 0;
+      while ((16 << bk) < rows) bk++;
+      if (nruns > 1) fix.push_back({int32_t(pi), tl, nparts, nruns});
+      for (int q = 0; q < nruns; q++) {
         Item it;
         it.panel = int32_t(pi);
         it.chunk = tl;
         it.seg_b = int32_t(P.seg_begin + int64_t(q) * kTcSegsPerItem);
         it.seg_e = int32_t(std::min<int64_t>(P.seg_end, P.seg_begin + int64_t(q + 1) * kTcSegsPerItem));
-        it.part = runs > 1 ? nparts++ : -1;
-        (is_big ? big : small).push_back(it);
+        it.part = nruns > 1 ? nparts++ : -1;
+        by[is_big][bk].push_back(it);
       }
     }
   }
+  for (int big = 0; big < 2; big++)
+    for (int bk = 0; bk < 5; bk++) {
+      const std::vector<Item>& v = by[big][bk];
+      if (v.empty()) continue;
+      runs.push_back({reinterpret_cast<const void*>(items.size()), int(v.size()), 16 << bk, big});
+      items.insert(items.end(), v.begin(), v.end());
+    }
 }
 
 void build_tc_plan(hodlr_op* op, cudaStream_t st) {
@@ -1828,11 +1848,11 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   if (T.built) return;
   if (!op->plan64.host) throw Failure{HODLR_ERR_STATE, "the operator keeps no host plan for the tensor-core path"};
   const Plan::Host& h = *op->plan64.host;
-  std::vector<Item> ns, nb, fs, fb;
+  std::vector<Item> ni, fi;
   std::vector<PanelFix> fxn, fxf;
   int pn = 0, pf = 0;
-  tc_panel_items(h.panels_near, int(tile_rows(8)), ns, nb, T.max_near_small, T.max_near_big, fxn, pn);
-  tc_panel_items(h.panels_far, int(tile_rows(2)), fs, fb, T.max_far_small, T.max_far_big, fxf, pf);
+  tc_panel_items(h.panels_near, int(tile_rows(8)), ni, T.near, fxn, pn);
+  tc_panel_items(h.panels_far, int(tile_rows(2)), fi, T.far, fxf, pf);
   // z groups: the low-rank blocks by source node (consecutive in the sorted
   // order), at most 256 rows per group.  A node is its first point and its
   // size: a node and its first child start at the same point.
@@ -1857,7 +1877,6 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
         k0 += take;
         if (g.rows == 256) {  // close the group, continue with a new one on the same source
           g.e_end = int32_t(ze.size());
-          T.max_zg = std::max(T.max_zg, g.rows);
           zg.push_back(g);
           g = TcZGroup{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0};
         }
@@ -1866,25 +1885,29 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
     }
     if (g.rows > 0) {
       g.e_end = int32_t(ze.size());
-      T.max_zg = std::max(T.max_zg, g.rows);
       zg.push_back(g);
     }
   }
-  T.near_small = upload(op->mem, ns, st, "tensor-core near items");
-  T.near_big = upload(op->mem, nb, st, "tensor-core near items");
-  T.far_small = upload(op->mem, fs, st, "tensor-core far items");
-  T.far_big = upload(op->mem, fb, st, "tensor-core far items");
-  T.n_near_small = int(ns.size());
-  T.n_near_big = int(nb.size());
-  T.n_far_small = int(fs.size());
-  T.n_far_big = int(fb.size());
+  // z groups by rows bucket
+  std::vector<TcZGroup> zgs;
+  for (int bk = 0; bk < 5; bk++) {
+    const size_t b0 = zgs.size();
+    for (const TcZGroup& g : zg)
+      if (tc_bucket(g.rows) == (16 << bk)) zgs.push_back(g);
+    if (zgs.size() > b0)
+      T.z.push_back({reinterpret_cast<const void*>(b0), int(zgs.size() - b0), 16 << bk, 0});
+  }
+  const Item* d_ni = upload(op->mem, ni, st, "tensor-core near items");
+  const Item* d_fi = upload(op->mem, fi, st, "tensor-core far items");
+  const TcZGroup* d_zg = upload(op->mem, zgs, st, "tensor-core z groups");
+  for (auto& r : T.near) r.items = d_ni + reinterpret_cast<size_t>(r.items);
+  for (auto& r : T.far) r.items = d_fi + reinterpret_cast<size_t>(r.items);
+  for (auto& r : T.z) r.items = d_zg + reinterpret_cast<size_t>(r.items);
   T.fix_near = upload(op->mem, fxn, st, "tensor-core near fix-ups");
   T.fix_far = upload(op->mem, fxf, st, "tensor-core far fix-ups");
   T.nfix_near = int(fxn.size());
   T.nfix_far = int(fxf.size());
-  T.zg = upload(op->mem, zg, st, "tensor-core z groups");
   T.ze = upload(op->mem, ze, st, "tensor-core z entries");
-  T.nzg = int(zg.size());
   const int64_t n = op->n;
   T.in = op->mem.alloc_n<float>(size_t(n + op->zlen) * kTcRhs, "tensor-core input (64 right-hand sides)");
   T.y = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots) * kTcRhs, "tensor-core output slots");
@@ -1911,30 +1934,32 @@ void apply_tc(hodlr_op* op, const float* x, int64_t ldx, float* y, int64_t ldy, 
   a.status = T.status;
   // z = V^T x, grouped by source node
   a.zb = P.zb;
-  a.zgroups = T.zg;
   a.zentries = T.ze;
-  a.nz = T.nzg;
-  a.nmax = T.max_zg;
-  CK(launch_tc(kTcZ, a, st));
+  for (const auto& r : T.z) {
+    a.zgroups = static_cast<const TcZGroup*>(r.items);
+    a.nz = r.n;
+    a.nmax = r.rows;
+    CK(launch_tc(kTcZ, a, st));
+  }
   a.nz = 0;
   // near field (FP64 tiles, three BF16 terms), then the far field (BF16)
   a.panels = P.panels_near;
   a.segs = P.segs_near;
   a.part = T.part_near;
   a.tile_rows = int(tile_rows(8));
-  a.items = T.near_small, a.nitems = T.n_near_small, a.big = 0, a.nmax = T.max_near_small;
-  CK(launch_tc(kTcNear, a, st));
-  a.items = T.near_big, a.nitems = T.n_near_big, a.big = 1, a.nmax = T.max_near_big;
-  CK(launch_tc(kTcNear, a, st));
+  for (const auto& r : T.near) {
+    a.items = static_cast<const Item*>(r.items), a.nitems = r.n, a.big = r.big, a.nmax = r.rows;
+    CK(launch_tc(kTcNear, a, st));
+  }
   CK(launch_tc_fix(P.panels_near, T.fix_near, T.nfix_near, int(tile_rows(8)), T.part_near, T.y, n, st));
   a.panels = P.panels_far;
   a.segs = P.segs_far;
   a.part = T.part_far;
   a.tile_rows = int(tile_rows(2));
-  a.items = T.far_small, a.nitems = T.n_far_small, a.big = 0, a.nmax = T.max_far_small;
-  CK(launch_tc(kTcFar, a, st));
-  a.items = T.far_big, a.nitems = T.n_far_big, a.big = 1, a.nmax = T.max_far_big;
-  CK(launch_tc(kTcFar, a, st));
+  for (const auto& r : T.far) {
+    a.items = static_cast<const Item*>(r.items), a.nitems = r.n, a.big = r.big, a.nmax = r.rows;
+    CK(launch_tc(kTcFar, a, st));
+  }
   CK(launch_tc_fix(P.panels_far, T.fix_far, T.nfix_far, int(tile_rows(2)), T.part_far, T.y, n, st));
   CK(launch_tc_combine(T.y, op->nslots, n, op->d_perm, y, ldy, nrhs, st));
 }

@@ -20,7 +20,7 @@
 namespace hodlr {
 
 constexpr int kTcRhs = 64;     // right-hand sides per block
-constexpr int kTcMaxSegs = 2048;  // segments of one panel item (the host splits longer items)
+constexpr int kTcMaxSegs = 256;  // segments of one panel item (the host splits longer items)
 
 // kind of product: z = V^T x (one item per low-rank block), near-field panels
 // (FP64 tiles), far-field panels (BF16 dense tiles and U factors)

@@ -122,11 +122,18 @@ struct TcRow {  // z groups: one output row
   float zscale;
   int32_t vp;
 };
+// panel items: the segments' first columns (kTcMaxSegs + 1 of them), then the
+// segment records; z groups: the rows
+constexpr int kTcStartBytes = (kTcMaxSegs + 1 + 31) / 32 * 32 * 4;
+constexpr int kTcPanelTable = kTcStartBytes + kTcMaxSegs * int(sizeof(Seg));
+template <int KIND>
+__host__ __device__ constexpr int tc_table_bytes() {
+  return KIND == kTcZ ? 256 * int(sizeof(TcRow)) : kTcPanelTable;
+}
 template <int KIND>
 __host__ __device__ constexpr int tc_smem_bytes(int npad) {
-  // header (barriers, tensor-memory slot, step table), segment column starts or
-  // z rows, two buffers
-  return 1024 + (KIND == kTcZ ? 256 * int(sizeof(TcRow)) : kTcMaxSegs * 4) + 2 * tc_buf_bytes<KIND>(npad);
+  // header (barriers, tensor-memory slot, step table), the item's table, two buffers
+  return 1024 + tc_table_bytes<KIND>() + 2 * tc_buf_bytes<KIND>(npad);
 }
 
 struct TcCol {
@@ -145,8 +152,9 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
   uint32_t* slot = reinterpret_cast<uint32_t*>(tsm + 16);  // tensor-memory address
   TcCol* tab = reinterpret_cast<TcCol*>(tsm + 64);         // 16 columns of the step being written
   int32_t* cstart = reinterpret_cast<int32_t*>(tsm + 1024);  // first column of each segment of the item
+  Seg* sseg = reinterpret_cast<Seg*>(tsm + 1024 + kTcStartBytes);  // the item's segment records
   TcRow* zrow = reinterpret_cast<TcRow*>(tsm + 1024);        // z groups: the rows
-  unsigned char* buf0 = tsm + 1024 + (KIND == kTcZ ? 256 * int(sizeof(TcRow)) : kTcMaxSegs * 4);
+  unsigned char* buf0 = tsm + 1024 + tc_table_bytes<KIND>();
   const int bufb = tc_buf_bytes<KIND>(npad_max);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int nitems = KIND == kTcZ ? a.nz : a.nitems;
@@ -250,8 +258,9 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
           if (q < nseg) cstart[q] = run + incl - k;
           run += __shfl_sync(0xffffffffu, incl, 31);
         }
-        if (lane == 0) cstart[min(nseg, kTcMaxSegs - 1)] = run;  // total (nseg < kTcMaxSegs: host-checked)
+        if (lane == 0) cstart[nseg] = run;  // total (nseg <= kTcMaxSegs: host-checked)
       }
+      for (int q = t; q < nseg; q += kTcThreads) sseg[q] = a.segs[qb + q];
       __syncthreads();
       C = cstart[nseg];
     }
@@ -293,7 +302,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
               if (cstart[mid] <= c) lo = mid;
               else hi = mid - 1;
             }
-            const Seg S = a.segs[qb + lo];
+            const Seg& S = sseg[lo];
             const int j = int(c - cstart[lo]);
             col.pos = S.in_off + j;
             if (S.cscale) col.scale = __ldg(S.cscale + j);
