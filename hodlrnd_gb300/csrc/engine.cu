@@ -236,7 +236,10 @@ struct hodlr_op {
     PanelFix *fix_near = nullptr, *fix_far = nullptr;
     int nfix_near = 0, nfix_far = 0;
     TcZEntry* ze = nullptr;
-    float *in = nullptr, *y = nullptr, *part_near = nullptr, *part_far = nullptr;
+    TcZFix* zfix = nullptr;  // split z groups
+    TcZRow* zrows = nullptr;
+    int nzfix = 0, zfix_rows = 0;
+    float *in = nullptr, *y = nullptr, *part_near = nullptr, *part_far = nullptr, *zpart = nullptr;
     unsigned int* status = nullptr;
     unsigned int* h_status = nullptr;
   } tc;
@@ -1802,20 +1805,37 @@ int tc_bucket(int rows) {
 }
 
 // Items of the tensor-core panel kernels for one family of panels: per panel,
-// its row tiles (one for panels of at most 32 rows) times runs of at most
-// kTcSegsPerItem segments (runs after the first write partial row blocks that
-// a fix-up adds in order).  Items are listed by launch: small then big panels,
+// its row tiles (one for panels of at most 32 rows) times runs of whole
+// segments of at most kTcColsPerItem columns (a longer segment alone) and at
+// most kTcMaxSegs segments -- a CTA works through an item's columns one
+// 16-column step after another, so long items would leave most SMs idle at
+// the end of a launch.  Runs after the first write partial row blocks that a
+// fix-up adds in order.  Items are listed by launch: small then big panels,
 // each by rows bucket; runs[] gets one entry per non-empty launch (offsets
 // into the items until the array is uploaded).
-constexpr int kTcSegsPerItem = kTcMaxSegs;  // the kernels hold an item's segment records in shared memory
-void tc_panel_items(const std::vector<Panel>& panels, int tile_rows, std::vector<Item>& items,
-                    std::vector<hodlr_op::TcPlan::Run>& runs, std::vector<PanelFix>& fix, int& nparts) {
+constexpr int kTcColsPerItem = 256;
+void tc_panel_items(const std::vector<Panel>& panels, const std::vector<Seg>& segs, int tile_rows,
+                    std::vector<Item>& items, std::vector<hodlr_op::TcPlan::Run>& runs, std::vector<PanelFix>& fix,
+                    int& nparts) {
   std::vector<Item> by[2][5];  // [big][bucket]
+  std::vector<std::pair<int32_t, int32_t>> cut;
   for (size_t pi = 0; pi < panels.size(); pi++) {
     const Panel& P = panels[pi];
     const int64_t ns = P.seg_end - P.seg_begin;
     if (ns <= 0 || P.m <= 0) continue;
-    const int nruns = int((ns + kTcSegsPerItem - 1) / kTcSegsPerItem);
+    cut.clear();
+    int64_t start = P.seg_begin, cols = 0;
+    for (int64_t q = P.seg_begin; q < P.seg_end; q++) {
+      const int64_t K = segs[size_t(q)].K;
+      if (q > start && (cols + K > kTcColsPerItem || q - start >= kTcMaxSegs)) {
+        cut.push_back({int32_t(start), int32_t(q)});
+        start = q;
+        cols = 0;
+      }
+      cols += K;
+    }
+    cut.push_back({int32_t(start), int32_t(P.seg_end)});
+    const int nruns = int(cut.size());
     const bool is_big = P.m > 32;
     const int tiles = is_big ? int((P.m + tile_rows - 1) / tile_rows) : 1;
     for (int tl = 0; tl < tiles; tl++) {
@@ -1827,8 +1847,8 @@ void tc_panel_items(const std::vector<Panel>& panels, int tile_rows, std::vector
         Item it;
         it.panel = int32_t(pi);
         it.chunk = tl;
-        it.seg_b = int32_t(P.seg_begin + int64_t(q) * kTcSegsPerItem);
-        it.seg_e = int32_t(std::min<int64_t>(P.seg_end, P.seg_begin + int64_t(q + 1) * kTcSegsPerItem));
+        it.seg_b = cut[size_t(q)].first;
+        it.seg_e = cut[size_t(q)].second;
         it.part = nruns > 1 ? nparts++ : -1;
         by[is_big][bk].push_back(it);
       }
@@ -1851,8 +1871,8 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   std::vector<Item> ni, fi;
   std::vector<PanelFix> fxn, fxf;
   int pn = 0, pf = 0;
-  tc_panel_items(h.panels_near, int(tile_rows(8)), ni, T.near, fxn, pn);
-  tc_panel_items(h.panels_far, int(tile_rows(2)), fi, T.far, fxf, pf);
+  tc_panel_items(h.panels_near, h.segs_near, int(tile_rows(8)), ni, T.near, fxn, pn);
+  tc_panel_items(h.panels_far, h.segs_far, int(tile_rows(2)), fi, T.far, fxf, pf);
   // z groups: the low-rank blocks by source node (consecutive in the sorted
   // order), at most 256 rows per group.  A node is its first point and its
   // size: a node and its first child start at the same point.
@@ -1867,7 +1887,7 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   std::vector<TcZEntry> ze;
   for (size_t q = 0; q < order.size();) {
     const ZBlock& z0 = h.zb[size_t(order[q])];
-    TcZGroup g{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0};
+    TcZGroup g{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0, -1, 0};
     while (q < order.size() && same_source(h.zb[size_t(order[q])], z0)) {
       const ZBlock& z = h.zb[size_t(order[q])];
       for (int32_t k0 = 0; k0 < z.r;) {
@@ -1878,7 +1898,7 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
         if (g.rows == 256) {  // close the group, continue with a new one on the same source
           g.e_end = int32_t(ze.size());
           zg.push_back(g);
-          g = TcZGroup{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0};
+          g = TcZGroup{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0, -1, 0};
         }
       }
       q++;
@@ -1887,6 +1907,36 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
       g.e_end = int32_t(ze.size());
       zg.push_back(g);
     }
+  }
+  // groups over more than kTcZCols points: column runs writing partial sums,
+  // added into z (and scaled) by a fix-up
+  std::vector<TcZFix> zfix;
+  std::vector<TcZRow> zrows;
+  int zparts = 0;
+  {
+    std::vector<TcZGroup> split;
+    for (const TcZGroup& g : zg) {
+      if (g.n <= kTcZCols) {
+        split.push_back(g);
+        continue;
+      }
+      const int runs = (g.n + kTcZCols - 1) / kTcZCols;
+      zfix.push_back({zparts, runs, g.rows, int32_t(zrows.size())});
+      T.zfix_rows = std::max(T.zfix_rows, g.rows);
+      for (int32_t e = g.e_begin; e < g.e_end; e++) {
+        const TcZEntry& E = ze[size_t(e)];
+        const ZBlock& Z = h.zb[size_t(E.zb)];
+        for (int32_t k = E.k0; k < E.k0 + E.nk; k++) zrows.push_back({Z.z_off + k, Z.zscale ? Z.zscale + k : nullptr});
+      }
+      for (int c = 0; c < runs; c++) {
+        TcZGroup r = g;
+        r.x_off = g.x_off + int64_t(c) * kTcZCols;
+        r.n = std::min(kTcZCols, g.n - c * kTcZCols);
+        r.part = zparts++;
+        split.push_back(r);
+      }
+    }
+    zg.swap(split);
   }
   // z groups by rows bucket
   std::vector<TcZGroup> zgs;
@@ -1908,6 +1958,10 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   T.nfix_near = int(fxn.size());
   T.nfix_far = int(fxf.size());
   T.ze = upload(op->mem, ze, st, "tensor-core z entries");
+  T.zfix = upload(op->mem, zfix, st, "tensor-core z fix-ups");
+  T.zrows = upload(op->mem, zrows, st, "tensor-core z rows");
+  T.nzfix = int(zfix.size());
+  T.zpart = op->mem.alloc_n<float>(size_t(std::max(zparts, 1)) * 256 * kTcRhs, "tensor-core z partial sums");
   const int64_t n = op->n;
   T.in = op->mem.alloc_n<float>(size_t(n + op->zlen) * kTcRhs, "tensor-core input (64 right-hand sides)");
   T.y = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots) * kTcRhs, "tensor-core output slots");
@@ -1935,12 +1989,14 @@ void apply_tc(hodlr_op* op, const float* x, int64_t ldx, float* y, int64_t ldy, 
   // z = V^T x, grouped by source node
   a.zb = P.zb;
   a.zentries = T.ze;
+  a.part = T.zpart;
   for (const auto& r : T.z) {
     a.zgroups = static_cast<const TcZGroup*>(r.items);
     a.nz = r.n;
     a.nmax = r.rows;
     CK(launch_tc(kTcZ, a, st));
   }
+  CK(launch_tc_zfix(T.zfix, T.nzfix, T.zfix_rows, T.zrows, T.zpart, T.in, st));
   a.nz = 0;
   // near field (FP64 tiles, three BF16 terms), then the far field (BF16)
   a.panels = P.panels_near;

@@ -34,10 +34,23 @@ struct TcZEntry {
   int32_t k0, nk;  // rows (columns of V) of z_b in this group
 };
 struct TcZGroup {
-  int64_t x_off;   // first point of the source node
-  int32_t n;       // points of the source node (the columns)
+  int64_t x_off;   // first point of the group's columns (of the source node)
+  int32_t n;       // columns: all points of the source node, or a run of at most kTcZCols of them
   int32_t e_begin, e_end;  // entries
   int32_t rows;    // sum of nk
+  int32_t part;    // < 0: the group writes z; else its partial sums go to part block `part` (a fix-up adds them)
+  int32_t pad;
+};
+// A source node with more points than kTcZCols is split into column runs
+// whose partial sums (blocks of 256 rows x 64) a fix-up adds into z.
+constexpr int kTcZCols = 256;
+struct TcZRow {        // row i of a split group: where its z goes
+  int64_t zpos;
+  const float* zscale;  // the row's z scale (BF16), or null
+};
+struct TcZFix {
+  int32_t part, count;  // part blocks part .. part + count - 1
+  int32_t rows, row0;   // rows, and their first entry in the TcZRow table
 };
 
 struct TcLaunch {
@@ -70,6 +83,9 @@ cudaError_t launch_tc_gather(const float* x, int64_t ld_x, int nrhs, const int64
 // y_out[perm[p] + r * ld_out] = sum over slots s of y[(s * n + p) * 64 + r], r < nrhs
 cudaError_t launch_tc_combine(const float* y, int nslots, int64_t n, const int64_t* perm, float* out,
                               int64_t ld_out, int nrhs, cudaStream_t st);
+// z of split z groups: in[zpos * 64 + r] = zscale * sum over the group's part blocks
+cudaError_t launch_tc_zfix(const TcZFix* fix, int nfix, int max_rows, const TcZRow* rows, const float* zpart,
+                           float* in, cudaStream_t st);
 // adds split panels' partial row blocks into their output rows (fix-up, as panel_fix_kernel)
 cudaError_t launch_tc_fix(const Panel* panels, const PanelFix* fix, int nfix, int rows_per_item, const float* part,
                           float* y, int64_t n, cudaStream_t st);

@@ -181,11 +181,13 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
     float* outp;
     int row0 = 0, tile = 0, m = 0;
     int64_t zx = 0;
+    int zpart = -1;
     if constexpr (KIND == kTcZ) {
       const TcZGroup G = a.zgroups[item];
       rows = G.rows;
       C = G.n;
       zx = G.x_off;
+      zpart = G.part;
       outp = a.in;
       out_base = 0;  // rows carry their z positions
       // row table: entry e covers rows re .. re + nk - 1 (prefix over entries by warp 0)
@@ -422,9 +424,12 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
           const int i = c0 + q;
           if (i < rows) {
             const float val = v[q] + xch[q * 64 + t];
-            if constexpr (KIND == kTcZ)
-              outp[zrow[i].zpos * kTcRhs + t] = val * zrow[i].zscale;
-            else
+            if constexpr (KIND == kTcZ) {
+              if (zpart < 0)
+                outp[zrow[i].zpos * kTcRhs + t] = val * zrow[i].zscale;
+              else  // a column run of a split group: unscaled partial sums
+                a.part[(int64_t(zpart) * 256 + i) * kTcRhs + t] = val;
+            } else
               outp[(out_base + i) * kTcRhs + t] = val;
           }
         }
@@ -462,6 +467,21 @@ __global__ void tc_combine_kernel(const float* __restrict__ y, int nslots, int64
     float v = 0.f;
     for (int s = 0; s < nslots; s++) v += y[int64_t(s) * total + e];
     out[perm[p] + int64_t(r) * ld_out] = v;
+  }
+}
+
+__global__ void tc_zfix_kernel(const TcZFix* __restrict__ fix, int nfix, int max_rows,
+                               const TcZRow* __restrict__ rows, const float* __restrict__ zpart, float* __restrict__ in) {
+  const int64_t total = int64_t(nfix) * max_rows * kTcRhs;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+    const int f = int(e / (int64_t(max_rows) * kTcRhs));
+    const int i = int((e / kTcRhs) % max_rows), r = int(e % kTcRhs);
+    const TcZFix F = fix[f];
+    if (i >= F.rows) continue;
+    float v = 0.f;
+    for (int q = 0; q < F.count; q++) v += zpart[(int64_t(F.part + q) * 256 + i) * kTcRhs + r];
+    const TcZRow R = rows[F.row0 + i];
+    in[R.zpos * kTcRhs + r] = R.zscale ? v * *R.zscale : v;
   }
 }
 
@@ -528,6 +548,14 @@ cudaError_t launch_tc_combine(const float* y, int nslots, int64_t n, const int64
                               int nrhs, cudaStream_t st) {
   count_launches(1);
   tc_combine_kernel<<<1216, 256, 0, st>>>(y, nslots, n, perm, out, ld_out, nrhs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_zfix(const TcZFix* fix, int nfix, int max_rows, const TcZRow* rows, const float* zpart,
+                           float* in, cudaStream_t st) {
+  if (nfix <= 0) return cudaSuccess;
+  count_launches(1);
+  tc_zfix_kernel<<<1216, 256, 0, st>>>(fix, nfix, max_rows, rows, zpart, in);
   return cudaGetLastError();
 }
 
