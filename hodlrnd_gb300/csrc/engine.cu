@@ -1931,6 +1931,7 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
       for (int c = 0; c < runs; c++) {
         TcZGroup r = g;
         r.x_off = g.x_off + int64_t(c) * kTcZCols;
+        r.col0 = c * kTcZCols;
         r.n = std::min(kTcZCols, g.n - c * kTcZCols);
         r.part = zparts++;
         split.push_back(r);

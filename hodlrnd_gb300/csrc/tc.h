@@ -39,7 +39,7 @@ struct TcZGroup {
   int32_t e_begin, e_end;  // entries
   int32_t rows;    // sum of nk
   int32_t part;    // < 0: the group writes z; else its partial sums go to part block `part` (a fix-up adds them)
-  int32_t pad;
+  int32_t col0;    // the first column's point within the source node (its row of V): 0 unless a column run
 };
 // A source node with more points than kTcZCols is split into column runs
 // whose partial sums (blocks of 256 rows x 64) a fix-up adds into z.

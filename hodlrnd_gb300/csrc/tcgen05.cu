@@ -220,8 +220,8 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
         const TcZEntry E = a.zentries[G.e_begin + lo];
         const ZBlock Z = a.zb[E.zb];
         const int k = E.k0 + (i - cstart[lo]);
-        rw[nr].v = static_cast<const uint16_t*>(Z.V) + k;
         rw[nr].vp = int32_t(vpad(Z.r, 2));
+        rw[nr].v = static_cast<const uint16_t*>(Z.V) + int64_t(G.col0) * rw[nr].vp + k;  // V row col0, column k
         rw[nr].zpos = Z.z_off + k;
         rw[nr].zscale = Z.zscale ? __ldg(Z.zscale + k) : 1.f;
       }
