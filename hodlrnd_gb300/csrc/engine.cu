@@ -1814,8 +1814,7 @@ int tc_bucket(int rows) {
 // each by rows bucket; runs[] gets one entry per non-empty launch (offsets
 // into the items until the array is uploaded).
 constexpr int kTcColsPerItem = 256;
-void tc_panel_items(const std::vector<Panel>& panels, const std::vector<Seg>& segs, int tile_rows,
-                    std::vector<Item>& items, std::vector<hodlr_op::TcPlan::Run>& runs, std::vector<PanelFix>& fix,
+void tc_panel_items(const std::vector<Panel>& panels, const std::vector<Seg>& segs, std::vector<Item>& items, std::vector<hodlr_op::TcPlan::Run>& runs, std::vector<PanelFix>& fix,
                     int& nparts) {
   std::vector<Item> by[2][5];  // [big][bucket]
   std::vector<std::pair<int32_t, int32_t>> cut;
@@ -1837,9 +1836,9 @@ void tc_panel_items(const std::vector<Panel>& panels, const std::vector<Seg>& se
     cut.push_back({int32_t(start), int32_t(P.seg_end)});
     const int nruns = int(cut.size());
     const bool is_big = P.m > 32;
-    const int tiles = is_big ? int((P.m + tile_rows - 1) / tile_rows) : 1;
+    const int tiles = is_big ? int((P.m + kTcRows - 1) / kTcRows) : 1;
     for (int tl = 0; tl < tiles; tl++) {
-      const int rows = is_big ? std::min<int>(tile_rows, P.m - tl * tile_rows) : P.m;
+      const int rows = is_big ? std::min<int>(kTcRows, P.m - tl * kTcRows) : P.m;
       int bk = 0;
       while ((16 << bk) < rows) bk++;
       if (nruns > 1) fix.push_back({int32_t(pi), tl, nparts, nruns});
@@ -1871,8 +1870,8 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   std::vector<Item> ni, fi;
   std::vector<PanelFix> fxn, fxf;
   int pn = 0, pf = 0;
-  tc_panel_items(h.panels_near, h.segs_near, int(tile_rows(8)), ni, T.near, fxn, pn);
-  tc_panel_items(h.panels_far, h.segs_far, int(tile_rows(2)), fi, T.far, fxf, pf);
+  tc_panel_items(h.panels_near, h.segs_near, ni, T.near, fxn, pn);
+  tc_panel_items(h.panels_far, h.segs_far, fi, T.far, fxf, pf);
   // z groups: the low-rank blocks by source node (consecutive in the sorted
   // order), at most 256 rows per group.  A node is its first point and its
   // size: a node and its first child start at the same point.
@@ -1891,11 +1890,11 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
     while (q < order.size() && same_source(h.zb[size_t(order[q])], z0)) {
       const ZBlock& z = h.zb[size_t(order[q])];
       for (int32_t k0 = 0; k0 < z.r;) {
-        const int32_t take = std::min(z.r - k0, 256 - g.rows);
+        const int32_t take = std::min(z.r - k0, kTcRows - g.rows);
         ze.push_back({order[q], k0, take});
         g.rows += take;
         k0 += take;
-        if (g.rows == 256) {  // close the group, continue with a new one on the same source
+        if (g.rows == kTcRows) {  // close the group, continue with a new one on the same source
           g.e_end = int32_t(ze.size());
           zg.push_back(g);
           g = TcZGroup{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0, -1, 0};
@@ -1962,12 +1961,12 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   T.zfix = upload(op->mem, zfix, st, "tensor-core z fix-ups");
   T.zrows = upload(op->mem, zrows, st, "tensor-core z rows");
   T.nzfix = int(zfix.size());
-  T.zpart = op->mem.alloc_n<float>(size_t(std::max(zparts, 1)) * 256 * kTcRhs, "tensor-core z partial sums");
+  T.zpart = op->mem.alloc_n<float>(size_t(std::max(zparts, 1)) * kTcRows * kTcRhs, "tensor-core z partial sums");
   const int64_t n = op->n;
   T.in = op->mem.alloc_n<float>(size_t(n + op->zlen) * kTcRhs, "tensor-core input (64 right-hand sides)");
   T.y = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots) * kTcRhs, "tensor-core output slots");
-  T.part_near = op->mem.alloc_n<float>(size_t(std::max(pn, 1)) * tile_rows(8) * kTcRhs, "tensor-core partial rows");
-  T.part_far = op->mem.alloc_n<float>(size_t(std::max(pf, 1)) * tile_rows(2) * kTcRhs, "tensor-core partial rows");
+  T.part_near = op->mem.alloc_n<float>(size_t(std::max(pn, 1)) * kTcRows * kTcRhs, "tensor-core partial rows");
+  T.part_far = op->mem.alloc_n<float>(size_t(std::max(pf, 1)) * kTcRows * kTcRhs, "tensor-core partial rows");
   T.status = op->mem.alloc_n<unsigned int>(1, "tensor-core status");
   CK(cudaMemsetAsync(T.status, 0, sizeof(unsigned int), st));
   CK(cudaMallocHost(&T.h_status, sizeof(unsigned int)));
@@ -2003,21 +2002,19 @@ void apply_tc(hodlr_op* op, const float* x, int64_t ldx, float* y, int64_t ldy, 
   a.panels = P.panels_near;
   a.segs = P.segs_near;
   a.part = T.part_near;
-  a.tile_rows = int(tile_rows(8));
   for (const auto& r : T.near) {
     a.items = static_cast<const Item*>(r.items), a.nitems = r.n, a.big = r.big, a.nmax = r.rows;
     CK(launch_tc(kTcNear, a, st));
   }
-  CK(launch_tc_fix(P.panels_near, T.fix_near, T.nfix_near, int(tile_rows(8)), T.part_near, T.y, n, st));
+  CK(launch_tc_fix(P.panels_near, T.fix_near, T.nfix_near, T.part_near, T.y, st));
   a.panels = P.panels_far;
   a.segs = P.segs_far;
   a.part = T.part_far;
-  a.tile_rows = int(tile_rows(2));
   for (const auto& r : T.far) {
     a.items = static_cast<const Item*>(r.items), a.nitems = r.n, a.big = r.big, a.nmax = r.rows;
     CK(launch_tc(kTcFar, a, st));
   }
-  CK(launch_tc_fix(P.panels_far, T.fix_far, T.nfix_far, int(tile_rows(2)), T.part_far, T.y, n, st));
+  CK(launch_tc_fix(P.panels_far, T.fix_far, T.nfix_far, T.part_far, T.y, st));
   CK(launch_tc_combine(T.y, op->nslots, n, op->d_perm, y, ldy, nrhs, st));
 }
 

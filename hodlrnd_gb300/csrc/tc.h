@@ -21,6 +21,11 @@ namespace hodlr {
 
 constexpr int kTcRhs = 64;     // right-hand sides per block
 constexpr int kTcMaxSegs = 256;  // segments of one panel item (the host splits longer items)
+// Output rows of one item: panels above 32 rows go in items of 64 rows, and z
+// groups hold at most 64 rows -- so a CTA holds at most 64 tensor-memory
+// columns and 8 CTAs share an SM.  Split items' partial sums are blocks of
+// kTcRows rows.
+constexpr int kTcRows = 64;
 
 // kind of product: z = V^T x (one item per low-rank block), near-field panels
 // (FP64 tiles), far-field panels (BF16 dense tiles and U factors)
@@ -42,7 +47,7 @@ struct TcZGroup {
   int32_t col0;    // the first column's point within the source node (its row of V): 0 unless a column run
 };
 // A source node with more points than kTcZCols is split into column runs
-// whose partial sums (blocks of 256 rows x 64) a fix-up adds into z.
+// whose partial sums (blocks of kTcRows rows x 64) a fix-up adds into z.
 constexpr int kTcZCols = 256;
 struct TcZRow {        // row i of a split group: where its z goes
   int64_t zpos;
@@ -64,8 +69,7 @@ struct TcLaunch {
   const Seg* segs;
   const Item* items;
   int nitems;
-  int big;          // items are row tiles of panels above 32 rows
-  int tile_rows;    // rows of one tile of the stored precision (big items)
+  int big;          // items are 64-row chunks of panels above 32 rows
   // z products: blocks, groups by source node, group entries
   const ZBlock* zb;
   const TcZGroup* zgroups;
@@ -86,8 +90,8 @@ cudaError_t launch_tc_combine(const float* y, int nslots, int64_t n, const int64
 // z of split z groups: in[zpos * 64 + r] = zscale * sum over the group's part blocks
 cudaError_t launch_tc_zfix(const TcZFix* fix, int nfix, int max_rows, const TcZRow* rows, const float* zpart,
                            float* in, cudaStream_t st);
-// adds split panels' partial row blocks into their output rows (fix-up, as panel_fix_kernel)
-cudaError_t launch_tc_fix(const Panel* panels, const PanelFix* fix, int nfix, int rows_per_item, const float* part,
-                          float* y, int64_t n, cudaStream_t st);
+// adds split panels' partial row blocks (kTcRows rows each) into their output rows
+cudaError_t launch_tc_fix(const Panel* panels, const PanelFix* fix, int nfix, const float* part, float* y,
+                          cudaStream_t st);
 
 }  // namespace hodlr

@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
 // ---- HODLR products for 64 right-hand sides (tc.h) ------------------------
 //
 // One CTA of 128 threads works through items (persistent: item it, it +
-// gridDim.x, ...).  An item is an output-row chunk (rows <= 256) and a
+// gridDim.x, ...).  An item is an output-row chunk (rows <= 64) and a
 // sequence of input columns -- all columns of its segments, in order; for a
 // z item, the rows of V.  Columns go in steps of 16: per step the CTA writes
 // the A tile (the 16 columns' inputs for 64 right-hand sides, split hi / lo)
@@ -128,7 +128,7 @@ constexpr int kTcStartBytes = (kTcMaxSegs + 1 + 31) / 32 * 32 * 4;
 constexpr int kTcPanelTable = kTcStartBytes + kTcMaxSegs * int(sizeof(Seg));
 template <int KIND>
 __host__ __device__ constexpr int tc_table_bytes() {
-  return KIND == kTcZ ? 256 * int(sizeof(TcRow)) : kTcPanelTable;
+  return KIND == kTcZ ? kTcRows * int(sizeof(TcRow)) : kTcPanelTable;
 }
 template <int KIND>
 __host__ __device__ constexpr int tc_smem_bytes(int npad) {
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
       outp = a.in;
       out_base = 0;  // rows carry their z positions
       // row table: entry e covers rows re .. re + nk - 1 (prefix over entries by warp 0)
-      const int ne = G.e_end - G.e_begin;  // <= 256: every entry has a row
+      const int ne = G.e_end - G.e_begin;  // <= kTcRows: every entry has a row
       if (warp == 0) {
         int32_t run = 0;
         for (int w0 = 0; w0 < ne; w0 += 32) {
@@ -208,9 +208,9 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
         }
       }
       __syncthreads();
-      TcRow rw[2];
+      TcRow rw[1];
       int nr = 0;
-      for (int i = t; i < rows && nr < 2; i += kTcThreads, nr++) {
+      for (int i = t; i < rows && nr < 1; i += kTcThreads, nr++) {
         int lo = 0, hi = ne - 1;
         while (lo < hi) {
           const int mid = (lo + hi + 1) >> 1;
@@ -227,15 +227,16 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
       }
       __syncthreads();  // the entry starts are read; the rows overwrite them
       nr = 0;
-      for (int i = t; i < rows && nr < 2; i += kTcThreads, nr++) zrow[i] = rw[nr];
+      for (int i = t; i < rows && nr < 1; i += kTcThreads, nr++) zrow[i] = rw[nr];
       __syncthreads();
     } else {
       const Item I = a.items[item];
       const Panel P = a.panels[I.panel];
       m = P.m;
-      tile = a.big ? I.chunk : 0;
-      row0 = tile * a.tile_rows;
-      rows = a.big ? min(a.tile_rows, m - row0) : m;
+      // big panels: rows row0 .. row0 + 63, inside one storage tile (its rows a multiple of 64)
+      row0 = a.big ? I.chunk * kTcRows : 0;
+      tile = int(row0 / tile_rows(int(sizeof(TB))));
+      rows = a.big ? min(kTcRows, m - row0) : m;
       qb = I.seg_b;
       nseg = I.seg_e - I.seg_b;
       if (I.part < 0) {
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
         out_base = P.yoff + row0;
       } else {
         outp = a.part;
-        out_base = int64_t(I.part) * a.tile_rows;
+        out_base = int64_t(I.part) * kTcRows;
       }
       // column starts of the segments (exclusive prefix sum), 32 at a time by warp 0
       if (warp == 0) {
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
             if (a.big) {
               const int esz = int(sizeof(TB));
               const int64_t T = tile_rows(esz), h = tile_height(m, tile, esz);
-              col.ptr = A + int64_t(tile) * T * S.K + int64_t(j) * h;
+              col.ptr = A + int64_t(tile) * T * S.K + int64_t(j) * h + (row0 - int64_t(tile) * T);
             } else {
               col.ptr = A + int64_t(j) * m;
             }
@@ -342,24 +343,32 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
         *reinterpret_cast<uint4*>(sa + umma_kmajor_offset(r, 8 * h, 2)) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
         *reinterpret_cast<uint4*>(sa + umma_kmajor_offset(r + 64, 8 * h, 2)) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
       }
-      // B: chunk (row i, column half h) -> 8 entries; rows >= rows and invalid columns are zero
-      for (int ch = t; ch < npad * 2; ch += kTcThreads) {
-        const int i = ch % npad, h = ch / npad;
+      // B: chunk (row i, column half h) -> 8 entries; rows >= rows and invalid columns are zero.
+      // npad <= 64: at most one chunk per thread, its loads all issued before use
+      if (t < npad * 2) {
+        const int i = t % npad, h = t / npad;
+        TB raw[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const TcCol& col = tab[8 * h + u];
+          const bool ok = col.valid && i < rows;
+          if constexpr (KIND == kTcZ) {
+            // column c of the group = point c of the run: row i's V entry
+            const int64_t c = int64_t(s) * 16 + 8 * h + u;
+            raw[u] = ok ? zrow[i].v[c * zrow[i].vp] : TB(0);
+          } else {
+            raw[u] = ok ? static_cast<const TB*>(col.ptr)[i] : TB(0);
+          }
+        }
         uint32_t w[kTerms][4];
 #pragma unroll
         for (int u = 0; u < 8; u += 2) {
           uint16_t e[kTerms][2];
 #pragma unroll
           for (int d = 0; d < 2; d++) {
-            const TcCol& col = tab[8 * h + u + d];
-            const bool ok = col.valid && i < rows;
-            if constexpr (KIND == kTcZ) {
-              // column c of the group = point c of the source node: row i's V entry
-              const int64_t c = int64_t(s) * 16 + 8 * h + u + d;
-              e[0][d] = ok ? zrow[i].v[c * zrow[i].vp] : uint16_t(0);
-            } else if constexpr (KIND == kTcNear) {
+            if constexpr (KIND == kTcNear) {
               // three BF16 terms of the FP64 entry: a = t0 + t1 + t2 + O(2^-24 a)
-              const float f = ok ? float(static_cast<const double*>(col.ptr)[i]) : 0.f;
+              const float f = float(raw[u + d]);
               const uint16_t t0 = bf16_bits(f);
               const float r1 = f - bf16_value(t0);
               const uint16_t t1 = bf16_bits(r1);
@@ -368,7 +377,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
               e[1 % kTerms][d] = t1;
               e[2 % kTerms][d] = t2;
             } else {
-              e[0][d] = ok ? static_cast<const uint16_t*>(col.ptr)[i] : uint16_t(0);
+              e[0][d] = uint16_t(raw[u + d]);
             }
           }
 #pragma unroll
@@ -428,7 +437,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
               if (zpart < 0)
                 outp[zrow[i].zpos * kTcRhs + t] = val * zrow[i].zscale;
               else  // a column run of a split group: unscaled partial sums
-                a.part[(int64_t(zpart) * 256 + i) * kTcRhs + t] = val;
+                a.part[(int64_t(zpart) * kTcRows + i) * kTcRhs + t] = val;
             } else
               outp[(out_base + i) * kTcRhs + t] = val;
           }
@@ -479,25 +488,24 @@ __global__ void tc_zfix_kernel(const TcZFix* __restrict__ fix, int nfix, int max
     const TcZFix F = fix[f];
     if (i >= F.rows) continue;
     float v = 0.f;
-    for (int q = 0; q < F.count; q++) v += zpart[(int64_t(F.part + q) * 256 + i) * kTcRhs + r];
+    for (int q = 0; q < F.count; q++) v += zpart[(int64_t(F.part + q) * kTcRows + i) * kTcRhs + r];
     const TcZRow R = rows[F.row0 + i];
     in[R.zpos * kTcRhs + r] = R.zscale ? v * *R.zscale : v;
   }
 }
 
-__global__ void tc_fix_kernel(const Panel* __restrict__ panels, const PanelFix* __restrict__ fix, int nfix, int rpi,
+// One CTA per split item chunk: its rows x 64 sums of the partial blocks.
+__global__ void tc_fix_kernel(const Panel* __restrict__ panels, const PanelFix* __restrict__ fix,
                               const float* __restrict__ part, float* __restrict__ y) {
-  const int64_t total = int64_t(nfix) * rpi * kTcRhs;
-  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
-    const int f = int(e / (int64_t(rpi) * kTcRhs));
-    const int i = int((e / kTcRhs) % rpi), r = int(e % kTcRhs);
-    const PanelFix F = fix[f];
-    const Panel P = panels[F.panel];
-    const int row = F.chunk * rpi + i;
-    if (row >= P.m) continue;
+  const PanelFix F = fix[blockIdx.x];
+  const Panel P = panels[F.panel];
+  const int row0 = P.m > 32 ? F.chunk * kTcRows : 0;
+  const int rows = min(kTcRows, P.m - row0);
+  for (int e = threadIdx.x; e < rows * kTcRhs; e += blockDim.x) {
+    const int i = e / kTcRhs, r = e % kTcRhs;
     float v = 0.f;
-    for (int q = 0; q < F.count; q++) v += part[(int64_t(F.part + q) * rpi + i) * kTcRhs + r];
-    y[(P.yoff + row) * kTcRhs + r] = v;
+    for (int q = 0; q < F.count; q++) v += part[(int64_t(F.part + q) * kTcRows + i) * kTcRhs + r];
+    y[(P.yoff + row0 + i) * kTcRhs + r] = v;
   }
 }
 
@@ -508,7 +516,7 @@ static cudaError_t launch_tc_k(const TcLaunch& a, cudaStream_t st) {
   const int nitems = KIND == kTcZ ? a.nz : a.nitems;
   if (nitems <= 0) return cudaSuccess;
   const int npad = tc_npad(a.nmax);
-  if (npad < 16 || npad > 256) return cudaErrorInvalidValue;
+  if (npad < 16 || npad > kTcRows) return cudaErrorInvalidValue;
   uint32_t tcols = 32;
   while (tcols < uint32_t(npad)) tcols <<= 1;
   const int smem = tc_smem_bytes<KIND>(npad);
@@ -559,12 +567,11 @@ cudaError_t launch_tc_zfix(const TcZFix* fix, int nfix, int max_rows, const TcZR
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc_fix(const Panel* panels, const PanelFix* fix, int nfix, int rows_per_item, const float* part,
-                          float* y, int64_t n, cudaStream_t st) {
-  (void)n;
+cudaError_t launch_tc_fix(const Panel* panels, const PanelFix* fix, int nfix, const float* part, float* y,
+                          cudaStream_t st) {
   if (nfix <= 0) return cudaSuccess;
   count_launches(1);
-  tc_fix_kernel<<<1216, 256, 0, st>>>(panels, fix, nfix, rows_per_item, part, y);
+  tc_fix_kernel<<<nfix, 256, 0, st>>>(panels, fix, part, y);
   return cudaGetLastError();
 }
 
