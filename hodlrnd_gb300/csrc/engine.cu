@@ -239,7 +239,8 @@ struct hodlr_op {
     TcZFix* zfix = nullptr;  // split z groups
     TcZRow* zrows = nullptr;
     int nzfix = 0, zfix_rows = 0;
-    float *in = nullptr, *y = nullptr, *part_near = nullptr, *part_far = nullptr, *zpart = nullptr;
+    uint32_t* in = nullptr;  // [x | z], 64 right-hand sides, packed BF16 pairs
+    float *y = nullptr, *part_near = nullptr, *part_far = nullptr, *zpart = nullptr;
     unsigned int* status = nullptr;
     unsigned int* h_status = nullptr;
   } tc;
@@ -1963,7 +1964,7 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   T.nzfix = int(zfix.size());
   T.zpart = op->mem.alloc_n<float>(size_t(std::max(zparts, 1)) * kTcRows * kTcRhs, "tensor-core z partial sums");
   const int64_t n = op->n;
-  T.in = op->mem.alloc_n<float>(size_t(n + op->zlen) * kTcRhs, "tensor-core input (64 right-hand sides)");
+  T.in = op->mem.alloc_n<uint32_t>(size_t(n + op->zlen) * kTcRhs, "tensor-core input (64 right-hand sides)");
   T.y = op->mem.alloc_n<float>(size_t(n) * size_t(op->nslots) * kTcRhs, "tensor-core output slots");
   T.part_near = op->mem.alloc_n<float>(size_t(std::max(pn, 1)) * kTcRows * kTcRhs, "tensor-core partial rows");
   T.part_far = op->mem.alloc_n<float>(size_t(std::max(pf, 1)) * kTcRows * kTcRhs, "tensor-core partial rows");

@@ -2,14 +2,17 @@
 // (tcgen05.cu).
 //
 // Vectors are "point major": entry p of a 64-column block sits at
-// v[p * 64 .. p * 64 + 63] (FP32), for the inputs [x | z] (tree positions,
-// then the z values of the low-rank blocks) and for the output slots.  Each
-// product is D (128 x N) = A (128 x K) B^T on the tensor cores: A holds the 64
-// right-hand sides split into BF16 high and low parts (rows 0-63 and 64-127,
-// x = hi + lo to about 2^-17 relative), B the factor columns (N output rows,
-// K input columns in steps of 16), D the FP32 accumulator in tensor memory;
-// the result is D_hi + D_lo.  BF16 factors are taken as they are stored; FP64
-// near-field entries are split into three BF16 terms (about 2^-24 relative).
+// v[p * 64 .. p * 64 + 63], for the inputs [x | z] (tree positions, then the
+// z values of the low-rank blocks) and for the FP32 output slots.  Inputs are
+// stored split once: each value as a packed pair of BF16 words, the high part
+// in the low half-word and the rest in the high half-word (x = hi + lo to
+// about 2^-17 relative).  Each product is D (128 x N) = A (128 x K) B^T on the
+// tensor cores: A holds the 64 right-hand sides' high parts (rows 0-63) and
+// low parts (rows 64-127), B the factor columns (N output rows, K input
+// columns in steps of 32), D the FP32 accumulator in tensor memory; the
+// result is D_hi + D_lo.  BF16 factors times their input scale (BF16 dense
+// tiles) are split into two BF16 terms, FP64 near-field entries into three
+// (about 2^-24 relative).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -59,7 +62,7 @@ struct TcZFix {
 };
 
 struct TcLaunch {
-  float* in;        // [x | z], point major
+  uint32_t* in;     // [x | z], point major, packed BF16 pairs
   float* y;         // output slots, point major: slot s of row p at (s * n + p) * 64
   float* part;      // partial row blocks of split panels: (part * rows_per_item + i) * 64
   int64_t n;        // points (rows of one slot)
@@ -80,16 +83,16 @@ struct TcLaunch {
 
 // One launch per kind (and small / big items); asynchronous on st.
 cudaError_t launch_tc(TcKind kind, const TcLaunch& a, cudaStream_t st);
-// in[p * 64 + r] = x[perm[p] + r * ld_x] (x in caller order, column major FP32), p < n, r < nrhs (<= 64);
-// columns r >= nrhs are zero
-cudaError_t launch_tc_gather(const float* x, int64_t ld_x, int nrhs, const int64_t* perm, int64_t n, float* in,
+// in[p * 64 + r] = split(x[perm[p] + r * ld_x]) (x in caller order, column major FP32), p < n,
+// r < nrhs (<= 64); columns r >= nrhs are zero
+cudaError_t launch_tc_gather(const float* x, int64_t ld_x, int nrhs, const int64_t* perm, int64_t n, uint32_t* in,
                              cudaStream_t st);
 // y_out[perm[p] + r * ld_out] = sum over slots s of y[(s * n + p) * 64 + r], r < nrhs
 cudaError_t launch_tc_combine(const float* y, int nslots, int64_t n, const int64_t* perm, float* out,
                               int64_t ld_out, int nrhs, cudaStream_t st);
 // z of split z groups: in[zpos * 64 + r] = zscale * sum over the group's part blocks
 cudaError_t launch_tc_zfix(const TcZFix* fix, int nfix, int max_rows, const TcZRow* rows, const float* zpart,
-                           float* in, cudaStream_t st);
+                           uint32_t* in, cudaStream_t st);
 // adds split panels' partial row blocks (kTcRows rows each) into their output rows
 cudaError_t launch_tc_fix(const Panel* panels, const PanelFix* fix, int nfix, const float* part, float* y,
                           cudaStream_t st);

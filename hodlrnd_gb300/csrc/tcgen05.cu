@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const uint16_t* __rest
 // and returns.
 
 constexpr int kTcThreads = 128;
-constexpr int kTcA = 128 * 16 * 2;  // bytes of one A tile (128 rows x 16 BF16)
+constexpr int kStepK = 32;               // columns per step (two MMAs of K = 16)
+constexpr int kTcA = 128 * kStepK * 2;  // bytes of one A tile (128 rows x kStepK BF16)
 
 template <int KIND>
 struct TcB;
@@ -102,7 +103,7 @@ struct TcB<kTcZ> {
 template <>
 struct TcB<kTcFar> {
   using T = uint16_t;
-  static constexpr int kTerms = 1;
+  static constexpr int kTerms = 2;  // the entry times its input scale, in two BF16 terms
 };
 template <>
 struct TcB<kTcNear> {
@@ -114,7 +115,7 @@ struct TcB<kTcNear> {
 __host__ __device__ constexpr int tc_npad(int rows) { return (rows + 15) / 16 * 16; }
 template <int KIND>
 __host__ __device__ constexpr int tc_buf_bytes(int npad) {
-  return kTcA + TcB<KIND>::kTerms * npad * 16 * 2;
+  return kTcA + TcB<KIND>::kTerms * npad * kStepK * 2;
 }
 struct TcRow {  // z groups: one output row
   const uint16_t* v;  // V_b + k: entry j (column j) at v[j * vp]
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
   extern __shared__ __align__(1024) unsigned char tsm[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(tsm);        // 2 buffers
   uint32_t* slot = reinterpret_cast<uint32_t*>(tsm + 16);  // tensor-memory address
-  TcCol* tab = reinterpret_cast<TcCol*>(tsm + 64);         // 16 columns of the step being written
+  TcCol* tab = reinterpret_cast<TcCol*>(tsm + 64);         // kStepK columns of the step being written
   int32_t* cstart = reinterpret_cast<int32_t*>(tsm + 1024);  // first column of each segment of the item
   Seg* sseg = reinterpret_cast<Seg*>(tsm + 1024 + kTcStartBytes);  // the item's segment records
   TcRow* zrow = reinterpret_cast<TcRow*>(tsm + 1024);        // z groups: the rows
@@ -177,8 +178,8 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
     // ---- the item: rows, output, columns
     int rows, nseg = 1, qb = 0;
     int64_t C;
-    int64_t out_base;  // output row 0: index (in 64-entry rows) into y, part, or in (z)
-    float* outp;
+    int64_t out_base = 0;  // output row 0: index (in 64-entry rows) into y or part (panels)
+    float* outp = nullptr;
     int row0 = 0, tile = 0, m = 0;
     int64_t zx = 0;
     int zpart = -1;
@@ -188,7 +189,6 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
       C = G.n;
       zx = G.x_off;
       zpart = G.part;
-      outp = a.in;
       out_base = 0;  // rows carry their z positions
       // row table: entry e covers rows re .. re + nk - 1 (prefix over entries by warp 0)
       const int ne = G.e_end - G.e_begin;  // <= kTcRows: every entry has a row
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
     }
     const int npad = tc_npad(rows);
     const uint32_t idesc = umma_idesc_bf16(128, npad);
-    const int nsteps = int((C + 15) / 16);
+    const int nsteps = int((C + kStepK - 1) / kStepK);
     for (int s = 0; s < nsteps && alive; s++) {
       const int b = s & 1;
       unsigned char* sa = buf0 + b * bufb;
@@ -289,9 +289,9 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
         }
         tc_fence_after();
       }
-      // step table: column c = 16 s + t of the item (threads 0..15)
-      if (t < 16) {
-        const int64_t c = int64_t(s) * 16 + t;
+      // step table: column c = kStepK s + t of the item (threads 0 .. kStepK - 1)
+      if (t < kStepK) {
+        const int64_t c = int64_t(s) * kStepK + t;
         TcCol col{nullptr, 0, 1.f, 0};
         if (c < C) {
           col.valid = 1;
@@ -322,31 +322,34 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
         tab[t] = col;
       }
       __syncthreads();
-      // A: thread t -> right-hand side r = t & 63, columns 8 h .. 8 h + 7, h = t >> 6;
-      // hi part at row r, lo part at row r + 64
+      // A: thread t -> right-hand side r = t & 63, columns 16 h .. 16 h + 15 (h = t >> 6) from the
+      // packed inputs (BF16 high part in the low half-word): high parts at row r, low parts at r + 64
       {
         const int r = t & 63, h = t >> 6;
-        uint32_t hw[4], lw[4];
+        uint32_t w[16];
 #pragma unroll
-        for (int u = 0; u < 8; u += 2) {
-          float v[2];
-#pragma unroll
-          for (int e = 0; e < 2; e++) {
-            const TcCol& col = tab[8 * h + u + e];
-            v[e] = col.valid ? a.in[col.pos * kTcRhs + r] * col.scale : 0.f;
-          }
-          const uint16_t h0 = bf16_bits(v[0]), h1 = bf16_bits(v[1]);
-          const uint16_t l0 = bf16_bits(v[0] - bf16_value(h0)), l1 = bf16_bits(v[1] - bf16_value(h1));
-          hw[u / 2] = uint32_t(h0) | (uint32_t(h1) << 16);
-          lw[u / 2] = uint32_t(l0) | (uint32_t(l1) << 16);
+        for (int u = 0; u < 16; u++) {
+          const TcCol& col = tab[16 * h + u];
+          w[u] = col.valid ? a.in[col.pos * kTcRhs + r] : 0u;
         }
-        *reinterpret_cast<uint4*>(sa + umma_kmajor_offset(r, 8 * h, 2)) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-        *reinterpret_cast<uint4*>(sa + umma_kmajor_offset(r + 64, 8 * h, 2)) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+#pragma unroll
+        for (int g = 0; g < 2; g++) {
+          uint32_t hw[4], lw[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            hw[u] = __byte_perm(w[8 * g + 2 * u], w[8 * g + 2 * u + 1], 0x5410);
+            lw[u] = __byte_perm(w[8 * g + 2 * u], w[8 * g + 2 * u + 1], 0x7632);
+          }
+          const uint32_t k = uint32_t(16 * h + 8 * g);
+          *reinterpret_cast<uint4*>(sa + umma_kmajor_offset(r, k, kStepK / 8)) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4*>(sa + umma_kmajor_offset(r + 64, k, kStepK / 8)) =
+              make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
       }
-      // B: chunk (row i, column half h) -> 8 entries; rows >= rows and invalid columns are zero.
-      // npad <= 64: at most one chunk per thread, its loads all issued before use
-      if (t < npad * 2) {
-        const int i = t % npad, h = t / npad;
+      // B: chunk (row i, column group h of 8) -> 8 entries in kTerms BF16 terms; rows >= rows and
+      // invalid columns are zero.  Every load of a chunk is issued before its entries are used.
+      for (int ch = t; ch < npad * (kStepK / 8); ch += kTcThreads) {
+        const int i = ch % npad, h = ch / npad;
         TB raw[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
@@ -354,13 +357,13 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
           const bool ok = col.valid && i < rows;
           if constexpr (KIND == kTcZ) {
             // column c of the group = point c of the run: row i's V entry
-            const int64_t c = int64_t(s) * 16 + 8 * h + u;
+            const int64_t c = int64_t(s) * kStepK + 8 * h + u;
             raw[u] = ok ? zrow[i].v[c * zrow[i].vp] : TB(0);
           } else {
             raw[u] = ok ? static_cast<const TB*>(col.ptr)[i] : TB(0);
           }
         }
-        uint32_t w[kTerms][4];
+        uint32_t wq[kTerms][4];
 #pragma unroll
         for (int u = 0; u < 8; u += 2) {
           uint16_t e[kTerms][2];
@@ -372,31 +375,43 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
               const uint16_t t0 = bf16_bits(f);
               const float r1 = f - bf16_value(t0);
               const uint16_t t1 = bf16_bits(r1);
-              const uint16_t t2 = bf16_bits(r1 - bf16_value(t1));
               e[0][d] = t0;
               e[1 % kTerms][d] = t1;
-              e[2 % kTerms][d] = t2;
+              e[2 % kTerms][d] = bf16_bits(r1 - bf16_value(t1));
+            } else if constexpr (KIND == kTcFar) {
+              // the stored entry times its column's input scale (BF16 dense tiles; 1 otherwise)
+              // in two BF16 terms (2^-16 relative)
+              const float f = bf16_value(uint16_t(raw[u + d])) * tab[8 * h + u + d].scale;
+              const uint16_t t0 = bf16_bits(f);
+              e[0][d] = t0;
+              e[1 % kTerms][d] = bf16_bits(f - bf16_value(t0));
             } else {
               e[0][d] = uint16_t(raw[u + d]);
             }
           }
 #pragma unroll
-          for (int q = 0; q < kTerms; q++) w[q][u / 2] = uint32_t(e[q][0]) | (uint32_t(e[q][1]) << 16);
+          for (int q = 0; q < kTerms; q++) wq[q][u / 2] = uint32_t(e[q][0]) | (uint32_t(e[q][1]) << 16);
         }
 #pragma unroll
         for (int q = 0; q < kTerms; q++)
-          *reinterpret_cast<uint4*>(sb + q * npad * 32 + umma_kmajor_offset(i, 8 * h, 2)) =
-              make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+          *reinterpret_cast<uint4*>(sb + q * npad * (kStepK * 2) + umma_kmajor_offset(i, 8 * h, kStepK / 8)) =
+              make_uint4(wq[q][0], wq[q][1], wq[q][2], wq[q][3]);
       }
       fence_proxy_async();  // this thread's operand writes, visible to the tensor core
       tc_fence_before();
       __syncthreads();
       tc_fence_after();
       if (t == 0) {
-        const uint64_t da = umma_desc(sa, 128, 256);
+        // K-major tiles with kStepK / 8 core matrices along K: leading offset 128 B, stride kStepK * 16 B;
+        // each MMA consumes 16 columns (two core matrices, 256 B further along)
 #pragma unroll
-        for (int q = 0; q < kTerms; q++)
-          umma_bf16(tmem, da, umma_desc(sb + q * npad * 32, 128, 256), idesc, (s > 0 || q > 0) ? 1u : 0u);
+        for (int k = 0; k < kStepK / 16; k++) {
+          const uint64_t da = umma_desc(sa + 256 * k, 128, kStepK * 16);
+#pragma unroll
+          for (int q = 0; q < kTerms; q++)
+            umma_bf16(tmem, da, umma_desc(sb + q * npad * (kStepK * 2) + 256 * k, 128, kStepK * 16), idesc,
+                      (s > 0 || k > 0 || q > 0) ? 1u : 0u);
+        }
         umma_commit(bar + b);
       }
       commits[b]++;
@@ -435,7 +450,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
             const float val = v[q] + xch[q * 64 + t];
             if constexpr (KIND == kTcZ) {
               if (zpart < 0)
-                outp[zrow[i].zpos * kTcRhs + t] = val * zrow[i].zscale;
+                a.in[zrow[i].zpos * kTcRhs + t] = split_pack(val * zrow[i].zscale);
               else  // a column run of a split group: unscaled partial sums
                 a.part[(int64_t(zpart) * kTcRows + i) * kTcRhs + t] = val;
             } else
@@ -457,12 +472,12 @@ __global__ void __launch_bounds__(kTcThreads) tc_kernel(TcLaunch a, int npad_max
 }
 
 __global__ void tc_gather_kernel(const float* __restrict__ x, int64_t ld_x, int nrhs, const int64_t* __restrict__ perm,
-                                 int64_t n, float* __restrict__ in) {
+                                 int64_t n, uint32_t* __restrict__ in) {
   const int64_t total = n * kTcRhs;
   for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
     const int64_t p = e / kTcRhs;
     const int r = int(e % kTcRhs);
-    in[e] = r < nrhs ? x[perm[p] + int64_t(r) * ld_x] : 0.f;
+    in[e] = split_pack(r < nrhs ? x[perm[p] + int64_t(r) * ld_x] : 0.f);
   }
 }
 
@@ -480,7 +495,7 @@ __global__ void tc_combine_kernel(const float* __restrict__ y, int nslots, int64
 }
 
 __global__ void tc_zfix_kernel(const TcZFix* __restrict__ fix, int nfix, int max_rows,
-                               const TcZRow* __restrict__ rows, const float* __restrict__ zpart, float* __restrict__ in) {
+                               const TcZRow* __restrict__ rows, const float* __restrict__ zpart, uint32_t* __restrict__ in) {
   const int64_t total = int64_t(nfix) * max_rows * kTcRhs;
   for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
     const int f = int(e / (int64_t(max_rows) * kTcRhs));
@@ -490,7 +505,7 @@ __global__ void tc_zfix_kernel(const TcZFix* __restrict__ fix, int nfix, int max
     float v = 0.f;
     for (int q = 0; q < F.count; q++) v += zpart[(int64_t(F.part + q) * kTcRows + i) * kTcRhs + r];
     const TcZRow R = rows[F.row0 + i];
-    in[R.zpos * kTcRhs + r] = R.zscale ? v * *R.zscale : v;
+    in[R.zpos * kTcRhs + r] = split_pack(R.zscale ? v * *R.zscale : v);
   }
 }
 
@@ -545,7 +560,7 @@ cudaError_t launch_tc(TcKind kind, const TcLaunch& a, cudaStream_t st) {
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_tc_gather(const float* x, int64_t ld_x, int nrhs, const int64_t* perm, int64_t n, float* in,
+cudaError_t launch_tc_gather(const float* x, int64_t ld_x, int nrhs, const int64_t* perm, int64_t n, uint32_t* in,
                              cudaStream_t st) {
   count_launches(1);
   tc_gather_kernel<<<1216, 256, 0, st>>>(x, ld_x, nrhs, perm, n, in);
@@ -560,7 +575,7 @@ cudaError_t launch_tc_combine(const float* y, int nslots, int64_t n, const int64
 }
 
 cudaError_t launch_tc_zfix(const TcZFix* fix, int nfix, int max_rows, const TcZRow* rows, const float* zpart,
-                           float* in, cudaStream_t st) {
+                           uint32_t* in, cudaStream_t st) {
   if (nfix <= 0) return cudaSuccess;
   count_launches(1);
   tc_zfix_kernel<<<1216, 256, 0, st>>>(fix, nfix, max_rows, rows, zpart, in);

@@ -102,5 +102,11 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 // BF16 bits of an FP32 value, rounded to nearest even
 __device__ __forceinline__ uint16_t bf16_bits(float f) { return __bfloat16_as_ushort(__float2bfloat16_rn(f)); }
 __device__ __forceinline__ float bf16_value(uint16_t b) { return __uint_as_float(uint32_t(b) << 16); }
+// An FP32 value as two BF16 words packed in 32 bits: the value rounded to
+// BF16 in the low half-word, the rounded remainder in the high half-word.
+__device__ __forceinline__ uint32_t split_pack(float v) {
+  const uint16_t h = bf16_bits(v);
+  return uint32_t(h) | (uint32_t(bf16_bits(v - bf16_value(h))) << 16);
+}
 
 }  // namespace hodlr
