@@ -30,9 +30,11 @@ struct PointsDev {
 // One matrix entry A(i, j) for tree positions i, j (kernel_function::getRow /
 // getCol / getMatrix + the user getMatrixEntry, include/kernel_function.hpp:20-53).
 // d2 is accumulated in dimension order with one rounding per operation (the
-// explicit _rn intrinsics keep the compiler from contracting into FMAs), so
-// the entry is bit-identical to the scalar host code; sqrt and division are
-// IEEE round-to-nearest on both sides.
+// explicit _rn intrinsics keep the compiler from contracting into FMAs); sqrt
+// and division are IEEE round-to-nearest on both sides, so the 1/r and 1/r^2
+// entries are bit-identical to the scalar host code.  The log r and e^-r
+// kinds call CUDA's log and exp, which need not round as the host's libm
+// does: those entries agree to a few units in the last place.
 template <int D>
 __device__ __forceinline__ double kernel_entry(const PointsDev& P, const KernelDev& K, int64_t i, int64_t j,
                                                const double* xi) {
