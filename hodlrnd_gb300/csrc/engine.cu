@@ -723,12 +723,17 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     P = PointsDev{jp, ntot};
     d_lmap = static_cast<const int32_t*>(s_lmap.p);
   }
+  // large blocks first keeps the CTA-team launch ahead of the warp teams: a
+  // stable counting sort by max(m, n), descending (the sizes are node sizes)
   std::vector<size_t> todo(nb);
-  for (size_t g = 0; g < nb; g++) todo[g] = g;
-  // large blocks first keeps the CTA-team launch ahead of the warp teams
-  std::stable_sort(todo.begin(), todo.end(), [&](size_t a, size_t b) {
-    return std::max(mm[a], nn[a]) > std::max(mm[b], nn[b]);
-  });
+  {
+    int32_t kmax = 0;
+    for (size_t g = 0; g < nb; g++) kmax = std::max(kmax, std::max(mm[g], nn[g]));
+    std::vector<size_t> start(size_t(kmax) + 2, 0);
+    for (size_t g = 0; g < nb; g++) start[size_t(kmax - std::max(mm[g], nn[g])) + 1]++;
+    for (size_t k = 1; k < start.size(); k++) start[k] += start[k - 1];
+    for (size_t g = 0; g < nb; g++) todo[start[size_t(kmax - std::max(mm[g], nn[g]))]++] = g;
+  }
 
   KernelDev K{op0->kd.kind, op0->kd.scale, op0->kd.diag};
   struct Events {
@@ -783,14 +788,34 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     } else {
       while (pos < todo.size() && take(todo[pos])) pos++;
     }
-    desc.resize(batch.size());
-    for (auto& l : team_list) l.clear();
-    uint64_t ow = 0, ob = 0, ol = 0;
-    for (size_t q = 0; q < batch.size(); q++) {
-      const size_t g = batch[q];
+    // descriptors: per-block sizes and teams (parallel: the blocks are visited
+    // in size order, so their arrays are read at random), offsets by a prefix
+    // sum, then the descriptors (parallel again)
+    const size_t nq = batch.size();
+    desc.resize(nq);
+    std::vector<uint64_t> qw(nq + 1), qb(nq + 1), ql(nq + 1);
+    std::vector<int8_t> qteam(nq);
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < int64_t(nq); q++) {
+      const size_t g = batch[size_t(q)];
+      qw[size_t(q) + 1] = ws_need(g);
+      qb[size_t(q) + 1] = uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32);
+      ql[size_t(q) + 1] = uint64_t(2 * (std::min(mm[g], nn[g]) + 2));
+      qteam[size_t(q)] = int8_t(aca_team(mm[g], nn[g]));
+    }
+    qw[0] = qb[0] = ql[0] = 0;
+    for (size_t q = 0; q < nq; q++) {
+      qw[q + 1] += qw[q];
+      qb[q + 1] += qb[q];
+      ql[q + 1] += ql[q];
+    }
+    const uint64_t ow = qw[nq], ob = qb[nq], ol = ql[nq];
+#pragma omp parallel for schedule(static)
+    for (int64_t q = 0; q < int64_t(nq); q++) {
+      const size_t g = batch[size_t(q)];
       const hodlr_op* op = ops[size_t(job[g])];
       const FarBlock& f = op->far[size_t(int64_t(g) - boff[size_t(job[g])])];
-      AcaBlockDesc& d = desc[q];
+      AcaBlockDesc& d = desc[size_t(q)];
       d.t_map = tmap[g];
       d.s_map = smap[g];
       d.m = mm[g];
@@ -798,16 +823,14 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       d.cap = cap[g];
       // the pivot lists hold every rank the block can reach, also after it grows into the arena
       d.lcap = std::min(mm[g], nn[g]);
-      d.ws = int64_t(ow);
-      d.bits = int64_t(ob);
-      d.lists = int64_t(ol);
+      d.ws = int64_t(qw[size_t(q)]);
+      d.bits = int64_t(qb[size_t(q)]);
+      d.lists = int64_t(ql[size_t(q)]);
       d.seed = block_seed(f.level, f.t, f.s);
       d.kscale = joint ? op->kd.scale : 0.0;
-      ow += ws_need(g);
-      ob += uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32);
-      ol += uint64_t(2 * (std::min(mm[g], nn[g]) + 2));
-      team_list[size_t(aca_team(mm[g], nn[g]))].push_back(int32_t(q));
     }
+    for (auto& l : team_list) l.clear();
+    for (size_t q = 0; q < nq; q++) team_list[size_t(qteam[q])].push_back(int32_t(q));
     // one index array, the team kinds one after another (largest blocks first)
     std::vector<int32_t> lst;
     AcaLists al;
@@ -856,10 +879,11 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       t_kernel += 1e-3 * double(ms);
     }
     // compaction of the finished blocks: one chunk per operator and batch
-    cds.clear();
     std::vector<uint64_t> bytes(nops, 0), off(batch.size(), 0);
+    std::vector<int64_t> kidx(batch.size() + 1, 0);  // position among the blocks compacted (dense or rank > 0)
     for (size_t q = 0; q < batch.size(); q++) {
       const size_t g = batch[q];
+      kidx[q + 1] = kidx[q];
       if (out[q].flags & kAcaOverflow) {
         cap[g] = std::min(std::min(mm[g], nn[g]), cap[g] * 4);
         retry.push_back(g);
@@ -872,7 +896,9 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       off[q] = bytes[size_t(job[g])];
       const int64_t r = op->rank[b];
       bytes[size_t(job[g])] += far_u_bytes(mm[g], nn[g], r, op->dense[b], fp) + far_v_bytes(nn[g], r, op->dense[b], fp);
+      if (op->dense[b] || r > 0) kidx[q + 1]++;
     }
+    cds.resize(size_t(kidx[batch.size()]));
     std::vector<char*> chunk(nops, nullptr);
     for (size_t j = 0; j < nops; j++)
       if (bytes[j] > 0) {
@@ -880,7 +906,9 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
         ops[j]->far_chunks.push_back(chunk[j]);
         CK(cudaMemsetAsync(chunk[j], 0, bytes[j], st));  // tile padding rows must read as zero
       }
-    for (size_t q = 0; q < batch.size(); q++) {
+#pragma omp parallel for schedule(static)
+    for (int64_t qi = 0; qi < int64_t(batch.size()); qi++) {
+      const size_t q = size_t(qi);
       const size_t g = batch[q];
       if (out[q].flags & kAcaOverflow) continue;
       hodlr_op* op = ops[size_t(job[g])];
@@ -909,7 +937,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       c.kscale = desc[q].kscale;
       op->uptr[b] = c.u_dst;
       op->vptr[b] = c.v_dst;
-      if (op->dense[b] || op->rank[b] > 0) cds.push_back(c);
+      if (kidx[q + 1] > kidx[q]) cds[size_t(kidx[q])] = c;
     }
     for (size_t b0 = 0; b0 < cds.size(); b0 += max_cd) {
       const size_t k = std::min(max_cd, cds.size() - b0);
@@ -925,8 +953,10 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     // the FP64 factors of the same blocks, for operators that keep them
     if (fp != Prec::kD) {
       std::vector<uint64_t> bytes64(nops, 0), off64(batch.size(), 0);
+      std::vector<int64_t> kidx64(batch.size() + 1, 0);
       for (size_t q = 0; q < batch.size(); q++) {
         const size_t g = batch[q];
+        kidx64[q + 1] = kidx64[q];
         hodlr_op* op = ops[size_t(job[g])];
         if (!op->has_ref || (out[q].flags & kAcaOverflow)) continue;
         const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
@@ -934,6 +964,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
         const int64_t r = op->rank[b];
         bytes64[size_t(job[g])] += far_u_bytes(mm[g], nn[g], r, op->dense[b], Prec::kD) +
                                    far_v_bytes(nn[g], r, op->dense[b], Prec::kD);
+        if (op->dense[b] || r > 0) kidx64[q + 1]++;
       }
       std::vector<char*> chunk64(nops, nullptr);
       bool any = false;
@@ -944,13 +975,14 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
           any = true;
         }
       if (any) {
-        std::vector<CompactDesc> cd64;
-        for (size_t q = 0; q < batch.size(); q++) {
+        std::vector<CompactDesc> cd64(static_cast<size_t>(kidx64[batch.size()]));
+#pragma omp parallel for schedule(static)
+        for (int64_t qi = 0; qi < int64_t(batch.size()); qi++) {
+          const size_t q = size_t(qi);
+          if (kidx64[q + 1] == kidx64[q]) continue;  // not kept (no FP64 copy, overflow, or rank 0)
           const size_t g = batch[q];
           hodlr_op* op = ops[size_t(job[g])];
-          if (!op->has_ref || (out[q].flags & kAcaOverflow)) continue;
           const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
-          if (!op->dense[b] && op->rank[b] <= 0) continue;
           char* ch = chunk64[size_t(job[g])];
           CompactDesc c;
           c.t_begin = tb[g];
@@ -970,7 +1002,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
           c.kscale = desc[q].kscale;
           op->uptr64[b] = c.u_dst;
           op->vptr64[b] = c.v_dst;
-          cd64.push_back(c);
+          cd64[size_t(kidx64[q])] = c;
         }
         for (size_t b0 = 0; b0 < cd64.size(); b0 += max_cd) {
           const size_t k = std::min(max_cd, cd64.size() - b0);
