@@ -528,14 +528,24 @@ void launch_sub(const AcaArgs& a, const int32_t* list, int count, cudaStream_t s
 }
 
 template <int D>
+void launch_kind(const AcaArgs& a, const AcaLists& L, int kind, cudaStream_t st) {
+  if (L.n[kind] <= 0) return;
+  switch (kind) {
+    case kAcaTeamCta:
+      aca_cta_kernel<D><<<aca_grid(a, L.n[kAcaTeamCta], 1), 256, 0, st>>>(a, L.list[kAcaTeamCta], L.n[kAcaTeamCta]);
+      break;
+    case kAcaTeamWarp:
+      aca_warp_kernel<D><<<aca_grid(a, L.n[kAcaTeamWarp], 4), 128, 0, st>>>(a, L.list[kAcaTeamWarp],
+                                                                            L.n[kAcaTeamWarp]);
+      break;
+    case kAcaTeam16: launch_sub<D, 16>(a, L.list[kAcaTeam16], L.n[kAcaTeam16], st); break;
+    case kAcaTeam8: launch_sub<D, 8>(a, L.list[kAcaTeam8], L.n[kAcaTeam8], st); break;
+  }
+}
+
+template <int D>
 void launch_d(const AcaArgs& a, const AcaLists& L, cudaStream_t st) {
-  if (L.n[kAcaTeamCta] > 0)
-    aca_cta_kernel<D><<<aca_grid(a, L.n[kAcaTeamCta], 1), 256, 0, st>>>(a, L.list[kAcaTeamCta], L.n[kAcaTeamCta]);
-  if (L.n[kAcaTeamWarp] > 0)
-    aca_warp_kernel<D><<<aca_grid(a, L.n[kAcaTeamWarp], 4), 128, 0, st>>>(a, L.list[kAcaTeamWarp],
-                                                                          L.n[kAcaTeamWarp]);
-  if (L.n[kAcaTeam16] > 0) launch_sub<D, 16>(a, L.list[kAcaTeam16], L.n[kAcaTeam16], st);
-  if (L.n[kAcaTeam8] > 0) launch_sub<D, 8>(a, L.list[kAcaTeam8], L.n[kAcaTeam8], st);
+  for (int k : {kAcaTeamCta, kAcaTeamWarp, kAcaTeam16, kAcaTeam8}) launch_kind<D>(a, L, k, st);
 }
 
 }  // namespace
@@ -546,6 +556,24 @@ int aca_team(int m, int n) {
   if (mx <= 16) return kAcaTeam16;
   if (mx <= 256) return kAcaTeamWarp;
   return kAcaTeamCta;
+}
+
+cudaError_t launch_aca_kind(int ndim, const AcaArgs& a, const AcaLists& L, int kind, cudaStream_t st) {
+  if (kind < 0 || kind >= kAcaTeamKinds) return cudaErrorInvalidValue;
+  if (L.n[kind] <= 0) return cudaSuccess;
+  count_launches(1);
+  switch (ndim) {
+    case 1: launch_kind<1>(a, L, kind, st); break;
+    case 2: launch_kind<2>(a, L, kind, st); break;
+    case 3: launch_kind<3>(a, L, kind, st); break;
+    case 4: launch_kind<4>(a, L, kind, st); break;
+    case 5: launch_kind<5>(a, L, kind, st); break;
+    case 6: launch_kind<6>(a, L, kind, st); break;
+    case 7: launch_kind<7>(a, L, kind, st); break;
+    case 8: launch_kind<8>(a, L, kind, st); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 cudaError_t launch_aca(int ndim, const AcaArgs& a, const AcaLists& L, cudaStream_t st) {

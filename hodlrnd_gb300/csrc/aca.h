@@ -75,5 +75,8 @@ struct AcaLists {
 };
 // Asynchronous on st.
 cudaError_t launch_aca(int ndim, const AcaArgs& a, const AcaLists& lists, cudaStream_t st);
+// The team kind `kind` alone (its list in lists), asynchronous on st: the kinds
+// touch disjoint blocks and may run on different streams at once.
+cudaError_t launch_aca_kind(int ndim, const AcaArgs& a, const AcaLists& lists, int kind, cudaStream_t st);
 
 }  // namespace hodlr

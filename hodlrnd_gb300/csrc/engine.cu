@@ -746,6 +746,21 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   check_cuda(cudaEventCreate(&evs.e[0]), "cudaEventCreate");
   check_cuda(cudaEventCreate(&evs.e[1]), "cudaEventCreate");
   cudaEvent_t ev_a0 = evs.e[0], ev_a1 = evs.e[1];
+  // side streams of the ACA team kinds (one each), with their join events
+  struct Side {
+    cudaStream_t s[kAcaTeamKinds] = {};
+    cudaEvent_t e[kAcaTeamKinds] = {};
+    ~Side() {
+      for (int k = 0; k < kAcaTeamKinds; k++) {
+        if (e[k]) cudaEventDestroy(e[k]);
+        if (s[k]) cudaStreamDestroy(s[k]);
+      }
+    }
+  } side;
+  for (int k = 0; k < kAcaTeamKinds; k++) {
+    check_cuda(cudaStreamCreateWithFlags(&side.s[k], cudaStreamNonBlocking), "cudaStreamCreate");
+    check_cuda(cudaEventCreateWithFlags(&side.e[k], cudaEventDisableTiming), "cudaEventCreate");
+  }
   double t_kernel = 0.0, t_compact = 0.0;
   // device times shared by every operator of the launch
   struct Report {
@@ -867,8 +882,14 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       al.list[k] = d_lists_idx + lpos[k];
       al.n[k] = int(team_list[size_t(k)].size());
     }
+    // the team kinds at once, on side streams forked from st and joined back
     CK(cudaEventRecord(ev_a0, st));
-    CK(launch_aca(ndim, a, al, st));
+    for (int k = 0; k < kAcaTeamKinds; k++) {
+      CK(cudaStreamWaitEvent(side.s[k], ev_a0, 0));
+      CK(launch_aca_kind(ndim, a, al, k, side.s[k]));
+      CK(cudaEventRecord(side.e[k], side.s[k]));
+      CK(cudaStreamWaitEvent(st, side.e[k], 0));
+    }
     CK(cudaEventRecord(ev_a1, st));
     out.resize(batch.size());
     CK(cudaMemcpyAsync(out.data(), d_out, out.size() * sizeof(AcaOut), cudaMemcpyDeviceToHost, st));
