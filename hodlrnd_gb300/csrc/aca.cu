@@ -44,6 +44,7 @@ namespace hodlr {
 namespace {
 
 constexpr int kMaxTries = 10;
+constexpr int kNormChunk = 512;  // norm-estimate terms a CTA team holds in shared memory at once
 
 __device__ __forceinline__ int rng_next(uint64_t& s) {
   s += 0x9E3779B97F4A7C15ull;
@@ -336,6 +337,42 @@ struct AcaTeam {
     tm.sync();
   }
 
+  // mnorm += 2 |u_k . u_r| |v_k . v_r| for k < r, in order of k (LowRank_matrix.hpp:335-338).
+  // A CTA team gives each dot product pair to one warp (a warp reduction, no
+  // barrier), writes the terms to shared memory and adds them in order after
+  // one barrier per kNormChunk columns; warp and sub-warp teams reduce each
+  // pair across the team.
+  __device__ void norm_update(int r, double& mnorm) {
+    if constexpr (Team::kSize > 32) {
+      constexpr int W = Team::kSize / 32;
+      const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+      for (int k0 = 0; k0 < r; k0 += kNormChunk) {
+        const int kn = min(kNormChunk, r - k0);
+        for (int kk = w; kk < kn; kk += W) {
+          const int k = k0 + kk;
+          double du = 0.0, dv = 0.0;
+          for (int i = lane; i < m; i += 32) du += U[i + int64_t(k) * m] * U[i + int64_t(r) * m];
+          for (int j = lane; j < n; j += 32) dv += V[j + int64_t(k) * n] * V[j + int64_t(r) * n];
+          du = WarpTeam().sum(du);
+          dv = WarpTeam().sum(dv);
+          if (lane == 0) tm.terms[kk] = __dmul_rn(__dmul_rn(2.0, fabs(du)), fabs(dv));
+        }
+        __syncthreads();
+        for (int kk = 0; kk < kn; kk++) mnorm += tm.terms[kk];
+        __syncthreads();
+      }
+    } else {
+      for (int k = 0; k < r; k++) {
+        double du = 0.0, dv = 0.0;
+        for (int i = tm.tid(); i < m; i += Team::kSize) du += U[i + int64_t(k) * m] * U[i + int64_t(r) * m];
+        for (int j = tm.tid(); j < n; j += Team::kSize) dv += V[j + int64_t(k) * n] * V[j + int64_t(r) * n];
+        du = tm.sum(du);
+        dv = tm.sum(dv);
+        mnorm += __dmul_rn(__dmul_rn(2.0, fabs(du)), fabs(dv));
+      }
+    }
+  }
+
   __device__ void run(AcaOut* out) {
     const double tol = a.tol;
     if constexpr (S) stage_points();
@@ -425,14 +462,7 @@ struct AcaTeam {
       row_norm = sqrt(rsq);
       col_norm = sqrt(csq);
       mnorm += fabs(__dmul_rn(__dmul_rn(__dmul_rn(gamma, gamma), rsq), csq));
-      for (int k = 0; k < r; k++) {
-        double du = 0.0, dv = 0.0;
-        for (int i = tm.tid(); i < m; i += Team::kSize) du += U[i + int64_t(k) * m] * U[i + int64_t(r) * m];
-        for (int j = tm.tid(); j < n; j += Team::kSize) dv += V[j + int64_t(k) * n] * V[j + int64_t(r) * n];
-        du = tm.sum(du);
-        dv = tm.sum(dv);
-        mnorm += __dmul_rn(__dmul_rn(2.0, fabs(du)), fabs(dv));
-      }
+      norm_update(r, mnorm);
       r++;
     } while (__dmul_rn(__dmul_rn(double(int(int64_t(r) * (m + n))), row_norm), col_norm) >
                  __dmul_rn(__dmul_rn(fabs(mx), tol), mnorm) &&
@@ -478,8 +508,9 @@ __global__ void __launch_bounds__(128) aca_warp_kernel(AcaArgs a, const int32_t*
 template <int D>
 __global__ void __launch_bounds__(256) aca_cta_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
   __shared__ double red[256 / 32 + 1];
+  __shared__ double terms[kNormChunk];
   __shared__ int redi[256 / 32 + 1];
-  CtaTeam<256> tm{red, redi};
+  CtaTeam<256> tm{red, redi, terms};
   int pass = 0;
   for (;;) {
     const int q = next_item(a, kAcaTeamCta, int(blockIdx.x), pass, tm);

@@ -188,8 +188,9 @@ template <int NT>
 struct CtaTeam {
   static constexpr int kSize = NT;
   static constexpr int kWarps = NT / 32;
-  double* red;  // shared, kWarps + 1
-  int* redi;    // shared, kWarps + 1
+  double* red;    // shared, kWarps + 1
+  int* redi;      // shared, kWarps + 1
+  double* terms;  // shared, kNormChunk: the norm estimate's terms of one pass (ACA)
   __device__ __forceinline__ int tid() const { return threadIdx.x; }
   __device__ __forceinline__ void sync() const { __syncthreads(); }
   __device__ __forceinline__ double sum(double v) const {
