@@ -325,13 +325,14 @@ int hodlr_aca_block_noalloc(const double* d_points, int64_t ld, int32_t ndim, co
  * BF16 far-field factors (HODLR_PREC_BF16_FACTORS), X and Y device arrays of
  * n x nrhs FP32, column major, caller's point order.  Blocks of 64 columns
  * go through tcgen05 MMAs (BF16 operands, FP32 accumulation in tensor
- * memory): every right-hand side split into BF16 high and low parts (to about
- * 2^-17 relative), the BF16 factors as stored, the FP64 near field in three
- * BF16 terms -- the product differs from the stored operator's FP32 product
- * by about 1e-5 relative, far below the BF16 storage itself (about 1e-3).
- * The first call builds the tensor-core plan and buffers (about n + sum of
- * ranks times 256 bytes).  Synchronises `stream`.  Replaces the mat-mat use
- * of HODLRdD_matrix::operator* (include/HDD_matrix.hpp:42-47). */
+ * memory): every right-hand side split once into BF16 high and low parts (to
+ * about 2^-17 relative), each BF16 factor entry times its input scale in two
+ * BF16 terms, the FP64 near field in three -- the product differs from the
+ * stored operator's single-RHS product by about 1e-5 relative, far below the
+ * BF16 storage itself (about 1e-3).  The first call builds the tensor-core
+ * plan and buffers (about (n + sum of ranks) x 256 bytes).  Synchronises
+ * `stream`.  Replaces the mat-mat use of HODLRdD_matrix::operator*
+ * (include/HDD_matrix.hpp:42-47). */
 int hodlr_matvec_tc_device(hodlr_op* op, const float* d_x, float* d_y, int64_t nrhs, void* stream);
 
 /* ---- tensor cores ---------------------------------------------------------
