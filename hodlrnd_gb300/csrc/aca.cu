@@ -493,7 +493,7 @@ __device__ __forceinline__ int next_item(const AcaArgs& a, int kind, int first, 
 }
 
 template <int D>
-__global__ void __launch_bounds__(128, 6) aca_warp_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
+__global__ void __launch_bounds__(128) aca_warp_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
   WarpTeam tm;
   int pass = 0;
   for (;;) {
@@ -506,7 +506,7 @@ __global__ void __launch_bounds__(128, 6) aca_warp_kernel(AcaArgs a, const int32
 }
 
 template <int D>
-__global__ void __launch_bounds__(256, 4) aca_cta_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
+__global__ void __launch_bounds__(256) aca_cta_kernel(AcaArgs a, const int32_t* __restrict__ list, int count) {
   __shared__ double red[256 / 32 + 1];
   __shared__ double terms[kNormChunk];
   __shared__ int redi[256 / 32 + 1];
