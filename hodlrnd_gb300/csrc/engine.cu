@@ -217,6 +217,19 @@ struct hodlr_op {
   NearList near;
   std::vector<int32_t> rank, dense;
   std::vector<const void*> uptr, vptr;  // stored factors (or dense tile) of each far block
+  // FP32 / BF16 V factors after the relayout: the low-rank blocks of one source
+  // node share row-major chunks of at most 128 columns.  Per block: the row
+  // stride of its chunk (elements; 0: its own vpad(rank)), its z scales (BF16)
+  // and the position of its z in the input buffer [x | z].
+  struct VChunk {
+    const void* V;          // n x w, row major
+    int64_t x_off, zbase;   // source node's first tree position; z position of column 0
+    int32_t n, w;
+    const float* zscale;    // BF16: w scales
+  };
+  std::vector<VChunk> vchunks;
+  std::vector<int64_t> vstride, zpos;
+  std::vector<const float*> zsptr;
   // reduced-precision operators with the FP64 check: the FP64 factors of
   // every far block and the FP64 operator's plan (the refinement residuals)
   bool has_ref = false;
@@ -457,6 +470,8 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
   std::vector<PanelFix> pfix;
   int64_t nypart = 0;
   int64_t zoff = op->n;
+  // FP32 / BF16 after the relayout: z = V^T x per chunk of source-node columns
+  const bool chunks = a != Prec::kD && !op->vchunks.empty();
   size_t b = 0;
   while (b < op->far.size()) {
     const int l = op->far[b].level;
@@ -483,6 +498,11 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
         if (a == Prec::kB)
           s.cscale = reinterpret_cast<const float*>(static_cast<const char*>(uptr[q]) +
                                                     far_u_data_bytes(p.m, ns, 0, true, a));
+        segs.push_back(s);
+      } else if (op->rank[q] > 0 && chunks) {
+        s.A = uptr[q];
+        s.in_off = op->zpos[q];
+        s.K = op->rank[q];
         segs.push_back(s);
       } else if (op->rank[q] > 0) {
         ZBlock z;
@@ -535,7 +555,21 @@ void build_far_plan(hodlr_op* op, const std::vector<const void*>& uptr, const st
     }
     b = e;
   }
-  op->zlen = zoff - op->n;
+  if (chunks) {
+    for (const hodlr_op::VChunk& c : op->vchunks) {
+      ZBlock z;
+      z.V = c.V;
+      z.x_off = c.x_off;
+      z.z_off = c.zbase;
+      z.n = c.n;
+      z.r = c.w;  // the chunk's columns, padding included (its padding columns give z = 0)
+      z.zscale = c.zscale;
+      zb.push_back(z);
+      zoff = std::max(zoff, c.zbase + c.w);
+    }
+  }
+  // the input buffers hold the longest z of the operator's plans
+  op->zlen = std::max(op->zlen, zoff - op->n);
   plan.a_far = a;
   // FP64 far factors stay where the ACA batches put them, so whether a panel's
   // blocks follow one another depends on the batch split (and differs for an
@@ -1464,8 +1498,8 @@ void relayout_far(hodlr_op* op, cudaStream_t st) {
   const size_t nb = op->far.size();
   if (nb == 0 || op->p.precision == HODLR_PREC_FP64) return;
   const Prec fp = far_prec(op->p);
-  std::vector<uint64_t> uoff(nb, 0), voff(nb, 0);
-  uint64_t ubytes = 0, vbytes = 0;
+  std::vector<uint64_t> uoff(nb, 0);
+  uint64_t ubytes = 0;
   const Tree& t = op->tree;
   // op->far is grouped by (level, target): the plan's panel order
   for (size_t q = 0; q < nb; q++) {
@@ -1474,23 +1508,90 @@ void relayout_far(hodlr_op* op, cudaStream_t st) {
     if (!op->dense[q] && op->rank[q] <= 0) continue;
     uoff[q] = ubytes;
     ubytes += far_u_bytes(m, n, op->rank[q], op->dense[q], fp);
-    voff[q] = vbytes;
-    vbytes += far_v_bytes(n, op->rank[q], op->dense[q], fp);
   }
   char* fu = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(ubytes, 16), "far-field factors (panel order)"));
-  char* fv = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(vbytes, 16), "far-field V factors"));
   std::vector<CopyDesc> cd;
-  cd.reserve(nb * 2);
+  cd.reserve(nb);
   for (size_t q = 0; q < nb; q++) {
     const int l = op->far[q].level;
     const int64_t m = t.count[size_t(t.gid(l, op->far[q].t))], n = t.count[size_t(t.gid(l, op->far[q].s))];
     if (!op->dense[q] && op->rank[q] <= 0) continue;
     cd.push_back({op->uptr[q], fu + uoff[q], far_u_bytes(m, n, op->rank[q], op->dense[q], fp)});
     op->uptr[q] = fu + uoff[q];
-    if (!op->dense[q]) {
-      cd.push_back({op->vptr[q], fv + voff[q], far_v_bytes(n, op->rank[q], false, fp)});
-      op->vptr[q] = fv + voff[q];
+  }
+  // V: the low-rank blocks of each source node (level, s), in far-block order,
+  // packed side by side into row-major chunks of at most kVChunkCols columns
+  // (each block its vpad(rank) columns; a wider block gets a chunk of its
+  // own), so that z = V^T x reads one contiguous run per chunk.  BF16 chunks
+  // keep their w z scales after the values.
+  const int esz = prec_size(fp);
+  const int kVChunkCols = std::min(32 * (16 / esz), kZPart);
+  std::vector<size_t> lr;
+  for (size_t q = 0; q < nb; q++)
+    if (!op->dense[q] && op->rank[q] > 0) lr.push_back(q);
+  std::stable_sort(lr.begin(), lr.end(), [&](size_t a, size_t b) {
+    return op->far[a].level != op->far[b].level ? op->far[a].level < op->far[b].level
+                                                : op->far[a].s < op->far[b].s;
+  });
+  op->vstride.assign(nb, 0);
+  op->zpos.assign(nb, 0);
+  op->zsptr.assign(nb, nullptr);
+  op->vchunks.clear();
+  struct Place {
+    size_t chunk;
+    int32_t coff;
+  };
+  std::vector<Place> place(nb, Place{0, 0});
+  std::vector<uint64_t> cbyte;  // chunk offsets in the V array
+  uint64_t vbytes = 0;
+  int64_t zb = op->n;
+  for (size_t i = 0; i < lr.size();) {
+    const int l = op->far[lr[i]].level;
+    const int64_t s_ = op->far[lr[i]].s;
+    size_t e = i;
+    while (e < lr.size() && op->far[lr[e]].level == l && op->far[lr[e]].s == s_) e++;
+    const int64_t gs = t.gid(l, s_);
+    const int32_t n = int32_t(t.count[size_t(gs)]);
+    for (size_t k = i; k < e;) {
+      hodlr_op::VChunk c{nullptr, t.begin[size_t(gs)], zb, n, 0, nullptr};
+      while (k < e) {
+        const int32_t w = int32_t(vpad(op->rank[lr[k]], esz));
+        if (c.w > 0 && c.w + w > kVChunkCols) break;
+        place[lr[k]] = Place{op->vchunks.size(), c.w};
+        c.w += w;
+        k++;
+      }
+      cbyte.push_back(vbytes);
+      vbytes += round16(uint64_t(n) * uint64_t(c.w) * uint64_t(esz)) + (fp == Prec::kB ? round16(uint64_t(c.w) * 4) : 0);
+      zb += c.w;
+      op->vchunks.push_back(c);
     }
+    i = e;
+  }
+  char* fv = static_cast<char*>(op->mem.alloc(std::max<uint64_t>(vbytes, 16), "far-field V factors (by source)"));
+  CK(cudaMemsetAsync(fv, 0, std::max<uint64_t>(vbytes, 16), st));  // scale slots of padding columns
+  for (size_t c = 0; c < op->vchunks.size(); c++) {
+    hodlr_op::VChunk& C = op->vchunks[c];
+    C.V = fv + cbyte[c];
+    if (fp == Prec::kB)
+      C.zscale = reinterpret_cast<const float*>(fv + cbyte[c] + round16(uint64_t(C.n) * uint64_t(C.w) * uint64_t(esz)));
+  }
+  std::vector<RowCopy> rc;
+  rc.reserve(lr.size() * (fp == Prec::kB ? 2 : 1));
+  for (size_t q : lr) {
+    const hodlr_op::VChunk& C = op->vchunks[place[q].chunk];
+    const int32_t r = op->rank[q], w = int32_t(vpad(r, esz)), coff = place[q].coff;
+    char* dst = static_cast<char*>(const_cast<void*>(C.V)) + int64_t(coff) * esz;
+    rc.push_back({op->vptr[q], dst, int64_t(w) * esz, int64_t(C.w) * esz, int32_t(w * esz), C.n});
+    if (fp == Prec::kB) {
+      const char* s_scale = static_cast<const char*>(op->vptr[q]) + far_v_data_bytes(C.n, r, false, fp);
+      float* d_scale = const_cast<float*>(C.zscale) + coff;
+      rc.push_back({s_scale, d_scale, 0, 0, int32_t(round16(uint64_t(r) * 4)), 1});
+      op->zsptr[q] = d_scale;
+    }
+    op->vptr[q] = dst;
+    op->vstride[q] = C.w;
+    op->zpos[q] = C.zbase + coff;
   }
   // descriptors in slices of 2^20 (one CTA each)
   const size_t slice = size_t(1) << 20;
@@ -1501,6 +1602,14 @@ void relayout_far(hodlr_op* op, cudaStream_t st) {
     CK(launch_copy16(d_cd, int(k), st));
     CK(cudaStreamSynchronize(st));
   }
+  RowCopy* d_rc = op->mem.alloc_n<RowCopy>(std::min(rc.size(), slice) + 1, "relayout descriptors");
+  for (size_t b = 0; b < rc.size(); b += slice) {
+    const size_t k = std::min(slice, rc.size() - b);
+    CK(cudaMemcpyAsync(d_rc, rc.data() + b, k * sizeof(RowCopy), cudaMemcpyHostToDevice, st));
+    CK(launch_copy_rows(d_rc, int(k), st));
+    CK(cudaStreamSynchronize(st));
+  }
+  op->mem.release(d_rc);
   op->mem.release(d_cd);
   for (void* c : op->far_chunks) op->mem.release(c);
   op->far_chunks.clear();
@@ -1545,9 +1654,7 @@ void build_finish(hodlr_op* op, BuildState& bs, cudaStream_t st) {
   if (op->has_ref) {
     // the FP64 operator: the FP64 near field of plan64, the FP64 far factors
     Plan& r = op->plan_ref;
-    const int64_t zlen = op->zlen;
     build_far_plan(op, op->uptr64, op->vptr64, Prec::kD, r, st);
-    if (op->zlen != zlen) throw Failure{HODLR_ERR_DEVICE, "the FP64 far field has other ranks than the stored one"};
     r.a_near = op->plan64.a_near;
     r.panels_near = op->plan64.panels_near;
     r.segs_near = op->plan64.segs_near;
@@ -2440,15 +2547,19 @@ int hodlr_get_block(const hodlr_op* op, int64_t b, int32_t* m, int32_t* n, int32
       fetch(ub, size_t(mm), r, U);
       const char* vb = static_cast<const char*>(op->vptr[size_t(b)]);
       if (U && vb && r > 0 && fp == Prec::kB) {  // BF16: U V^T = U' diag(z scales) V'^T
-        const std::vector<float> zs = scales(vb + far_v_data_bytes(nn, int64_t(r), false, fp), r);
+        const char* zsb = op->zsptr.empty() || !op->zsptr[size_t(b)]
+                              ? vb + far_v_data_bytes(nn, int64_t(r), false, fp)
+                              : reinterpret_cast<const char*>(op->zsptr[size_t(b)]);
+        const std::vector<float> zs = scales(zsb, r);
         for (size_t k = 0; k < r; k++)
           for (size_t i = 0; i < size_t(mm); i++) U[k * size_t(mm) + i] *= double(zs[k]);
       }
-      if (V && vb && r > 0) {  // V is row major, nn x vpad(r)
+      if (V && vb && r > 0) {  // V is row major, nn x vpad(r), rows `stride` elements apart
         const size_t rp = size_t(vpad(int64_t(r), esz));
-        const std::vector<double> tmp = to_double(vb, size_t(nn) * rp);
+        const size_t stride = op->vstride.empty() || op->vstride[size_t(b)] == 0 ? rp : size_t(op->vstride[size_t(b)]);
+        const std::vector<double> tmp = to_double(vb, (size_t(nn) - 1) * stride + rp);
         for (size_t k = 0; k < r; k++)
-          for (size_t j = 0; j < size_t(nn); j++) V[k * size_t(nn) + j] = tmp[j * rp + k];
+          for (size_t j = 0; j < size_t(nn); j++) V[k * size_t(nn) + j] = tmp[j * stride + k];
       }
     }
     return HODLR_OK;
@@ -2753,9 +2864,20 @@ int hodlr_op_save(const hodlr_op* op, const double* points, const char* path) {
       const int32_t r = op->rank[size_t(q)], dn = op->dense[size_t(q)];
       if (!dn && r <= 0) continue;
       const uint64_t bu = block_u_bytes(m, n, r, dn, esz), bv = block_v_bytes(n, r, dn, esz);
-      buf.resize(bu + bv);
+      buf.assign(bu + bv, 0);
       CK(cudaMemcpy(buf.data(), op->uptr[size_t(q)], bu, cudaMemcpyDeviceToHost));
-      if (bv) CK(cudaMemcpy(buf.data() + bu, op->vptr[size_t(q)], bv, cudaMemcpyDeviceToHost));
+      const int64_t stride = op->vstride.empty() ? 0 : op->vstride[size_t(q)];
+      if (bv && stride == 0) {
+        CK(cudaMemcpy(buf.data() + bu, op->vptr[size_t(q)], bv, cudaMemcpyDeviceToHost));
+      } else if (bv) {  // a block of a source chunk: its rows, then (BF16) its z scales
+        const int es = prec_size(esz);
+        const size_t row = size_t(vpad(r, es)) * size_t(es);
+        CK(cudaMemcpy2D(buf.data() + bu, row, op->vptr[size_t(q)], size_t(stride) * size_t(es), row, size_t(n),
+                        cudaMemcpyDeviceToHost));
+        if (esz == Prec::kB)
+          CK(cudaMemcpy(buf.data() + bu + far_v_data_bytes(n, r, false, esz), op->zsptr[size_t(q)],
+                        size_t(r) * 4, cudaMemcpyDeviceToHost));
+      }
       put(buf.data(), bu + bv);
     }
     if (op->has_ref)  // the FP64 factors of the FP64 check, in the same order

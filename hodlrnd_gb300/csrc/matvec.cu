@@ -1654,6 +1654,25 @@ __global__ void __launch_bounds__(128) copy16_kernel(const CopyDesc* __restrict_
   for (uint64_t i = threadIdx.x; i < D.bytes / 16; i += blockDim.x) t[i] = s[i];
 }
 
+// One CTA per descriptor: 16-byte units of every row.
+__global__ void __launch_bounds__(128) copy_rows_kernel(const RowCopy* __restrict__ d) {
+  const RowCopy D = d[blockIdx.x];
+  const int units = D.row_bytes / 16;
+  const int64_t total = int64_t(units) * D.rows;
+  for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+    const int64_t row = e / units, u = e - row * units;
+    *reinterpret_cast<int4*>(static_cast<char*>(D.dst) + row * D.dst_pitch + u * 16) =
+        *reinterpret_cast<const int4*>(static_cast<const char*>(D.src) + row * D.src_pitch + u * 16);
+  }
+}
+
+cudaError_t launch_copy_rows(const RowCopy* d, int n, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  count_launches(1);
+  copy_rows_kernel<<<unsigned(n), 128, 0, st>>>(d);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_copy16(const CopyDesc* d, int n, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   count_launches(1);

@@ -187,6 +187,15 @@ struct CopyDesc {
   uint64_t bytes;
 };
 cudaError_t launch_copy16(const CopyDesc* d, int n, cudaStream_t st);
+// rows x row_bytes from src (rows src_pitch bytes apart) to dst (dst_pitch
+// apart); row_bytes, the pitches and both addresses multiples of 16 bytes.
+struct RowCopy {
+  const void* src;
+  void* dst;
+  int64_t src_pitch, dst_pitch;
+  int32_t row_bytes, rows;
+};
+cudaError_t launch_copy_rows(const RowCopy* d, int n, cudaStream_t st);
 
 // One instance of a batch of operators: its n rows sit at x_base in the
 // caller's concatenated vectors, at in_base in the batch's input buffer and
