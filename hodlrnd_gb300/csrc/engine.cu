@@ -229,6 +229,7 @@ struct hodlr_op {
   };
   std::vector<VChunk> vchunks;
   std::vector<int64_t> vstride, zpos;
+  std::vector<int32_t> vchunk_of;  // the chunk of each low-rank block (-1: none)
   std::vector<const float*> zsptr;
   // reduced-precision operators with the FP64 check: the FP64 factors of
   // every far block and the FP64 operator's plan (the refinement residuals)
@@ -1535,6 +1536,7 @@ void relayout_far(hodlr_op* op, cudaStream_t st) {
   });
   op->vstride.assign(nb, 0);
   op->zpos.assign(nb, 0);
+  op->vchunk_of.assign(nb, -1);
   op->zsptr.assign(nb, nullptr);
   op->vchunks.clear();
   struct Place {
@@ -1590,6 +1592,7 @@ void relayout_far(hodlr_op* op, cudaStream_t st) {
       op->zsptr[q] = d_scale;
     }
     op->vptr[q] = dst;
+    op->vchunk_of[q] = int32_t(place[q].chunk);
     op->vstride[q] = C.w;
     op->zpos[q] = C.zbase + coff;
   }
@@ -2033,26 +2036,41 @@ void build_tc_plan(hodlr_op* op, cudaStream_t st) {
   int pn = 0, pf = 0;
   tc_panel_items(h.panels_near, h.segs_near, ni, T.near, fxn, pn);
   tc_panel_items(h.panels_far, h.segs_far, fi, T.far, fxf, pf);
-  // z groups: the low-rank blocks by source node (consecutive in the sorted
-  // order), at most 256 rows per group.  A node is its first point and its
-  // size: a node and its first child start at the same point.
-  std::vector<int32_t> order(h.zb.size());
-  for (size_t q = 0; q < order.size(); q++) order[q] = int32_t(q);
+  // z groups: the rows of z by source node, at most kTcRows rows per group.
+  // Rows are (z block, k0, nk) runs: with source chunks each low-rank block's
+  // own columns of its chunk (its padding columns skipped), else every column
+  // of each z block.  A node is its first point and its size: a node and its
+  // first child start at the same point.
+  struct ZRun {
+    int32_t zb, k0, nk;
+  };
+  std::vector<ZRun> runs;
+  if (!op->vchunk_of.empty()) {
+    for (size_t q = 0; q < op->far.size(); q++) {
+      const int32_t c = op->vchunk_of[q];
+      if (c < 0) continue;
+      runs.push_back({c, int32_t(op->zpos[q] - op->vchunks[size_t(c)].zbase), op->rank[q]});
+    }
+  } else {
+    for (size_t q = 0; q < h.zb.size(); q++) runs.push_back({int32_t(q), 0, h.zb[q].r});
+  }
   auto same_source = [&](const ZBlock& a, const ZBlock& b) { return a.x_off == b.x_off && a.n == b.n; };
-  std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-    const ZBlock &a = h.zb[size_t(x)], &b = h.zb[size_t(y)];
-    return a.x_off != b.x_off ? a.x_off < b.x_off : a.n < b.n;
+  std::stable_sort(runs.begin(), runs.end(), [&](const ZRun& x, const ZRun& y) {
+    const ZBlock &a = h.zb[size_t(x.zb)], &b = h.zb[size_t(y.zb)];
+    if (a.x_off != b.x_off) return a.x_off < b.x_off;
+    if (a.n != b.n) return a.n < b.n;
+    return x.zb != y.zb ? x.zb < y.zb : x.k0 < y.k0;
   });
   std::vector<TcZGroup> zg;
   std::vector<TcZEntry> ze;
-  for (size_t q = 0; q < order.size();) {
-    const ZBlock& z0 = h.zb[size_t(order[q])];
+  for (size_t q = 0; q < runs.size();) {
+    const ZBlock& z0 = h.zb[size_t(runs[q].zb)];
     TcZGroup g{z0.x_off, z0.n, int32_t(ze.size()), int32_t(ze.size()), 0, -1, 0};
-    while (q < order.size() && same_source(h.zb[size_t(order[q])], z0)) {
-      const ZBlock& z = h.zb[size_t(order[q])];
-      for (int32_t k0 = 0; k0 < z.r;) {
-        const int32_t take = std::min(z.r - k0, kTcRows - g.rows);
-        ze.push_back({order[q], k0, take});
+    while (q < runs.size() && same_source(h.zb[size_t(runs[q].zb)], z0)) {
+      const ZRun& R = runs[q];
+      for (int32_t k0 = 0; k0 < R.nk;) {
+        const int32_t take = std::min(R.nk - k0, kTcRows - g.rows);
+        ze.push_back({R.zb, R.k0 + k0, take});
         g.rows += take;
         k0 += take;
         if (g.rows == kTcRows) {  // close the group, continue with a new one on the same source
