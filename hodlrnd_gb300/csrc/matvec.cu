@@ -710,20 +710,10 @@ static_assert(kLStageBytes % 16 == 0 && kLStageBytes >= 512 && kLStageBytes <= 6
               "leaf stage: a multiple of 16 bytes in 512 .. 65536 (column offsets are 16-bit)");
 static_assert(kLCols % 32 == 0 && kLCols <= 1024, "leaf stage columns: a multiple of 32");
 static_assert(32 + kLStages * 8 <= kLHead, "leaf ring header too small");
-// One staged column: its input value, its first element in the stage's
-// factor bytes and (BF16 dense tiles) its input scale -- one 16-byte shared
-// load per column in the product loop.
-template <typename TX>
-struct alignas(16) LRec {
-  TX x;
-  int32_t off;
-  float scale;
-};
-static_assert(sizeof(LRec<double>) == 16 && sizeof(LRec<float>) == 16, "leaf column records are 16 bytes");
-// stage: factor bytes | column records (kLCols x 16 bytes)
+// stage: factor bytes | inputs (kLCols x TX) | column offsets (kLCols x u16) | BF16 scales (kLCols x f32)
 template <typename TA, typename TX>
 __host__ __device__ constexpr int l_stage_smem() {
-  return kLStageBytes + kLCols * int(sizeof(LRec<TX>));
+  return kLStageBytes + kLCols * int(sizeof(TX)) + kLCols * 2 + (sizeof(TA) == 2 ? kLCols * 4 : 0);
 }
 template <typename TA, typename TX>
 __host__ __device__ constexpr int l_warp_smem() { return kLHead + kLStages * l_stage_smem<TA, TX>(); }
@@ -753,7 +743,7 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
   constexpr int esz = int(sizeof(TA));
   constexpr bool kScaled = esz == 2;
   constexpr int kStage = l_stage_smem<TA, TX>(), kWarpSmem = l_warp_smem<TA, TX>();
-  constexpr int kROff = kLStageBytes;  // column records
+  constexpr int kXOff = kLStageBytes, kOOff = kXOff + kLCols * int(sizeof(TX)), kSOff = kOOff + kLCols * 2;
   extern __shared__ __align__(16) unsigned char lsm[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int w = blockIdx.x * kLWarps + wid;
@@ -788,7 +778,9 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
   auto issue = [&](int st) -> bool {
     if (pq >= qe) return false;
     unsigned char* su = ring + st * kStage;
-    LRec<TX>* rec = reinterpret_cast<LRec<TX>*>(su + kROff);
+    TX* xs = reinterpret_cast<TX*>(su + kXOff);
+    uint16_t* co = reinterpret_cast<uint16_t*>(su + kOOff);
+    float* sc = reinterpret_cast<float*>(su + kSOff);
     int32_t sbase = 0, cols = 0, end = 0;
     bool first = true, more = true;
     while (more) {
@@ -845,10 +837,9 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
         unsigned long long csk = 0;
         if constexpr (kScaled) csk = __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(cs), k);
         if (c < wcols) {
-          LRec<TX>& R = rec[cols + c];
-          R.off = (sok + jk * colb - sbase) / esz;
-          cp_async_gather(&R.x, inc + ink + jk, int(sizeof(TX)));
-          if constexpr (kScaled) R.scale = csk ? __ldg(reinterpret_cast<const float*>(csk) + jk) : 1.f;
+          co[cols + c] = uint16_t((sok + jk * colb - sbase) / esz);
+          cp_async_gather(xs + cols + c, inc + ink + jk, int(sizeof(TX)));
+          if constexpr (kScaled) sc[cols + c] = csk ? __ldg(reinterpret_cast<const float*>(csk) + jk) : 1.f;
         }
       }
       // the last lane with columns ends the stage's bytes and moves the cursor
@@ -903,25 +894,24 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
     const int C = meta[st].x;
     const unsigned char* sb = ring + st * kStage;
     const TA* su = reinterpret_cast<const TA*>(sb);
-    const LRec<TX>* rec = reinterpret_cast<const LRec<TX>*>(sb + kROff);
+    const TX* xs = reinterpret_cast<const TX*>(sb + kXOff);
+    const uint16_t* co = reinterpret_cast<const uint16_t*>(sb + kOOff);
+    const float* sc = reinterpret_cast<const float*>(sb + kSOff);
     if (i < m) {
-      const TA* sui = su + i;  // this lane's row of every column
       int c = sl;
       for (; c + slices < C; c += 2 * slices) {
-        const LRec<TX> r0 = rec[c], r1 = rec[c + slices];
-        typename AC::X x0 = AC::in(r0.x), x1 = AC::in(r1.x);
+        typename AC::X x0 = AC::in(xs[c]), x1 = AC::in(xs[c + slices]);
         if constexpr (kScaled) {
-          x0 = AC::xscale(x0, r0.scale);
-          x1 = AC::xscale(x1, r1.scale);
+          x0 = AC::xscale(x0, sc[c]);
+          x1 = AC::xscale(x1, sc[c + slices]);
         }
-        AC::fma(a0acc, sui[r0.off], x0);
-        AC::fma(a1acc, sui[r1.off], x1);
+        AC::fma(a0acc, su[co[c] + i], x0);
+        AC::fma(a1acc, su[co[c + slices] + i], x1);
       }
       if (c < C) {
-        const LRec<TX> r0 = rec[c];
-        typename AC::X x0 = AC::in(r0.x);
-        if constexpr (kScaled) x0 = AC::xscale(x0, r0.scale);
-        AC::fma(a0acc, sui[r0.off], x0);
+        typename AC::X x0 = AC::in(xs[c]);
+        if constexpr (kScaled) x0 = AC::xscale(x0, sc[c]);
+        AC::fma(a0acc, su[co[c] + i], x0);
       }
     }
     __syncwarp();  // stage k's slot is refilled for stage k + kLStages
