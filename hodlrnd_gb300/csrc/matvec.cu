@@ -731,6 +731,41 @@ __device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// The products of one staged stage for one lane (row i of slice sl): columns
+// sl, sl + S, sl + 2S, ... of the stage, alternately into a0 and a1.  S (the
+// slice count) is a compile-time constant so that the column strides are
+// immediate offsets.
+template <int S, typename TA, typename TX, typename TACC, bool kScaled>
+__device__ __forceinline__ void leaf_products(const TA* __restrict__ su, const TX* __restrict__ xs,
+                                              const uint16_t* __restrict__ co, const float* __restrict__ sc, int C,
+                                              int sl, int i, typename Acc<TACC>::A& a0, typename Acc<TACC>::A& a1) {
+  using AC = Acc<TACC>;
+  const TA* sui = su + i;
+  const TX* px = xs + sl;
+  const uint16_t* pc = co + sl;
+  const float* ps = sc + sl;
+  int c = sl;
+  for (; c + 3 * S < C; c += 4 * S, px += 4 * S, pc += 4 * S, ps += 4 * S) {
+    typename AC::X x0 = AC::in(px[0]), x1 = AC::in(px[S]), x2 = AC::in(px[2 * S]), x3 = AC::in(px[3 * S]);
+    if constexpr (kScaled) {
+      x0 = AC::xscale(x0, ps[0]);
+      x1 = AC::xscale(x1, ps[S]);
+      x2 = AC::xscale(x2, ps[2 * S]);
+      x3 = AC::xscale(x3, ps[3 * S]);
+    }
+    const TA v0 = sui[pc[0]], v1 = sui[pc[S]], v2 = sui[pc[2 * S]], v3 = sui[pc[3 * S]];
+    AC::fma(a0, v0, x0);
+    AC::fma(a1, v1, x1);
+    AC::fma(a0, v2, x2);
+    AC::fma(a1, v3, x3);
+  }
+  for (int k = 0; c < C; c += S, px += S, pc += S, ps += S, k++) {
+    typename AC::X x0 = AC::in(px[0]);
+    if constexpr (kScaled) x0 = AC::xscale(x0, ps[0]);
+    AC::fma((k & 1) ? a1 : a0, sui[pc[0]], x0);
+  }
+}
+
 template <typename TA, typename TACC>
 __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
     panel_leaf_kernel(const Panel* __restrict__ panels, const Seg* __restrict__ segs, const Item* __restrict__ items,
@@ -898,20 +933,13 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
     const uint16_t* co = reinterpret_cast<const uint16_t*>(sb + kOOff);
     const float* sc = reinterpret_cast<const float*>(sb + kSOff);
     if (i < m) {
-      int c = sl;
-      for (; c + slices < C; c += 2 * slices) {
-        typename AC::X x0 = AC::in(xs[c]), x1 = AC::in(xs[c + slices]);
-        if constexpr (kScaled) {
-          x0 = AC::xscale(x0, sc[c]);
-          x1 = AC::xscale(x1, sc[c + slices]);
-        }
-        AC::fma(a0acc, su[co[c] + i], x0);
-        AC::fma(a1acc, su[co[c + slices] + i], x1);
-      }
-      if (c < C) {
-        typename AC::X x0 = AC::in(xs[c]);
-        if constexpr (kScaled) x0 = AC::xscale(x0, sc[c]);
-        AC::fma(a0acc, su[co[c] + i], x0);
+      switch (slices) {
+        case 32: leaf_products<32, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
+        case 16: leaf_products<16, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
+        case 8: leaf_products<8, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
+        case 4: leaf_products<4, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
+        case 2: leaf_products<2, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
+        default: leaf_products<1, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
       }
     }
     __syncwarp();  // stage k's slot is refilled for stage k + kLStages
