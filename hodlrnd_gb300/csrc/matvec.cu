@@ -293,12 +293,14 @@ __device__ __forceinline__ float2 to_input<FH>(float a) {
 // Ring shapes (stages x bytes) of the staged kernels; HODLR_TUNE_* override
 // them at compile time for tuning runs.  Two stages per warp measured best on
 // GB300 (the shared memory per warp, not the stage count, limits the warps
-// per SM, and more warps hide more latency than deeper rings).
+// per SM, and more warps hide more latency than deeper rings); V^T x stages
+// of 4 KB (with V grouped by source node, whole-row runs are long) beat 2 KB
+// by 2% per solve at N = 262144.
 #ifndef HODLR_TUNE_Z_STAGES
 #define HODLR_TUNE_Z_STAGES 2
 #endif
 #ifndef HODLR_TUNE_Z_BYTES
-#define HODLR_TUNE_Z_BYTES 2048
+#define HODLR_TUNE_Z_BYTES 4096
 #endif
 #ifndef HODLR_TUNE_P_STAGES
 #define HODLR_TUNE_P_STAGES 2
