@@ -92,7 +92,8 @@ typedef struct hodlr_params {
   int32_t ortho;     /* GMRES orthogonalisation, HODLR_ORTHO_* */
   int32_t relax;     /* FP32_FACTORS, BF16_FACTORS: HODLR_RELAX_AUTO, _OFF or _ALWAYS */
   double relax_below; /* FP32_FACTORS, BF16_FACTORS: relative residual estimate below which products
-                         are relaxed (<= 0: the default, tol * 1e5) */
+                         are relaxed (<= 0: the default -- from the first iteration when the FP64
+                         check is on, tol * 1e5 when it is off) */
   int32_t fp64_check; /* FP32_FACTORS, BF16_FACTORS, MIXED: HODLR_FP64_CHECK_AUTO (on) or _OFF */
   int32_t aca_workspace_mib; /* FP64 workspace of one ACA launch, MiB (0: a quarter of the free device
                                 memory, 4 to 64 GiB); blocks beyond it go to further launches.  Freed
