@@ -339,6 +339,17 @@ def run_gb300(args):
         torch.cuda.synchronize()
         x64 = x64[0].cpu().numpy()
         acc["rel_diff_vs_fp64_solution"] = float(np.linalg.norm(x0 - x64) / np.linalg.norm(x64))
+        # a known solution (the reference's self-check, include/main.cpp:42-57): b = A64 x_true,
+        # solved by the headline engine and by the FP64 engine; both errors are bounded by the
+        # conditioning times the 1e-8 residual, so the headline's is compared with the FP64 engine's
+        x_true = np.random.default_rng(SEED + 99).standard_normal(n)
+        b_true = M64 * x_true
+        x_h, x_f = M.solve(b_true), M64.solve(b_true)
+        acc["known_solution"] = {
+            "rel_error_headline": float(np.linalg.norm(x_h - x_true) / np.linalg.norm(x_true)),
+            "rel_error_fp64_engine": float(np.linalg.norm(x_f - x_true) / np.linalg.norm(x_true)),
+            "rel_residual_headline_fp64_operator": float(np.linalg.norm(b_true - M64 * x_h) / np.linalg.norm(b_true)),
+            "rel_residual_fp64_engine": float(np.linalg.norm(b_true - M64 * x_f) / np.linalg.norm(b_true))}
 
     # ---- end to end through the host-pointer C ABI (pinned host buffers)
     hb = torch.empty((K, n), dtype=torch.float64, pin_memory=True)
