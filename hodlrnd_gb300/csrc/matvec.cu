@@ -671,25 +671,30 @@ __global__ void __launch_bounds__(kSWarps * 32, HODLR_TUNE_S_MINB)
 // Phase 2, panels of at most 32 rows, when the segments of every item lie
 // in memory in segment order (the far field after its relayout in panel
 // order, the near field as assembled).  All segments of a panel have its m
-// rows, so an item's factors form one run of m-row columns (with up to 15
-// bytes of padding after each segment).  The run is streamed through a
-// per-warp ring of kLStages stages; a stage is the bytes of a run of whole
-// columns -- at most kLStageBytes, at most kLCols columns -- fetched by ONE
-// bulk copy (from the 16-byte boundary at or below its first column), and
-// the input values of those columns, gathered into the stage by the lanes
-// with 4- or 8-byte asynchronous copies (cp.async) that complete on the
-// stage's mbarrier.  Both are issued kLStages - 1 stages ahead of the
-// products, so neither the factor bytes nor the scattered inputs (read from
-// L2: x and z are small) are waited for in the loop.
+// rows, so an item's factors form one run of m-row columns (after each
+// segment up to 15 bytes of padding, and for a BF16 dense tile its column
+// scales).  The run is streamed through a per-warp ring of kLStages stages;
+// a stage is the bytes of a run of whole columns -- at most kLStageBytes, at
+// most kLCols columns -- fetched by ONE bulk copy (from the 16-byte boundary
+// at or below its first column), and the input values of those columns,
+// gathered into the stage by the lanes with 4- or 8-byte asynchronous copies
+// (cp.async) that complete on the stage's mbarrier.  Relaxed products read
+// only the high part of a split input, so only that part is staged.  Both
+// are issued kLStages - 1 stages ahead of the products, so neither the
+// factor bytes nor the scattered inputs (read from L2: x and z are small)
+// are waited for in the loop.
 //
 // The warp plans each stage together: lane k reads the record of the k-th
-// next segment (one coalesced load per 32 segments), a warp scan places each
-// segment's columns in the stage, and every lane then fills the stage's
-// column table (the element offset of each column in the stage buffer; for
-// BF16 dense tiles its input scale) and starts the gathers of columns lane,
-// lane + 32, ...  The products then read only shared memory: lanes form
-// slices of mpad lanes (one lane per row), slice sl takes the stage's
-// columns sl, sl + slices, ..., column parity picks the accumulator.
+// next segment (one coalesced load per 32 segments; the first 32 of each
+// plan are loaded one stage ahead), a warp scan places each segment's
+// columns in the stage, and every lane then fills the stage's column table
+// (the element offset of each column in the stage buffer) and starts the
+// gathers of columns lane, lane + 32, ... (for BF16 dense tiles also the
+// gathers of their column scales).  After the wait the lanes multiply the
+// staged inputs of BF16 dense tiles by their scales, once per column.  The
+// products then read only shared memory: lanes form slices of mpad lanes
+// (one lane per row), slice sl takes the stage's columns sl, sl + slices,
+// ..., column parity picks the accumulator.
 #ifndef HODLR_TUNE_L_STAGES
 #define HODLR_TUNE_L_STAGES 2
 #endif
@@ -712,6 +717,20 @@ static_assert(kLStageBytes % 16 == 0 && kLStageBytes >= 512 && kLStageBytes <= 6
               "leaf stage: a multiple of 16 bytes in 512 .. 65536 (column offsets are 16-bit)");
 static_assert(kLCols % 32 == 0 && kLCols <= 1024, "leaf stage columns: a multiple of 32");
 static_assert(32 + kLStages * 8 <= kLHead, "leaf ring header too small");
+// The staged input of one column: the input element, or for relaxed products
+// (which read only the high part of a split input) that high part alone.
+template <typename TACC>
+struct LeafX {
+  using T = typename IO<TACC>::TI;
+};
+template <>
+struct LeafX<FH> {
+  using T = float;
+};
+// An input after scaling, in its staged form.
+__device__ __forceinline__ void put_staged(float2& d, DF x) { d = make_float2(x.hi, x.lo); }
+__device__ __forceinline__ void put_staged(float& d, float x) { d = x; }
+__device__ __forceinline__ void put_staged(double& d, double x) { d = x; }
 // stage: factor bytes | inputs (kLCols x TX) | column offsets (kLCols x u16) | BF16 scales (kLCols x f32)
 template <typename TA, typename TX>
 __host__ __device__ constexpr int l_stage_smem() {
@@ -737,35 +756,24 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // sl, sl + S, sl + 2S, ... of the stage, alternately into a0 and a1.  S (the
 // slice count) is a compile-time constant so that the column strides are
 // immediate offsets.
-template <int S, typename TA, typename TX, typename TACC, bool kScaled>
+template <int S, typename TA, typename TX, typename TACC>
 __device__ __forceinline__ void leaf_products(const TA* __restrict__ su, const TX* __restrict__ xs,
-                                              const uint16_t* __restrict__ co, const float* __restrict__ sc, int C,
-                                              int sl, int i, typename Acc<TACC>::A& a0, typename Acc<TACC>::A& a1) {
+                                              const uint16_t* __restrict__ co, int C, int sl, int i,
+                                              typename Acc<TACC>::A& a0, typename Acc<TACC>::A& a1) {
   using AC = Acc<TACC>;
   const TA* sui = su + i;
   const TX* px = xs + sl;
   const uint16_t* pc = co + sl;
-  const float* ps = sc + sl;
   int c = sl;
-  for (; c + 3 * S < C; c += 4 * S, px += 4 * S, pc += 4 * S, ps += 4 * S) {
-    typename AC::X x0 = AC::in(px[0]), x1 = AC::in(px[S]), x2 = AC::in(px[2 * S]), x3 = AC::in(px[3 * S]);
-    if constexpr (kScaled) {
-      x0 = AC::xscale(x0, ps[0]);
-      x1 = AC::xscale(x1, ps[S]);
-      x2 = AC::xscale(x2, ps[2 * S]);
-      x3 = AC::xscale(x3, ps[3 * S]);
-    }
+  for (; c + 3 * S < C; c += 4 * S, px += 4 * S, pc += 4 * S) {
+    const typename AC::X x0 = AC::in(px[0]), x1 = AC::in(px[S]), x2 = AC::in(px[2 * S]), x3 = AC::in(px[3 * S]);
     const TA v0 = sui[pc[0]], v1 = sui[pc[S]], v2 = sui[pc[2 * S]], v3 = sui[pc[3 * S]];
     AC::fma(a0, v0, x0);
     AC::fma(a1, v1, x1);
     AC::fma(a0, v2, x2);
     AC::fma(a1, v3, x3);
   }
-  for (int k = 0; c < C; c += S, px += S, pc += S, ps += S, k++) {
-    typename AC::X x0 = AC::in(px[0]);
-    if constexpr (kScaled) x0 = AC::xscale(x0, ps[0]);
-    AC::fma((k & 1) ? a1 : a0, sui[pc[0]], x0);
-  }
+  for (int k = 0; c < C; c += S, px += S, pc += S, k++) AC::fma((k & 1) ? a1 : a0, sui[pc[0]], AC::in(px[0]));
 }
 
 template <typename TA, typename TACC>
@@ -774,7 +782,8 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
                       int nitems, const typename IO<TACC>::TI* __restrict__ in, int64_t ld_in,
                       typename IO<TACC>::TY* __restrict__ y, int64_t ld_y, int nslots,
                       typename IO<TACC>::TY* __restrict__ ypart) {
-  using TX = typename IO<TACC>::TI;
+  using TI = typename IO<TACC>::TI;
+  using TX = typename LeafX<TACC>::T;
   using TY = typename IO<TACC>::TY;
   using AC = Acc<TACC>;
   constexpr int esz = int(sizeof(TA));
@@ -789,7 +798,7 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
   const Panel P = panels[it.panel];
   const int m = P.m;
   const int colb = m * esz;  // bytes per column
-  const TX* inc = in + blockIdx.y * ld_in;
+  const TI* inc = in + blockIdx.y * ld_in;
   TY* yo = y + int64_t(blockIdx.y) * nslots * ld_y + P.yoff;
   int mpad = 1;
   while (mpad < m) mpad <<= 1;
@@ -810,6 +819,25 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
 
   // next column to stage (the same in every lane): segment pq, column pj
   int32_t pq = it.seg_b, pj = 0;
+  // lane k's record of segment rq + k, loaded a stage ahead of its use (the
+  // first window of the next plan), so that its latency overlaps the products
+  int32_t rq = -1, rK = 0, rso = 0;
+  int64_t rino = 0;
+  const float* rcs = nullptr;
+  auto prefetch = [&]() {
+    rq = pq;
+    rK = 0;
+    rso = 0;
+    rino = 0;
+    rcs = nullptr;
+    if (pq + lane < qe) {
+      const Seg S = segs[pq + lane];
+      rK = S.K;
+      rso = int32_t(static_cast<const char*>(S.A) - a0);
+      rino = S.in_off;
+      rcs = S.cscale;
+    }
+  };
   // Plans the stage from (pq, pj) into slot st and issues its copies; false
   // when every column is staged.  Warp-uniform.
   auto issue = [&](int st) -> bool {
@@ -826,7 +854,12 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
       int32_t K = 0, so = 0;
       int64_t ino = 0;
       const float* cs = nullptr;
-      if (q < qe) {
+      if (pq == rq) {  // warp-uniform
+        K = rK;
+        so = rso;
+        ino = rino;
+        cs = rcs;
+      } else if (q < qe) {
         const Seg S = segs[q];
         K = S.K;
         so = int32_t(static_cast<const char*>(S.A) - a0);
@@ -875,8 +908,14 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
         if constexpr (kScaled) csk = __shfl_sync(0xffffffffu, reinterpret_cast<unsigned long long>(cs), k);
         if (c < wcols) {
           co[cols + c] = uint16_t((sok + jk * colb - sbase) / esz);
-          cp_async_gather(xs + cols + c, inc + ink + jk, int(sizeof(TX)));
-          if constexpr (kScaled) sc[cols + c] = csk ? __ldg(reinterpret_cast<const float*>(csk) + jk) : 1.f;
+          // relaxed products stage only the high part (the first member) of a split input
+          cp_async_gather(xs + cols + c, reinterpret_cast<const TX*>(inc + ink + jk), int(sizeof(TX)));
+          if constexpr (kScaled) {
+            if (csk)
+              cp_async_gather(sc + cols + c, reinterpret_cast<const float*>(csk) + jk, 4);
+            else
+              sc[cols + c] = 1.f;
+          }
         }
       }
       // the last lane with columns ends the stage's bytes and moves the cursor
@@ -914,9 +953,11 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
   };
 
   int nissued = 0;
+  prefetch();
   for (int s = 0; s < kLStages; s++) {
     if (!issue(s)) break;
     nissued++;
+    prefetch();
   }
   typename AC::A a0acc = AC::zero(), a1acc = AC::zero();
   for (int k = 0; k < nissued; k++) {
@@ -934,18 +975,28 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
     const TX* xs = reinterpret_cast<const TX*>(sb + kXOff);
     const uint16_t* co = reinterpret_cast<const uint16_t*>(sb + kOOff);
     const float* sc = reinterpret_cast<const float*>(sb + kSOff);
+    if constexpr (kScaled) {
+      // BF16: the staged inputs times their column scales, once per column
+      // (lane c % 32 gathered column c and scales it), before the products
+      TX* xw = const_cast<TX*>(xs);
+      for (int c = lane; c < C; c += 32) put_staged(xw[c], AC::xscale(AC::in(xw[c]), sc[c]));
+      __syncwarp();
+    }
     if (i < m) {
       switch (slices) {
-        case 32: leaf_products<32, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
-        case 16: leaf_products<16, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
-        case 8: leaf_products<8, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
-        case 4: leaf_products<4, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
-        case 2: leaf_products<2, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
-        default: leaf_products<1, TA, TX, TACC, kScaled>(su, xs, co, sc, C, sl, i, a0acc, a1acc); break;
+        case 32: leaf_products<32, TA, TX, TACC>(su, xs, co, C, sl, i, a0acc, a1acc); break;
+        case 16: leaf_products<16, TA, TX, TACC>(su, xs, co, C, sl, i, a0acc, a1acc); break;
+        case 8: leaf_products<8, TA, TX, TACC>(su, xs, co, C, sl, i, a0acc, a1acc); break;
+        case 4: leaf_products<4, TA, TX, TACC>(su, xs, co, C, sl, i, a0acc, a1acc); break;
+        case 2: leaf_products<2, TA, TX, TACC>(su, xs, co, C, sl, i, a0acc, a1acc); break;
+        default: leaf_products<1, TA, TX, TACC>(su, xs, co, C, sl, i, a0acc, a1acc); break;
       }
     }
     __syncwarp();  // stage k's slot is refilled for stage k + kLStages
-    if (issue(st)) nissued++;
+    if (issue(st)) {
+      nissued++;
+      prefetch();
+    }
   }
   typename AC::A acc = AC::add(a0acc, a1acc);
   for (int o = mpad; o < 32; o <<= 1) acc = AC::add(acc, AC::shfl_xor(acc, o));
@@ -958,14 +1009,20 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
 }
 
 // Phase 2, panels of more than 32 rows: item chunk = row tile t of the
-// panel (T = 512 / sizeof(TA) rows, lane l owns rows t*T + l*RPL ..).  Every
+// panel (T = 512 / sizeof(TA) rows; a lane owns RPL = 16 / sizeof(TA) rows
+// t*T + g*RPL ..).  A tile of rows <= 16 RPL rows needs fewer than 32 lanes
+// per column: the warp then splits into slices of L lanes (L = the row
+// groups rounded up to a power of two), slice sl taking the columns
+// j = sl (mod 32 / L) of each segment, so that every lane has work (a
+// 64-row BF16 tile keeps 8 lanes per column and 4 columns in flight).  Every
 // segment's tile is h x K, column major with column stride h (h = the tile's
 // row count rounded up to height_quantum rows), so a run of its columns is one contiguous byte
 // range, and so is the run of their input values.  Both are staged through a
 // per-warp ring of kPStages shared-memory stages by bulk copies, at most
-// kPStageBytes of tile and kPCols columns per stage.  Column j of a segment
-// goes to accumulator set j & 1.  BF16 dense tiles: the warp multiplies the
-// staged inputs by the column scales first, as in the leaf-panel kernel.
+// kPStageBytes of tile and kPCols columns per stage.  Within one stage a
+// slice's k-th column goes to accumulator set k & 1; the slices' sums are
+// added by shuffles at the end.  BF16 dense tiles: the warp multiplies the
+// staged inputs by the column scales first, once, in place.
 constexpr int kPWarps = 4;           // warps per CTA of panel_tile_kernel
 constexpr int kPStages = HODLR_TUNE_P_STAGES;
 constexpr int kPStageBytes = HODLR_TUNE_P_BYTES;
@@ -999,7 +1056,11 @@ __global__ void __launch_bounds__(kPWarps * 32, HODLR_TUNE_P_MINB)
   const int64_t h = tile_height(m, t, int(sizeof(TA)));
   const int colb = int(h) * int(sizeof(TA));  // bytes per tile column: 16 .. 512, a multiple of 16
   const int cps = min(kPCols, kPStageBytes / colb);
-  const bool act = lane * RPL < rows;
+  int lg = 1;  // lanes per slice
+  while (lg * RPL < rows) lg <<= 1;
+  const int slices = 32 / lg;
+  const int g = lane & (lg - 1), sl = lane / lg;
+  const bool act = g * RPL < rows;
   typename AC::A a0[RPL], a1[RPL];
 #pragma unroll
   for (int q = 0; q < RPL; q++) a0[q] = a1[q] = AC::zero();
@@ -1062,7 +1123,7 @@ __global__ void __launch_bounds__(kPWarps * 32, HODLR_TUNE_P_MINB)
     }
     const int xo = int((reinterpret_cast<uintptr_t>(inc + S.in_off + cc) & 15u) / sizeof(TX));
     const TX* xsm = reinterpret_cast<const TX*>(xbuf + st * kPXBytes) + xo;
-    const unsigned char* us = ubuf + st * kPStageBytes + lane * 16;
+    const unsigned char* us = ubuf + st * kPStageBytes + g * 16;
     if constexpr (sizeof(TA) == 2) {
       // BF16 dense tile: the staged inputs times the column scales, once, in place
       if (S.cscale) {
@@ -1072,25 +1133,17 @@ __global__ void __launch_bounds__(kPWarps * 32, HODLR_TUNE_P_MINB)
       }
     }
 #define HODLR_XIN(j_) AC::in(xsm[j_])
-    int j = 0;
-    for (; j + 1 < nc; j += 2) {
+    // this slice's columns of the stage: segment columns cc + j, j = sl (mod slices)
+    int j = (sl - cc) & (slices - 1);
+    for (; j + slices < nc; j += 2 * slices) {
       const VT v0 = act ? *reinterpret_cast<const VT*>(us + j * colb) : vzero<VT>();
-      const VT v1 = act ? *reinterpret_cast<const VT*>(us + (j + 1) * colb) : vzero<VT>();
-      // column cc + j has the parity of cc + j
-      if (((cc + j) & 1) == 0) {
-        axpy16<TACC>(v0, HODLR_XIN(j), a0);
-        axpy16<TACC>(v1, HODLR_XIN(j + 1), a1);
-      } else {
-        axpy16<TACC>(v0, HODLR_XIN(j), a1);
-        axpy16<TACC>(v1, HODLR_XIN(j + 1), a0);
-      }
+      const VT v1 = act ? *reinterpret_cast<const VT*>(us + (j + slices) * colb) : vzero<VT>();
+      axpy16<TACC>(v0, HODLR_XIN(j), a0);
+      axpy16<TACC>(v1, HODLR_XIN(j + slices), a1);
     }
     if (j < nc) {
       const VT v0 = act ? *reinterpret_cast<const VT*>(us + j * colb) : vzero<VT>();
-      if (((cc + j) & 1) == 0)
-        axpy16<TACC>(v0, HODLR_XIN(j), a0);
-      else
-        axpy16<TACC>(v0, HODLR_XIN(j), a1);
+      axpy16<TACC>(v0, HODLR_XIN(j), a0);
     }
 #undef HODLR_XIN
     cc += nc;
@@ -1098,21 +1151,28 @@ __global__ void __launch_bounds__(kPWarps * 32, HODLR_TUNE_P_MINB)
     HODLR_PANEL_ISSUE_NEXT();  // the next run, if any, into the stage just consumed
   }
 #undef HODLR_PANEL_ISSUE_NEXT
-  if (act) {
-    const int i = t * T + lane * RPL;
+#pragma unroll
+  for (int q = 0; q < RPL; q++) {
+    a0[q] = AC::add(a0[q], a1[q]);
+    for (int o = lg; o < 32; o <<= 1) a0[q] = AC::add(a0[q], AC::shfl_xor(a0[q], o));
+  }
+  if (act && sl == 0) {
+    const int i = t * T + g * RPL;
     TY* dst = it.part < 0 ? y + int64_t(blockIdx.y) * nslots * ld_y + P.yoff + i
-                          : ypart + int64_t(it.part) * T + lane * RPL;
+                          : ypart + int64_t(it.part) * T + g * RPL;
 #pragma unroll
     for (int q = 0; q < RPL; q++)
-      if (i + q < m) dst[q] = TY(AC::value(AC::add(a0[q], a1[q])));
+      if (i + q < m) dst[q] = TY(AC::value(a0[q]));
   }
 }
 
 // ---- direct-load variants, used for FP64 factors ----------------------------
 // FP64 products run on GB300's FP64 pipe, whose rate (not the bytes in
 // flight) bounds these kernels; plain loads with eight warps per CTA keep
-// that pipe busier than the shared-memory staged versions above.  Same lane
-// layouts and summation orders as described above for each phase.
+// that pipe busier than the shared-memory staged versions above.  Lane
+// layouts as described above for each phase; the node-panel variant keeps
+// one column per warp step (no column slices), with columns alternating
+// between the two accumulator sets.
 template <typename TA, typename TACC>
 __global__ void __launch_bounds__(256) zgemv_direct_kernel(const ZBlock* __restrict__ zb, const ZItem* __restrict__ items,
                                                     int nitems, typename IO<TACC>::TY* __restrict__ zpart,
@@ -1504,10 +1564,11 @@ static void panels_leaf(const Panel* panels, const Seg* segs, const Item* small,
                         int64_t ld_in, void* ypart, void* y, int64_t ld_y, int nslots, int nrhs, cudaStream_t st) {
   using TI = typename IO<TACC>::TI;
   using TY = typename IO<TACC>::TY;
+  using TX = typename LeafX<TACC>::T;
   dim3 g(unsigned((nsmall + kLWarps - 1) / kLWarps), unsigned(nrhs));
   cudaFuncSetAttribute(panel_leaf_kernel<TA, TACC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       kLWarps * l_warp_smem<TA, TI>());
-  panel_leaf_kernel<TA, TACC><<<g, kLWarps * 32, kLWarps * l_warp_smem<TA, TI>(), st>>>(
+                       kLWarps * l_warp_smem<TA, TX>());
+  panel_leaf_kernel<TA, TACC><<<g, kLWarps * 32, kLWarps * l_warp_smem<TA, TX>(), st>>>(
       panels, segs, small, nsmall, static_cast<const TI*>(in), ld_in, static_cast<TY*>(y), ld_y, nslots,
       static_cast<TY*>(ypart));
 }
