@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -17,6 +18,7 @@
 #include "dtree.h"
 #include "gmres.h"
 #include "matvec.h"
+#include "par.h"
 #include "tc.h"
 #include "tree.hpp"
 
@@ -670,25 +672,28 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   const int ndim = op0->p.ndim;
   const Prec fp = far_prec(op0->p);
   const int cap0 = op0->p.rank_cap > 0 ? op0->p.rank_cap : 64;
+  bool any_ref = false;  // some operator keeps an FP64 copy of its far field
+  for (const hodlr_op* op : ops) any_ref = any_ref || op->has_ref;
   // global block g = boff[j] + b: operator j, its far block b
   std::vector<int32_t> job(nb), cap(nb), mm(nb), nn(nb);
   std::vector<int64_t> tb(nb), sb(nb), tmap(nb), smap(nb);
-  for (size_t j = 0; j < nops; j++) {
+#pragma omp parallel for schedule(static) num_threads(par_threads(int64_t(nb)))
+  for (int64_t gi = 0; gi < int64_t(nb); gi++) {
+    const size_t g = size_t(gi);
+    // the operator holding g: the last j with boff[j] <= g (empty operators skipped)
+    const size_t j = size_t(std::upper_bound(boff.begin(), boff.end(), gi) - boff.begin()) - 1;
     const hodlr_op* op = ops[j];
     const Tree& t = op->tree;
-    for (size_t b = 0; b < op->far.size(); b++) {
-      const size_t g = size_t(boff[j]) + b;
-      const FarBlock& f = op->far[b];
-      const int64_t gt = t.gid(f.level, f.t), gs = t.gid(f.level, f.s);
-      job[g] = int32_t(j);
-      mm[g] = int32_t(t.count[size_t(gt)]);
-      nn[g] = int32_t(t.count[size_t(gs)]);
-      tb[g] = pbase[j] + t.begin[size_t(gt)];
-      sb[g] = pbase[j] + t.begin[size_t(gs)];
-      tmap[g] = lbase[j] + int64_t(f.level) * op->n + t.begin[size_t(gt)];
-      smap[g] = lbase[j] + int64_t(f.level) * op->n + t.begin[size_t(gs)];
-      cap[g] = std::min({mm[g], nn[g], cap0});
-    }
+    const FarBlock& f = op->far[g - size_t(boff[j])];
+    const int64_t gt = t.gid(f.level, f.t), gs = t.gid(f.level, f.s);
+    job[g] = int32_t(j);
+    mm[g] = int32_t(t.count[size_t(gt)]);
+    nn[g] = int32_t(t.count[size_t(gs)]);
+    tb[g] = pbase[j] + t.begin[size_t(gt)];
+    sb[g] = pbase[j] + t.begin[size_t(gs)];
+    tmap[g] = lbase[j] + int64_t(f.level) * op->n + t.begin[size_t(gt)];
+    smap[g] = lbase[j] + int64_t(f.level) * op->n + t.begin[size_t(gs)];
+    cap[g] = std::min({mm[g], nn[g], cap0});
   }
   auto ws_need = [&](size_t g) { return uint64_t(cap[g]) * uint64_t(mm[g] + nn[g]); };
   // Scratch of one batch: the FP64 workspace is bounded (4 GiB by default);
@@ -759,16 +764,46 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     d_lmap = static_cast<const int32_t*>(s_lmap.p);
   }
   // large blocks first keeps the CTA-team launch ahead of the warp teams: a
-  // stable counting sort by max(m, n), descending (the sizes are node sizes)
+  // stable counting sort by max(m, n), descending (the sizes are node sizes);
+  // threads count and place contiguous shares, with at most 64 MB of counters
   std::vector<size_t> todo(nb);
   {
     int32_t kmax = 0;
-    for (size_t g = 0; g < nb; g++) kmax = std::max(kmax, std::max(mm[g], nn[g]));
-    std::vector<size_t> start(size_t(kmax) + 2, 0);
-    for (size_t g = 0; g < nb; g++) start[size_t(kmax - std::max(mm[g], nn[g])) + 1]++;
-    for (size_t k = 1; k < start.size(); k++) start[k] += start[k - 1];
-    for (size_t g = 0; g < nb; g++) todo[start[size_t(kmax - std::max(mm[g], nn[g]))]++] = g;
+#pragma omp parallel for schedule(static) reduction(max : kmax) num_threads(par_threads(int64_t(nb)))
+    for (int64_t g = 0; g < int64_t(nb); g++) kmax = std::max(kmax, std::max(mm[size_t(g)], nn[size_t(g)]));
+    const size_t K = size_t(kmax) + 1;
+    const int T = int(std::max<int64_t>(1, std::min<int64_t>(par_threads(int64_t(nb)), (int64_t(8) << 20) / int64_t(K))));
+    std::vector<uint64_t> cnt(size_t(T) * K, 0);
+    auto key = [&](size_t g) { return size_t(kmax - std::max(mm[g], nn[g])); };
+#pragma omp parallel num_threads(T)
+    {
+      const int t = omp_get_thread_num();
+      int64_t b, e;
+      par_share(int64_t(nb), t, T, b, e);
+      uint64_t* c = cnt.data() + size_t(t) * K;
+      for (int64_t g = b; g < e; g++) c[key(size_t(g))]++;
+#pragma omp barrier
+#pragma omp single
+      {
+        uint64_t s = 0;  // (key, thread) order
+        for (size_t k = 0; k < K; k++)
+          for (int u = 0; u < T; u++) {
+            const uint64_t v = cnt[size_t(u) * K + k];
+            cnt[size_t(u) * K + k] = s;
+            s += v;
+          }
+      }
+      for (int64_t g = b; g < e; g++) todo[c[key(size_t(g))]++] = size_t(g);
+    }
   }
+  // budgets of the blocks in that order (prefix sums): FP64 workspace, pivot
+  // bitmap words and pivot list entries
+  auto bits_need = [&](size_t g) { return uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32); };
+  auto list_need = [&](size_t g) { return uint64_t(2 * (std::min(mm[g], nn[g]) + 2)); };
+  std::vector<uint64_t> pw(nb + 1), pbits(nb + 1), plist(nb + 1);
+  par_exclusive_scan(int64_t(nb), pw.data(), [&](int64_t i) { return ws_need(todo[size_t(i)]); });
+  par_exclusive_scan(int64_t(nb), pbits.data(), [&](int64_t i) { return bits_need(todo[size_t(i)]); });
+  par_exclusive_scan(int64_t(nb), plist.data(), [&](int64_t i) { return list_need(todo[size_t(i)]); });
 
   KernelDev K{op0->kd.kind, op0->kd.scale, op0->kd.diag};
   struct Events {
@@ -812,15 +847,13 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   std::vector<size_t> retry;
   std::vector<AcaBlockDesc> desc;
   std::vector<AcaOut> out;
-  std::vector<std::vector<int32_t>> team_list(kAcaTeamKinds);
   std::vector<CompactDesc> cds;
   while (pos < todo.size() || !retry.empty()) {
     // next batch
     std::vector<size_t> batch;
     uint64_t acc_w = 0, acc_b = 0, acc_l = 0;
     auto take = [&](size_t g) {
-      const uint64_t w = ws_need(g), bw = uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32),
-                     lw = uint64_t(2 * (std::min(mm[g], nn[g]) + 2));
+      const uint64_t w = ws_need(g), bw = bits_need(g), lw = list_need(g);
       if (!batch.empty() && (acc_w + w > ws_doubles || acc_b + bw > bits_room || acc_l + lw > list_room ||
                              batch.size() >= max_batch))
         return false;
@@ -836,31 +869,41 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
         if (!take(g)) rest.push_back(g);
       retry.swap(rest);
     } else {
-      while (pos < todo.size() && take(todo[pos])) pos++;
+      // the longest run from pos within every budget (at least one block):
+      // the prefix sums are monotone, so a binary search finds its end
+      auto fits = [&](size_t e) {
+        return pw[e] - pw[pos] <= ws_doubles && pbits[e] - pbits[pos] <= bits_room &&
+               plist[e] - plist[pos] <= list_room && e - pos <= max_batch;
+      };
+      size_t lo = pos + 1, hi = todo.size();  // fits(lo) is not required: one block always goes
+      while (lo < hi) {
+        const size_t mid = lo + (hi - lo + 1) / 2;
+        if (fits(mid))
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      batch.assign(todo.begin() + int64_t(pos), todo.begin() + int64_t(lo));
+      pos = lo;
     }
     // descriptors: per-block sizes and teams (parallel: the blocks are visited
     // in size order, so their arrays are read at random), offsets by a prefix
     // sum, then the descriptors (parallel again)
     const size_t nq = batch.size();
+    const int tq = par_threads(int64_t(nq));
     desc.resize(nq);
     std::vector<uint64_t> qw(nq + 1), qb(nq + 1), ql(nq + 1);
+    par_exclusive_scan(int64_t(nq), qw.data(), [&](int64_t q) { return ws_need(batch[size_t(q)]); });
+    par_exclusive_scan(int64_t(nq), qb.data(), [&](int64_t q) { return bits_need(batch[size_t(q)]); });
+    par_exclusive_scan(int64_t(nq), ql.data(), [&](int64_t q) { return list_need(batch[size_t(q)]); });
     std::vector<int8_t> qteam(nq);
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(tq)
     for (int64_t q = 0; q < int64_t(nq); q++) {
       const size_t g = batch[size_t(q)];
-      qw[size_t(q) + 1] = ws_need(g);
-      qb[size_t(q) + 1] = uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32);
-      ql[size_t(q) + 1] = uint64_t(2 * (std::min(mm[g], nn[g]) + 2));
       qteam[size_t(q)] = int8_t(aca_team(mm[g], nn[g]));
     }
-    qw[0] = qb[0] = ql[0] = 0;
-    for (size_t q = 0; q < nq; q++) {
-      qw[q + 1] += qw[q];
-      qb[q + 1] += qb[q];
-      ql[q + 1] += ql[q];
-    }
     const uint64_t ow = qw[nq], ob = qb[nq], ol = ql[nq];
-#pragma omp parallel for schedule(static)
+#pragma omp parallel for schedule(static) num_threads(tq)
     for (int64_t q = 0; q < int64_t(nq); q++) {
       const size_t g = batch[size_t(q)];
       const hodlr_op* op = ops[size_t(job[g])];
@@ -879,16 +922,25 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       d.seed = block_seed(f.level, f.t, f.s);
       d.kscale = joint ? op->kd.scale : 0.0;
     }
-    for (auto& l : team_list) l.clear();
-    for (size_t q = 0; q < nq; q++) team_list[size_t(qteam[q])].push_back(int32_t(q));
-    // one index array, the team kinds one after another (largest blocks first)
-    std::vector<int32_t> lst;
+    // one index array, the team kinds one after another (largest teams
+    // first), each kind's blocks in batch order (a stable partition)
+    std::vector<uint64_t> lofs(nq), lcount;
+    par_group_offsets(
+        int64_t(nq), kAcaTeamKinds, lofs.data(), lcount,
+        [&](int64_t q) { return kAcaTeamKinds - 1 - int(qteam[size_t(q)]); }, [](int64_t) { return uint64_t(1); });
     AcaLists al;
-    size_t lpos[kAcaTeamKinds];
-    for (int k = kAcaTeamKinds - 1; k >= 0; k--) {
-      lpos[k] = lst.size();
-      lst.insert(lst.end(), team_list[size_t(k)].begin(), team_list[size_t(k)].end());
+    size_t lpos[kAcaTeamKinds], lcnt[kAcaTeamKinds];
+    {
+      size_t base = 0;
+      for (int k = kAcaTeamKinds - 1; k >= 0; k--) {
+        lpos[k] = base;
+        lcnt[k] = size_t(lcount[size_t(kAcaTeamKinds - 1 - k)]);
+        base += lcnt[k];
+      }
     }
+    std::vector<int32_t> lst(nq);
+#pragma omp parallel for schedule(static) num_threads(tq)
+    for (int64_t q = 0; q < int64_t(nq); q++) lst[lpos[qteam[size_t(q)]] + lofs[size_t(q)]] = int32_t(q);
     s_ws.ensure((ow + arena_doubles) * 8, st, "ACA workspace");
     s_bits.ensure(std::max<uint64_t>(ob, 1) * 4, st, "ACA bitmaps");
     s_lists.ensure(std::max<uint64_t>(ol, 1) * 4, st, "ACA index lists");
@@ -915,7 +967,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     a.max_ctas = sms * 16;
     for (int k = 0; k < kAcaTeamKinds; k++) {
       al.list[k] = d_lists_idx + lpos[k];
-      al.n[k] = int(team_list[size_t(k)].size());
+      al.n[k] = int(lcnt[k]);
     }
     // the team kinds at once, on side streams forked from st and joined back
     CK(cudaEventRecord(ev_a0, st));
@@ -934,26 +986,48 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
       t_kernel += 1e-3 * double(ms);
     }
-    // compaction of the finished blocks: one chunk per operator and batch
-    std::vector<uint64_t> bytes(nops, 0), off(batch.size(), 0);
-    std::vector<int64_t> kidx(batch.size() + 1, 0);  // position among the blocks compacted (dense or rank > 0)
-    for (size_t q = 0; q < batch.size(); q++) {
-      const size_t g = batch[q];
-      kidx[q + 1] = kidx[q];
+    // compaction of the finished blocks: one chunk per operator and batch.
+    // Blocks that outgrew their columns go back with 4x the columns.
+    int64_t novf = 0;
+#pragma omp parallel for schedule(static) reduction(+ : novf) num_threads(tq)
+    for (int64_t qi = 0; qi < int64_t(nq); qi++) {
+      const size_t q = size_t(qi), g = batch[q];
       if (out[q].flags & kAcaOverflow) {
         cap[g] = std::min(std::min(mm[g], nn[g]), cap[g] * 4);
-        retry.push_back(g);
+        novf++;
         continue;
       }
       hodlr_op* op = ops[size_t(job[g])];
       const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
       op->rank[b] = out[q].rank;
       op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
-      off[q] = bytes[size_t(job[g])];
-      const int64_t r = op->rank[b];
-      bytes[size_t(job[g])] += far_u_bytes(mm[g], nn[g], r, op->dense[b], fp) + far_v_bytes(nn[g], r, op->dense[b], fp);
-      if (op->dense[b] || r > 0) kidx[q + 1]++;
     }
+    if (novf > 0)
+      for (size_t q = 0; q < nq; q++)
+        if (out[q].flags & kAcaOverflow) retry.push_back(batch[q]);
+    // a finished block's op, its index there, and whether it is stored
+    auto blk = [&](int64_t q, hodlr_op*& op, size_t& b) -> bool {
+      const size_t g = batch[size_t(q)];
+      op = ops[size_t(job[g])];
+      b = size_t(int64_t(g) - boff[size_t(job[g])]);
+      return !(out[size_t(q)].flags & kAcaOverflow);
+    };
+    auto job_of = [&](int64_t q) { return int(job[batch[size_t(q)]]); };
+    // byte offsets within each operator's chunk (batch order) and the
+    // position among the blocks compacted (dense or rank > 0)
+    std::vector<uint64_t> bytes, off(nq), kidx(nq + 1);
+    par_group_offsets(int64_t(nq), int(nops), off.data(), bytes, job_of, [&](int64_t q) -> uint64_t {
+      hodlr_op* op;
+      size_t b;
+      if (!blk(q, op, b)) return 0;
+      const size_t g = batch[size_t(q)];
+      return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], fp) + far_v_bytes(nn[g], op->rank[b], op->dense[b], fp);
+    });
+    par_exclusive_scan(int64_t(nq), kidx.data(), [&](int64_t q) -> uint64_t {
+      hodlr_op* op;
+      size_t b;
+      return blk(q, op, b) && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
+    });
     cds.resize(size_t(kidx[batch.size()]));
     std::vector<char*> chunk(nops, nullptr);
     for (size_t j = 0; j < nops; j++)
@@ -1007,21 +1081,21 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       t_compact += 1e-3 * double(ms);
     }
     // the FP64 factors of the same blocks, for operators that keep them
-    if (fp != Prec::kD) {
-      std::vector<uint64_t> bytes64(nops, 0), off64(batch.size(), 0);
-      std::vector<int64_t> kidx64(batch.size() + 1, 0);
-      for (size_t q = 0; q < batch.size(); q++) {
-        const size_t g = batch[q];
-        kidx64[q + 1] = kidx64[q];
-        hodlr_op* op = ops[size_t(job[g])];
-        if (!op->has_ref || (out[q].flags & kAcaOverflow)) continue;
-        const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
-        off64[q] = bytes64[size_t(job[g])];
-        const int64_t r = op->rank[b];
-        bytes64[size_t(job[g])] += far_u_bytes(mm[g], nn[g], r, op->dense[b], Prec::kD) +
-                                   far_v_bytes(nn[g], r, op->dense[b], Prec::kD);
-        if (op->dense[b] || r > 0) kidx64[q + 1]++;
-      }
+    if (fp != Prec::kD && any_ref) {
+      std::vector<uint64_t> bytes64, off64(nq), kidx64(nq + 1);
+      par_group_offsets(int64_t(nq), int(nops), off64.data(), bytes64, job_of, [&](int64_t q) -> uint64_t {
+        hodlr_op* op;
+        size_t b;
+        if (!blk(q, op, b) || !op->has_ref) return 0;
+        const size_t g = batch[size_t(q)];
+        return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD) +
+               far_v_bytes(nn[g], op->rank[b], op->dense[b], Prec::kD);
+      });
+      par_exclusive_scan(int64_t(nq), kidx64.data(), [&](int64_t q) -> uint64_t {
+        hodlr_op* op;
+        size_t b;
+        return blk(q, op, b) && op->has_ref && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
+      });
       std::vector<char*> chunk64(nops, nullptr);
       bool any = false;
       for (size_t j = 0; j < nops; j++)
@@ -1426,6 +1500,41 @@ int guarded(hodlr_ctx* ctx, const std::function<int()>& f) {
   } catch (const std::exception& e) {
     return fail(ctx, HODLR_ERR_INVALID, e.what());
   }
+}
+
+// Runs f(i, stream) for i < n on host threads, each with the device set and
+// its own non-blocking stream (synchronised before the thread ends): the
+// per-instance parts of a batch build are independent, and their host work
+// (plans, allocations) dominates for small instances.  The first failure is
+// rethrown once every thread has finished.
+template <class F>
+void for_each_instance(int n, int device, F f) {
+  const int T = std::max(1, std::min(n, std::min(omp_get_max_threads(), 16)));
+  std::vector<Failure> errs(size_t(T), Failure{HODLR_OK, std::string()});
+  std::atomic<int> next{0};
+  auto worker = [&](int t) {
+    Failure& err = errs[size_t(t)];
+    cudaStream_t s = nullptr;
+    try {
+      check_cuda(cudaSetDevice(device), "cudaSetDevice");
+      check_cuda(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
+      for (int i = next++; i < n; i = next++) f(i, s);
+    } catch (const Failure& e) {
+      err = e;
+    } catch (const std::bad_alloc&) {
+      err = Failure{HODLR_ERR_OOM, "host allocation failed"};
+    } catch (const std::exception& e) {
+      err = Failure{HODLR_ERR_INVALID, e.what()};
+    }
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  };
+#pragma omp parallel num_threads(T)
+  worker(omp_get_thread_num());
+  for (const Failure& e : errs)
+    if (e.code != HODLR_OK) throw e;
 }
 
 }  // namespace
@@ -2747,15 +2856,19 @@ int hodlr_build_batch(hodlr_ctx* ctx, int32_t count, const double* const* points
       op->keep_host_plans = true;
       op->batch_owned = true;
       std::memset(&op->st, 0, sizeof(op->st));
-      build_prepare(op, points[i], box_lo + size_t(i) * d, box_hi + size_t(i) * d, st, bs[size_t(i)]);
     }
+    CK(cudaStreamSynchronize(st));
+    for_each_instance(count, ctx->p.device, [&](int i, cudaStream_t s) {
+      build_prepare(b->ops[size_t(i)], points[i], box_lo + size_t(i) * d, box_hi + size_t(i) * d, s, bs[size_t(i)]);
+    });
     const double ta = now_s();
     run_aca(b->ops, st);
     const double t_aca = now_s() - ta;
-    for (int32_t i = 0; i < count; i++) {
+    CK(cudaStreamSynchronize(st));
+    for_each_instance(count, ctx->p.device, [&](int i, cudaStream_t s) {
       b->ops[size_t(i)]->st.t_aca_s = t_aca;
-      build_finish(b->ops[size_t(i)], bs[size_t(i)], st);
-    }
+      build_finish(b->ops[size_t(i)], bs[size_t(i)], s);
+    });
     build_batch_plan(*b, st);
     *out = b.release();
     return HODLR_OK;
