@@ -1029,14 +1029,41 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       return blk(q, op, b) && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
     });
     cds.resize(size_t(kidx[batch.size()]));
-    std::vector<char*> chunk(nops, nullptr);
-    for (size_t j = 0; j < nops; j++)
+    // the FP64 copy of the same blocks, for operators that keep one: with
+    // FP32 factors both copies come from one compaction pass (the entries of
+    // a dense tile are evaluated once)
+    const bool ref64 = fp != Prec::kD && any_ref, dual = ref64 && fp == Prec::kF;
+    std::vector<uint64_t> bytes64, off64, kidx64;
+    if (ref64) {
+      off64.resize(nq);
+      kidx64.resize(nq + 1);
+      par_group_offsets(int64_t(nq), int(nops), off64.data(), bytes64, job_of, [&](int64_t q) -> uint64_t {
+        hodlr_op* op;
+        size_t b;
+        if (!blk(q, op, b) || !op->has_ref) return 0;
+        const size_t g = batch[size_t(q)];
+        return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD) +
+               far_v_bytes(nn[g], op->rank[b], op->dense[b], Prec::kD);
+      });
+      par_exclusive_scan(int64_t(nq), kidx64.data(), [&](int64_t q) -> uint64_t {
+        hodlr_op* op;
+        size_t b;
+        return blk(q, op, b) && op->has_ref && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
+      });
+    }
+    std::vector<char*> chunk(nops, nullptr), chunk64(nops, nullptr);
+    for (size_t j = 0; j < nops; j++) {
       if (bytes[j] > 0) {
         chunk[j] = static_cast<char*>(ops[j]->mem.alloc(bytes[j], "far-field factors"));
         ops[j]->far_chunks.push_back(chunk[j]);
         CK(cudaMemsetAsync(chunk[j], 0, bytes[j], st));  // tile padding rows must read as zero
       }
-#pragma omp parallel for schedule(static)
+      if (ref64 && bytes64[j] > 0) {
+        chunk64[j] = static_cast<char*>(ops[j]->mem.alloc(bytes64[j], "far-field factors (FP64 reference)"));
+        CK(cudaMemsetAsync(chunk64[j], 0, bytes64[j], st));
+      }
+    }
+#pragma omp parallel for schedule(static) num_threads(tq)
     for (int64_t qi = 0; qi < int64_t(batch.size()); qi++) {
       const size_t q = size_t(qi);
       const size_t g = batch[q];
@@ -1065,6 +1092,14 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       c.cap = out[q].cap ? out[q].cap : desc[q].cap;
       c.pad = 0;
       c.kscale = desc[q].kscale;
+      c.u64_dst = c.v64_dst = nullptr;
+      if (dual && kidx64[q + 1] > kidx64[q]) {
+        char* ch64 = chunk64[size_t(job[g])];
+        c.u64_dst = ch64 + off64[q];
+        c.v64_dst = ch64 + off64[q] + far_u_bytes(mm[g], nn[g], rk, op->dense[b], Prec::kD);
+        op->uptr64[b] = c.u64_dst;
+        op->vptr64[b] = c.v64_dst;
+      }
       op->uptr[b] = c.u_dst;
       op->vptr[b] = c.v_dst;
       if (kidx[q + 1] > kidx[q]) cds[size_t(kidx[q])] = c;
@@ -1080,30 +1115,10 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
       t_compact += 1e-3 * double(ms);
     }
-    // the FP64 factors of the same blocks, for operators that keep them
-    if (fp != Prec::kD && any_ref) {
-      std::vector<uint64_t> bytes64, off64(nq), kidx64(nq + 1);
-      par_group_offsets(int64_t(nq), int(nops), off64.data(), bytes64, job_of, [&](int64_t q) -> uint64_t {
-        hodlr_op* op;
-        size_t b;
-        if (!blk(q, op, b) || !op->has_ref) return 0;
-        const size_t g = batch[size_t(q)];
-        return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD) +
-               far_v_bytes(nn[g], op->rank[b], op->dense[b], Prec::kD);
-      });
-      par_exclusive_scan(int64_t(nq), kidx64.data(), [&](int64_t q) -> uint64_t {
-        hodlr_op* op;
-        size_t b;
-        return blk(q, op, b) && op->has_ref && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
-      });
-      std::vector<char*> chunk64(nops, nullptr);
+    // BF16 factors: the FP64 copy in a pass of its own
+    if (ref64 && !dual) {
       bool any = false;
-      for (size_t j = 0; j < nops; j++)
-        if (bytes64[j] > 0) {
-          chunk64[j] = static_cast<char*>(ops[j]->mem.alloc(bytes64[j], "far-field factors (FP64 reference)"));
-          CK(cudaMemsetAsync(chunk64[j], 0, bytes64[j], st));
-          any = true;
-        }
+      for (size_t j = 0; j < nops; j++) any = any || chunk64[j] != nullptr;
       if (any) {
         std::vector<CompactDesc> cd64(static_cast<size_t>(kidx64[batch.size()]));
 #pragma omp parallel for schedule(static)
@@ -1130,6 +1145,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
           c.cap = out[q].cap ? out[q].cap : desc[q].cap;
           c.pad = 0;
           c.kscale = desc[q].kscale;
+          c.u64_dst = c.v64_dst = nullptr;
           op->uptr64[b] = c.u_dst;
           op->vptr64[b] = c.v_dst;
           cd64[size_t(kidx64[q])] = c;

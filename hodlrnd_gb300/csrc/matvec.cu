@@ -1404,6 +1404,7 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
                                                       const CompactDesc* __restrict__ blocks, int nblocks) {
   const CompactDesc B = blocks[blockIdx.x];
   TO* u = static_cast<TO*>(B.u_dst);
+  double* u64 = static_cast<double*>(B.u64_dst);  // the FP64 copy too, when asked for
   constexpr int esz = int(sizeof(TO));
   if (B.kscale != 0.0) K.scale = B.kscale;
   if (B.dense) {
@@ -1412,23 +1413,30 @@ __global__ void __launch_bounds__(256) compact_kernel(PointsDev P, KernelDev K, 
       const int i = int(e % B.m), j = int(e / B.m);
       double xi[D];
       load_point<D>(P, B.t_begin + i, xi);
-      u[elem_offset(i, j, B.m, B.n, esz)] = TO(kernel_entry<D>(P, K, B.t_begin + i, B.s_begin + j, xi));
+      const double a = kernel_entry<D>(P, K, B.t_begin + i, B.s_begin + j, xi);
+      u[elem_offset(i, j, B.m, B.n, esz)] = TO(a);
+      if (u64) u64[elem_offset(i, j, B.m, B.n, 8)] = a;
     }
   } else {
     const double* U = ws + B.ws;
     const int64_t nu = int64_t(B.m) * B.rank;
     for (int64_t e = threadIdx.x; e < nu; e += blockDim.x) {
       const int i = int(e % B.m), k = int(e / B.m);
-      u[elem_offset(lmap[B.t_map + i] - B.t_begin, k, B.m, B.rank, esz)] = TO(U[e]);
+      const int64_t row = lmap[B.t_map + i] - B.t_begin;
+      u[elem_offset(row, k, B.m, B.rank, esz)] = TO(U[e]);
+      if (u64) u64[elem_offset(row, k, B.m, B.rank, 8)] = U[e];
     }
     // V follows U's full workspace (m x cap); stored row major, n x vpad(rank)
     const double* Vw = ws + B.ws + int64_t(B.m) * B.cap;
     TO* v = static_cast<TO*>(B.v_dst);
-    const int64_t rp = vpad(B.rank, esz);
+    double* v64 = static_cast<double*>(B.v64_dst);
+    const int64_t rp = vpad(B.rank, esz), rp64 = vpad(B.rank, 8);
     const int64_t nv = int64_t(B.n) * B.rank;
     for (int64_t e = threadIdx.x; e < nv; e += blockDim.x) {
       const int j = int(e % B.n), k = int(e / B.n);
-      v[(lmap[B.s_map + j] - B.s_begin) * rp + k] = TO(Vw[e]);
+      const int64_t row = lmap[B.s_map + j] - B.s_begin;
+      v[row * rp + k] = TO(Vw[e]);
+      if (v64) v64[row * rp64 + k] = Vw[e];
     }
   }
 }

@@ -272,6 +272,8 @@ struct CompactDesc {
   int32_t pad;
   double kscale;      // kernel scale for a dense block's entries; 0: the launch's K.scale
   float* s_dst;       // BF16: column scales of a dense tile, or z column scales of a low-rank block
+  void* u64_dst;      // FP32 launches: the FP64 copy of U or of the dense tile as well (null: none)
+  void* v64_dst;      // and of V
 };
 // U row i (reference order) lands on tree row lmap[t_map + i] - t_begin; V likewise.
 cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,
