@@ -574,6 +574,19 @@ void launch_kind(const AcaArgs& a, const AcaLists& L, int kind, cudaStream_t st)
   }
 }
 
+// The launches' kernels, loaded before the first launch: with lazy module
+// loading, loading a kernel while others run waits for them, which would
+// serialise the team kinds' concurrent launches.
+template <int D>
+cudaError_t preload_d() {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, aca_cta_kernel<D>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, aca_warp_kernel<D>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, aca_sub_kernel<D, 16>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, aca_sub_kernel<D, 8>);
+  return e;
+}
+
 template <int D>
 void launch_d(const AcaArgs& a, const AcaLists& L, cudaStream_t st) {
   for (int k : {kAcaTeamCta, kAcaTeamWarp, kAcaTeam16, kAcaTeam8}) launch_kind<D>(a, L, k, st);
@@ -587,6 +600,20 @@ int aca_team(int m, int n) {
   if (mx <= 16) return kAcaTeam16;
   if (mx <= 256) return kAcaTeamWarp;
   return kAcaTeamCta;
+}
+
+cudaError_t aca_preload(int ndim) {
+  switch (ndim) {
+    case 1: return preload_d<1>();
+    case 2: return preload_d<2>();
+    case 3: return preload_d<3>();
+    case 4: return preload_d<4>();
+    case 5: return preload_d<5>();
+    case 6: return preload_d<6>();
+    case 7: return preload_d<7>();
+    case 8: return preload_d<8>();
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 cudaError_t launch_aca_kind(int ndim, const AcaArgs& a, const AcaLists& L, int kind, cudaStream_t st) {

@@ -78,5 +78,8 @@ cudaError_t launch_aca(int ndim, const AcaArgs& a, const AcaLists& lists, cudaSt
 // The team kind `kind` alone (its list in lists), asynchronous on st: the kinds
 // touch disjoint blocks and may run on different streams at once.
 cudaError_t launch_aca_kind(int ndim, const AcaArgs& a, const AcaLists& lists, int kind, cudaStream_t st);
+// Loads the ACA kernels of points in ndim dimensions (before launches that
+// should run concurrently).
+cudaError_t aca_preload(int ndim);
 
 }  // namespace hodlr

@@ -647,6 +647,23 @@ Prec far_prec(const hodlr_params& p) {
 // FP32) and op->uptr / op->vptr record where.  With several operators their
 // points and reference-order maps are concatenated for the launches, and each
 // block carries its operator's kernel scale.
+// Batches of at least kAcaWaveMin blocks (run_aca) are compacted kind by
+// kind while the other kinds are still being compressed.
+constexpr size_t kAcaWaveMin = size_t(1) << 18;
+constexpr size_t kAcaCtrBytes = 32;  // the arena counter, then the kinds' queue counters (from byte 16)
+
+// Events without timing, destroyed with the set.
+struct EventSet {
+  std::vector<cudaEvent_t> e;
+  explicit EventSet(int n) : e(size_t(n), nullptr) {
+    for (cudaEvent_t& x : e) check_cuda(cudaEventCreateWithFlags(&x, cudaEventDisableTiming), "cudaEventCreate");
+  }
+  ~EventSet() {
+    for (cudaEvent_t x : e)
+      if (x) cudaEventDestroy(x);
+  }
+};
+
 void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   const size_t nops = ops.size();
   hodlr_op* op0 = ops[0];
@@ -734,8 +751,9 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   s_idx.ensure(nslot * sizeof(int32_t), st, "ACA team lists");
   const size_t max_cd = size_t(1) << 20;  // compaction descriptors per launch
   s_cd.ensure(std::min(nslot, max_cd) * sizeof(CompactDesc), st, "compaction descriptors");
-  // the work-queue counters of the team kinds and the growth arena's counter
-  s_ctr.ensure(64, st, "ACA counters");
+  // the growth arena's counter (bytes 0..7), then the work-queue counters of
+  // the team kinds (from byte 16)
+  s_ctr.ensure(kAcaCtrBytes, st, "ACA counters");
   int sms = 0;
   check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op0->p.device), "cudaDeviceGetAttribute");
   AcaBlockDesc* d_desc = static_cast<AcaBlockDesc*>(s_desc.p);
@@ -806,6 +824,9 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   par_exclusive_scan(int64_t(nb), plist.data(), [&](int64_t i) { return list_need(todo[size_t(i)]); });
 
   KernelDev K{op0->kd.kind, op0->kd.scale, op0->kd.diag};
+  // every kernel of the launches below loaded now, while the GPU is idle
+  check_cuda(aca_preload(ndim), "ACA kernels");
+  check_cuda(compact_preload(ndim), "compaction kernels");
   struct Events {
     cudaEvent_t e[2] = {nullptr, nullptr};
     ~Events() {
@@ -820,17 +841,27 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   struct Side {
     cudaStream_t s[kAcaTeamKinds] = {};
     cudaEvent_t e[kAcaTeamKinds] = {};
+    cudaStream_t cs = nullptr;              // compaction stream
+    cudaEvent_t c0 = nullptr, c1 = nullptr;  // compaction launch timing
     ~Side() {
+      if (cs) cudaStreamSynchronize(cs);
       for (int k = 0; k < kAcaTeamKinds; k++) {
+        if (s[k]) cudaStreamSynchronize(s[k]);
         if (e[k]) cudaEventDestroy(e[k]);
         if (s[k]) cudaStreamDestroy(s[k]);
       }
+      if (c0) cudaEventDestroy(c0);
+      if (c1) cudaEventDestroy(c1);
+      if (cs) cudaStreamDestroy(cs);
     }
   } side;
   for (int k = 0; k < kAcaTeamKinds; k++) {
     check_cuda(cudaStreamCreateWithFlags(&side.s[k], cudaStreamNonBlocking), "cudaStreamCreate");
     check_cuda(cudaEventCreateWithFlags(&side.e[k], cudaEventDisableTiming), "cudaEventCreate");
   }
+  check_cuda(cudaStreamCreateWithFlags(&side.cs, cudaStreamNonBlocking), "cudaStreamCreate");
+  check_cuda(cudaEventCreate(&side.c0), "cudaEventCreate");
+  check_cuda(cudaEventCreate(&side.c1), "cudaEventCreate");
   double t_kernel = 0.0, t_compact = 0.0;
   // device times shared by every operator of the launch
   struct Report {
@@ -892,6 +923,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     const size_t nq = batch.size();
     const int tq = par_threads(int64_t(nq));
     desc.resize(nq);
+    out.resize(nq);
     std::vector<uint64_t> qw(nq + 1), qb(nq + 1), ql(nq + 1);
     par_exclusive_scan(int64_t(nq), qw.data(), [&](int64_t q) { return ws_need(batch[size_t(q)]); });
     par_exclusive_scan(int64_t(nq), qb.data(), [&](int64_t q) { return bits_need(batch[size_t(q)]); });
@@ -903,50 +935,10 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       qteam[size_t(q)] = int8_t(aca_team(mm[g], nn[g]));
     }
     const uint64_t ow = qw[nq], ob = qb[nq], ol = ql[nq];
-#pragma omp parallel for schedule(static) num_threads(tq)
-    for (int64_t q = 0; q < int64_t(nq); q++) {
-      const size_t g = batch[size_t(q)];
-      const hodlr_op* op = ops[size_t(job[g])];
-      const FarBlock& f = op->far[size_t(int64_t(g) - boff[size_t(job[g])])];
-      AcaBlockDesc& d = desc[size_t(q)];
-      d.t_map = tmap[g];
-      d.s_map = smap[g];
-      d.m = mm[g];
-      d.n = nn[g];
-      d.cap = cap[g];
-      // the pivot lists hold every rank the block can reach, also after it grows into the arena
-      d.lcap = std::min(mm[g], nn[g]);
-      d.ws = int64_t(qw[size_t(q)]);
-      d.bits = int64_t(qb[size_t(q)]);
-      d.lists = int64_t(ql[size_t(q)]);
-      d.seed = block_seed(f.level, f.t, f.s);
-      d.kscale = joint ? op->kd.scale : 0.0;
-    }
-    // one index array, the team kinds one after another (largest teams
-    // first), each kind's blocks in batch order (a stable partition)
-    std::vector<uint64_t> lofs(nq), lcount;
-    par_group_offsets(
-        int64_t(nq), kAcaTeamKinds, lofs.data(), lcount,
-        [&](int64_t q) { return kAcaTeamKinds - 1 - int(qteam[size_t(q)]); }, [](int64_t) { return uint64_t(1); });
-    AcaLists al;
-    size_t lpos[kAcaTeamKinds], lcnt[kAcaTeamKinds];
-    {
-      size_t base = 0;
-      for (int k = kAcaTeamKinds - 1; k >= 0; k--) {
-        lpos[k] = base;
-        lcnt[k] = size_t(lcount[size_t(kAcaTeamKinds - 1 - k)]);
-        base += lcnt[k];
-      }
-    }
-    std::vector<int32_t> lst(nq);
-#pragma omp parallel for schedule(static) num_threads(tq)
-    for (int64_t q = 0; q < int64_t(nq); q++) lst[lpos[qteam[size_t(q)]] + lofs[size_t(q)]] = int32_t(q);
     s_ws.ensure((ow + arena_doubles) * 8, st, "ACA workspace");
     s_bits.ensure(std::max<uint64_t>(ob, 1) * 4, st, "ACA bitmaps");
     s_lists.ensure(std::max<uint64_t>(ol, 1) * 4, st, "ACA index lists");
     double* ws = static_cast<double*>(s_ws.p);
-    CK(cudaMemcpyAsync(d_desc, desc.data(), desc.size() * sizeof(AcaBlockDesc), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(d_lists_idx, lst.data(), lst.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     AcaArgs a;
     a.lmap = d_lmap;
     a.P = P;
@@ -957,211 +949,301 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     a.bits = static_cast<uint32_t*>(s_bits.p);
     a.lists = static_cast<int32_t*>(s_lists.p);
     a.out = d_out;
-    // one persistent launch per team kind: teams take their blocks from a
-    // work queue; blocks whose rank outgrows their columns continue in the arena
-    CK(cudaMemsetAsync(s_ctr.p, 0, 64, st));
-    a.queue = static_cast<unsigned int*>(s_ctr.p);
-    a.arena_used = reinterpret_cast<unsigned long long*>(static_cast<char*>(s_ctr.p) + 32);
+    // one persistent launch per team kind: teams take their blocks from the
+    // kind's work queue; blocks whose rank outgrows their columns continue in
+    // the arena
+    a.queue = reinterpret_cast<unsigned int*>(static_cast<char*>(s_ctr.p) + 16);
+    a.arena_used = static_cast<unsigned long long*>(s_ctr.p);
     a.arena_off = int64_t(ow);
     a.arena_size = arena_doubles;
     a.max_ctas = sms * 16;
-    for (int k = 0; k < kAcaTeamKinds; k++) {
-      al.list[k] = d_lists_idx + lpos[k];
-      al.n[k] = int(lcnt[k]);
+    CK(cudaMemsetAsync(s_ctr.p, 0, kAcaCtrBytes, st));
+    // Runs of the batch: in a batch in size order each team kind holds one
+    // consecutive run (largest kind first).  The runs are launched in that
+    // order, each as soon as its descriptors are on the device (the large
+    // blocks' long compression starts first and the small kinds fill its
+    // tail), and each run is compacted (on the compaction stream) once its
+    // launch is done, the last-launched first.  Other batches (retries, small
+    // batches) are one run of every kind.
+    struct Run {
+      size_t b, e;
+      int kind;  // -1: every kind
+    };
+    std::vector<Run> runs;
+    bool by_kind = nq >= kAcaWaveMin;
+    for (size_t q = 1; by_kind && q < nq; q++) by_kind = qteam[q] <= qteam[q - 1];
+    if (by_kind) {
+      size_t cnt[kAcaTeamKinds] = {};
+      for (int8_t t : qteam) cnt[size_t(t)]++;
+      size_t b0 = 0;
+      for (int k = kAcaTeamKinds - 1; k >= 0; k--) {
+        if (cnt[k] > 0) runs.push_back({b0, b0 + cnt[k], k});
+        b0 += cnt[k];
+      }
+    } else {
+      runs.push_back({0, nq, -1});
     }
-    // the team kinds at once, on side streams forked from st and joined back
-    CK(cudaEventRecord(ev_a0, st));
+    EventSet rev(2 * kAcaTeamKinds);
+    auto ev_copy = [&](size_t r) { return rev.e[r]; };
+    auto ev_done = [&](int k) { return rev.e[size_t(kAcaTeamKinds + k)]; };
+    std::vector<int32_t> lst(nq);
+    for (size_t r = 0; r < runs.size(); r++) {
+      const size_t q0 = runs[r].b, nw = runs[r].e - q0;
+      const int tw = par_threads(int64_t(nw));
+#pragma omp parallel for schedule(static) num_threads(tw)
+      for (int64_t q = int64_t(q0); q < int64_t(q0 + nw); q++) {
+        const size_t g = batch[size_t(q)];
+        const hodlr_op* op = ops[size_t(job[g])];
+        const FarBlock& f = op->far[size_t(int64_t(g) - boff[size_t(job[g])])];
+        AcaBlockDesc& d = desc[size_t(q)];
+        d.t_map = tmap[g];
+        d.s_map = smap[g];
+        d.m = mm[g];
+        d.n = nn[g];
+        d.cap = cap[g];
+        // the pivot lists hold every rank the block can reach, also after it grows into the arena
+        d.lcap = std::min(mm[g], nn[g]);
+        d.ws = int64_t(qw[size_t(q)]);
+        d.bits = int64_t(qb[size_t(q)]);
+        d.lists = int64_t(ql[size_t(q)]);
+        d.seed = block_seed(f.level, f.t, f.s);
+        d.kscale = joint ? op->kd.scale : 0.0;
+      }
+      // the run's index list: the team kinds one after another (largest
+      // teams first), each kind's blocks in batch order (a stable partition)
+      AcaLists al;
+      for (int k = 0; k < kAcaTeamKinds; k++) {
+        al.list[k] = d_lists_idx;
+        al.n[k] = 0;
+      }
+      if (runs[r].kind >= 0) {
+#pragma omp parallel for schedule(static) num_threads(tw)
+        for (int64_t q = int64_t(q0); q < int64_t(q0 + nw); q++) lst[size_t(q)] = int32_t(q);
+        al.list[runs[r].kind] = d_lists_idx + q0;
+        al.n[runs[r].kind] = int(nw);
+      } else {
+        std::vector<uint64_t> lofs(nw), lcount;
+        par_group_offsets(
+            int64_t(nw), kAcaTeamKinds, lofs.data(), lcount,
+            [&](int64_t i) { return kAcaTeamKinds - 1 - int(qteam[q0 + size_t(i)]); },
+            [](int64_t) { return uint64_t(1); });
+        size_t lpos[kAcaTeamKinds];
+        size_t base = q0;
+        for (int k = kAcaTeamKinds - 1; k >= 0; k--) {
+          lpos[k] = base;
+          al.list[k] = d_lists_idx + base;
+          al.n[k] = int(lcount[size_t(kAcaTeamKinds - 1 - k)]);
+          base += size_t(al.n[k]);
+        }
+#pragma omp parallel for schedule(static) num_threads(tw)
+        for (int64_t i = 0; i < int64_t(nw); i++)
+          lst[lpos[qteam[q0 + size_t(i)]] + lofs[size_t(i)]] = int32_t(q0 + size_t(i));
+      }
+      CK(cudaMemcpyAsync(d_desc + q0, desc.data() + q0, nw * sizeof(AcaBlockDesc), cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(d_lists_idx + q0, lst.data() + q0, nw * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+      if (r == 0) CK(cudaEventRecord(ev_a0, st));  // the launches' span starts here
+      CK(cudaEventRecord(ev_copy(r), st));
+      for (int k = 0; k < kAcaTeamKinds; k++) {
+        if (runs[r].kind >= 0 && k != runs[r].kind) continue;
+        CK(cudaStreamWaitEvent(side.s[k], ev_copy(r), 0));
+        CK(launch_aca_kind(ndim, a, al, k, side.s[k]));
+        CK(cudaEventRecord(ev_done(k), side.s[k]));
+      }
+    }
+    // the main stream joins every kind's launch
     for (int k = 0; k < kAcaTeamKinds; k++) {
-      CK(cudaStreamWaitEvent(side.s[k], ev_a0, 0));
-      CK(launch_aca_kind(ndim, a, al, k, side.s[k]));
       CK(cudaEventRecord(side.e[k], side.s[k]));
       CK(cudaStreamWaitEvent(st, side.e[k], 0));
     }
     CK(cudaEventRecord(ev_a1, st));
-    out.resize(batch.size());
-    CK(cudaMemcpyAsync(out.data(), d_out, out.size() * sizeof(AcaOut), cudaMemcpyDeviceToHost, st));
+    // compaction of each run once its launch is done (the last-launched
+    // first), on the compaction stream
+    cudaStream_t cs = side.cs;
+    const bool ref64 = fp != Prec::kD && any_ref, dual = ref64 && fp == Prec::kF;
+    for (size_t rr = runs.size(); rr-- > 0;) {
+      const size_t q0 = runs[rr].b, nw = runs[rr].e - q0;
+      const int tw = par_threads(int64_t(nw));
+      for (int k = 0; k < kAcaTeamKinds; k++)
+        if (runs[rr].kind < 0 || k == runs[rr].kind) CK(cudaStreamWaitEvent(cs, ev_done(k), 0));
+      // into pageable memory: returns once the run's results are here
+      CK(cudaMemcpyAsync(out.data() + q0, d_out + q0, nw * sizeof(AcaOut), cudaMemcpyDeviceToHost, cs));
+      CK(cudaStreamSynchronize(cs));
+      // blocks that outgrew their columns go back with 4x the columns
+      int64_t novf = 0;
+#pragma omp parallel for schedule(static) reduction(+ : novf) num_threads(tw)
+      for (int64_t qi = int64_t(q0); qi < int64_t(q0 + nw); qi++) {
+        const size_t q = size_t(qi), g = batch[q];
+        if (out[q].flags & kAcaOverflow) {
+          cap[g] = std::min(std::min(mm[g], nn[g]), cap[g] * 4);
+          novf++;
+          continue;
+        }
+        hodlr_op* op = ops[size_t(job[g])];
+        const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
+        op->rank[b] = out[q].rank;
+        op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
+      }
+      if (novf > 0)
+        for (size_t q = q0; q < q0 + nw; q++)
+          if (out[q].flags & kAcaOverflow) retry.push_back(batch[q]);
+      // block i of the run: its op, its index there, and whether it is stored
+      auto blk = [&](int64_t i, hodlr_op*& op, size_t& b) -> bool {
+        const size_t q = q0 + size_t(i), g = batch[q];
+        op = ops[size_t(job[g])];
+        b = size_t(int64_t(g) - boff[size_t(job[g])]);
+        return !(out[q].flags & kAcaOverflow);
+      };
+      auto job_of = [&](int64_t i) { return int(job[batch[q0 + size_t(i)]]); };
+      // byte offsets within each operator's chunk of this run (batch order)
+      // and the position among the blocks compacted (dense or rank > 0)
+      std::vector<uint64_t> bytes, off(nw), kidx(nw + 1);
+      par_group_offsets(int64_t(nw), int(nops), off.data(), bytes, job_of, [&](int64_t i) -> uint64_t {
+        hodlr_op* op;
+        size_t b;
+        if (!blk(i, op, b)) return 0;
+        const size_t g = batch[q0 + size_t(i)];
+        return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], fp) +
+               far_v_bytes(nn[g], op->rank[b], op->dense[b], fp);
+      });
+      par_exclusive_scan(int64_t(nw), kidx.data(), [&](int64_t i) -> uint64_t {
+        hodlr_op* op;
+        size_t b;
+        return blk(i, op, b) && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
+      });
+      cds.resize(size_t(kidx[nw]));
+      // the FP64 copy of the same blocks, for operators that keep one: with
+      // FP32 factors both copies come from one compaction pass (the entries of
+      // a dense tile are evaluated once)
+      std::vector<uint64_t> bytes64, off64, kidx64;
+      if (ref64) {
+        off64.resize(nw);
+        kidx64.resize(nw + 1);
+        par_group_offsets(int64_t(nw), int(nops), off64.data(), bytes64, job_of, [&](int64_t i) -> uint64_t {
+          hodlr_op* op;
+          size_t b;
+          if (!blk(i, op, b) || !op->has_ref) return 0;
+          const size_t g = batch[q0 + size_t(i)];
+          return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD) +
+                 far_v_bytes(nn[g], op->rank[b], op->dense[b], Prec::kD);
+        });
+        par_exclusive_scan(int64_t(nw), kidx64.data(), [&](int64_t i) -> uint64_t {
+          hodlr_op* op;
+          size_t b;
+          return blk(i, op, b) && op->has_ref && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
+        });
+      }
+      std::vector<char*> chunk(nops, nullptr), chunk64(nops, nullptr);
+      for (size_t j = 0; j < nops; j++) {
+        if (bytes[j] > 0) {
+          chunk[j] = static_cast<char*>(ops[j]->mem.alloc(bytes[j], "far-field factors"));
+          ops[j]->far_chunks.push_back(chunk[j]);
+          CK(cudaMemsetAsync(chunk[j], 0, bytes[j], cs));  // tile padding rows must read as zero
+        }
+        if (ref64 && bytes64[j] > 0) {
+          chunk64[j] = static_cast<char*>(ops[j]->mem.alloc(bytes64[j], "far-field factors (FP64 reference)"));
+          CK(cudaMemsetAsync(chunk64[j], 0, bytes64[j], cs));
+        }
+      }
+#pragma omp parallel for schedule(static) num_threads(tw)
+      for (int64_t ii = 0; ii < int64_t(nw); ii++) {
+        const size_t i = size_t(ii), q = q0 + i;
+        const size_t g = batch[q];
+        if (out[q].flags & kAcaOverflow) continue;
+        hodlr_op* op = ops[size_t(job[g])];
+        const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
+        char* ch = chunk[size_t(job[g])];
+        CompactDesc c;
+        c.t_begin = tb[g];
+        c.s_begin = sb[g];
+        c.t_map = desc[q].t_map;
+        c.s_map = desc[q].s_map;
+        c.ws = out[q].cap ? out[q].ws : desc[q].ws;
+        const int32_t rk = std::max(op->rank[b], 0);
+        c.u_dst = ch + off[i];
+        c.v_dst = ch + off[i] + far_u_bytes(mm[g], nn[g], rk, op->dense[b], fp);
+        c.s_dst = nullptr;
+        if (fp == Prec::kB)
+          c.s_dst = reinterpret_cast<float*>(op->dense[b]
+                                                 ? ch + off[i] + far_u_data_bytes(mm[g], nn[g], rk, true, fp)
+                                                 : static_cast<char*>(c.v_dst) + far_v_data_bytes(nn[g], rk, false, fp));
+        c.m = mm[g];
+        c.n = nn[g];
+        c.rank = op->rank[b];
+        c.dense = op->dense[b];
+        c.cap = out[q].cap ? out[q].cap : desc[q].cap;
+        c.pad = 0;
+        c.kscale = desc[q].kscale;
+        c.u64_dst = c.v64_dst = nullptr;
+        if (dual && kidx64[i + 1] > kidx64[i]) {
+          char* ch64 = chunk64[size_t(job[g])];
+          c.u64_dst = ch64 + off64[i];
+          c.v64_dst = ch64 + off64[i] + far_u_bytes(mm[g], nn[g], rk, op->dense[b], Prec::kD);
+          op->uptr64[b] = c.u64_dst;
+          op->vptr64[b] = c.v64_dst;
+        }
+        op->uptr[b] = c.u_dst;
+        op->vptr[b] = c.v_dst;
+        if (kidx[i + 1] > kidx[i]) cds[size_t(kidx[i])] = c;
+      }
+      auto compact = [&](const std::vector<CompactDesc>& v, Prec to) {
+        for (size_t b0 = 0; b0 < v.size(); b0 += max_cd) {
+          const size_t k = std::min(max_cd, v.size() - b0);
+          CK(cudaMemcpyAsync(d_cd, v.data() + b0, k * sizeof(CompactDesc), cudaMemcpyHostToDevice, cs));
+          CK(cudaEventRecord(side.c0, cs));
+          CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(k), to, cs));
+          CK(cudaEventRecord(side.c1, cs));
+          CK(cudaStreamSynchronize(cs));  // d_cd is refilled next
+          float ms = 0.f;
+          CK(cudaEventElapsedTime(&ms, side.c0, side.c1));
+          t_compact += 1e-3 * double(ms);
+        }
+      };
+      compact(cds, fp);
+      // BF16 factors: the FP64 copy in a pass of its own
+      if (ref64 && !dual) {
+        bool any = false;
+        for (size_t j = 0; j < nops; j++) any = any || chunk64[j] != nullptr;
+        if (any) {
+          std::vector<CompactDesc> cd64(static_cast<size_t>(kidx64[nw]));
+#pragma omp parallel for schedule(static) num_threads(tw)
+          for (int64_t ii = 0; ii < int64_t(nw); ii++) {
+            const size_t i = size_t(ii), q = q0 + i;
+            if (kidx64[i + 1] == kidx64[i]) continue;  // not kept (no FP64 copy, overflow, or rank 0)
+            const size_t g = batch[q];
+            hodlr_op* op = ops[size_t(job[g])];
+            const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
+            char* ch = chunk64[size_t(job[g])];
+            CompactDesc c;
+            c.t_begin = tb[g];
+            c.s_begin = sb[g];
+            c.t_map = desc[q].t_map;
+            c.s_map = desc[q].s_map;
+            c.ws = out[q].cap ? out[q].ws : desc[q].ws;
+            c.u_dst = ch + off64[i];
+            c.v_dst = ch + off64[i] + far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD);
+            c.s_dst = nullptr;
+            c.m = mm[g];
+            c.n = nn[g];
+            c.rank = op->rank[b];
+            c.dense = op->dense[b];
+            c.cap = out[q].cap ? out[q].cap : desc[q].cap;
+            c.pad = 0;
+            c.kscale = desc[q].kscale;
+            c.u64_dst = c.v64_dst = nullptr;
+            op->uptr64[b] = c.u_dst;
+            op->vptr64[b] = c.v_dst;
+            cd64[size_t(kidx64[i])] = c;
+          }
+          compact(cd64, Prec::kD);
+        }
+      }
+    }
+    CK(cudaStreamSynchronize(cs));
     CK(cudaStreamSynchronize(st));
     {
       float ms = 0.f;
       CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
       t_kernel += 1e-3 * double(ms);
-    }
-    // compaction of the finished blocks: one chunk per operator and batch.
-    // Blocks that outgrew their columns go back with 4x the columns.
-    int64_t novf = 0;
-#pragma omp parallel for schedule(static) reduction(+ : novf) num_threads(tq)
-    for (int64_t qi = 0; qi < int64_t(nq); qi++) {
-      const size_t q = size_t(qi), g = batch[q];
-      if (out[q].flags & kAcaOverflow) {
-        cap[g] = std::min(std::min(mm[g], nn[g]), cap[g] * 4);
-        novf++;
-        continue;
-      }
-      hodlr_op* op = ops[size_t(job[g])];
-      const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
-      op->rank[b] = out[q].rank;
-      op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
-    }
-    if (novf > 0)
-      for (size_t q = 0; q < nq; q++)
-        if (out[q].flags & kAcaOverflow) retry.push_back(batch[q]);
-    // a finished block's op, its index there, and whether it is stored
-    auto blk = [&](int64_t q, hodlr_op*& op, size_t& b) -> bool {
-      const size_t g = batch[size_t(q)];
-      op = ops[size_t(job[g])];
-      b = size_t(int64_t(g) - boff[size_t(job[g])]);
-      return !(out[size_t(q)].flags & kAcaOverflow);
-    };
-    auto job_of = [&](int64_t q) { return int(job[batch[size_t(q)]]); };
-    // byte offsets within each operator's chunk (batch order) and the
-    // position among the blocks compacted (dense or rank > 0)
-    std::vector<uint64_t> bytes, off(nq), kidx(nq + 1);
-    par_group_offsets(int64_t(nq), int(nops), off.data(), bytes, job_of, [&](int64_t q) -> uint64_t {
-      hodlr_op* op;
-      size_t b;
-      if (!blk(q, op, b)) return 0;
-      const size_t g = batch[size_t(q)];
-      return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], fp) + far_v_bytes(nn[g], op->rank[b], op->dense[b], fp);
-    });
-    par_exclusive_scan(int64_t(nq), kidx.data(), [&](int64_t q) -> uint64_t {
-      hodlr_op* op;
-      size_t b;
-      return blk(q, op, b) && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
-    });
-    cds.resize(size_t(kidx[batch.size()]));
-    // the FP64 copy of the same blocks, for operators that keep one: with
-    // FP32 factors both copies come from one compaction pass (the entries of
-    // a dense tile are evaluated once)
-    const bool ref64 = fp != Prec::kD && any_ref, dual = ref64 && fp == Prec::kF;
-    std::vector<uint64_t> bytes64, off64, kidx64;
-    if (ref64) {
-      off64.resize(nq);
-      kidx64.resize(nq + 1);
-      par_group_offsets(int64_t(nq), int(nops), off64.data(), bytes64, job_of, [&](int64_t q) -> uint64_t {
-        hodlr_op* op;
-        size_t b;
-        if (!blk(q, op, b) || !op->has_ref) return 0;
-        const size_t g = batch[size_t(q)];
-        return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD) +
-               far_v_bytes(nn[g], op->rank[b], op->dense[b], Prec::kD);
-      });
-      par_exclusive_scan(int64_t(nq), kidx64.data(), [&](int64_t q) -> uint64_t {
-        hodlr_op* op;
-        size_t b;
-        return blk(q, op, b) && op->has_ref && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
-      });
-    }
-    std::vector<char*> chunk(nops, nullptr), chunk64(nops, nullptr);
-    for (size_t j = 0; j < nops; j++) {
-      if (bytes[j] > 0) {
-        chunk[j] = static_cast<char*>(ops[j]->mem.alloc(bytes[j], "far-field factors"));
-        ops[j]->far_chunks.push_back(chunk[j]);
-        CK(cudaMemsetAsync(chunk[j], 0, bytes[j], st));  // tile padding rows must read as zero
-      }
-      if (ref64 && bytes64[j] > 0) {
-        chunk64[j] = static_cast<char*>(ops[j]->mem.alloc(bytes64[j], "far-field factors (FP64 reference)"));
-        CK(cudaMemsetAsync(chunk64[j], 0, bytes64[j], st));
-      }
-    }
-#pragma omp parallel for schedule(static) num_threads(tq)
-    for (int64_t qi = 0; qi < int64_t(batch.size()); qi++) {
-      const size_t q = size_t(qi);
-      const size_t g = batch[q];
-      if (out[q].flags & kAcaOverflow) continue;
-      hodlr_op* op = ops[size_t(job[g])];
-      const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
-      char* ch = chunk[size_t(job[g])];
-      CompactDesc c;
-      c.t_begin = tb[g];
-      c.s_begin = sb[g];
-      c.t_map = desc[q].t_map;
-      c.s_map = desc[q].s_map;
-      c.ws = out[q].cap ? out[q].ws : desc[q].ws;
-      const int32_t rk = std::max(op->rank[b], 0);
-      c.u_dst = ch + off[q];
-      c.v_dst = ch + off[q] + far_u_bytes(mm[g], nn[g], rk, op->dense[b], fp);
-      c.s_dst = nullptr;
-      if (fp == Prec::kB)
-        c.s_dst = reinterpret_cast<float*>(op->dense[b]
-                                               ? ch + off[q] + far_u_data_bytes(mm[g], nn[g], rk, true, fp)
-                                               : static_cast<char*>(c.v_dst) + far_v_data_bytes(nn[g], rk, false, fp));
-      c.m = mm[g];
-      c.n = nn[g];
-      c.rank = op->rank[b];
-      c.dense = op->dense[b];
-      c.cap = out[q].cap ? out[q].cap : desc[q].cap;
-      c.pad = 0;
-      c.kscale = desc[q].kscale;
-      c.u64_dst = c.v64_dst = nullptr;
-      if (dual && kidx64[q + 1] > kidx64[q]) {
-        char* ch64 = chunk64[size_t(job[g])];
-        c.u64_dst = ch64 + off64[q];
-        c.v64_dst = ch64 + off64[q] + far_u_bytes(mm[g], nn[g], rk, op->dense[b], Prec::kD);
-        op->uptr64[b] = c.u64_dst;
-        op->vptr64[b] = c.v64_dst;
-      }
-      op->uptr[b] = c.u_dst;
-      op->vptr[b] = c.v_dst;
-      if (kidx[q + 1] > kidx[q]) cds[size_t(kidx[q])] = c;
-    }
-    for (size_t b0 = 0; b0 < cds.size(); b0 += max_cd) {
-      const size_t k = std::min(max_cd, cds.size() - b0);
-      CK(cudaMemcpyAsync(d_cd, cds.data() + b0, k * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
-      CK(cudaEventRecord(ev_a0, st));
-      CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(k), fp, st));
-      CK(cudaEventRecord(ev_a1, st));
-      CK(cudaStreamSynchronize(st));
-      float ms = 0.f;
-      CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
-      t_compact += 1e-3 * double(ms);
-    }
-    // BF16 factors: the FP64 copy in a pass of its own
-    if (ref64 && !dual) {
-      bool any = false;
-      for (size_t j = 0; j < nops; j++) any = any || chunk64[j] != nullptr;
-      if (any) {
-        std::vector<CompactDesc> cd64(static_cast<size_t>(kidx64[batch.size()]));
-#pragma omp parallel for schedule(static)
-        for (int64_t qi = 0; qi < int64_t(batch.size()); qi++) {
-          const size_t q = size_t(qi);
-          if (kidx64[q + 1] == kidx64[q]) continue;  // not kept (no FP64 copy, overflow, or rank 0)
-          const size_t g = batch[q];
-          hodlr_op* op = ops[size_t(job[g])];
-          const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
-          char* ch = chunk64[size_t(job[g])];
-          CompactDesc c;
-          c.t_begin = tb[g];
-          c.s_begin = sb[g];
-          c.t_map = desc[q].t_map;
-          c.s_map = desc[q].s_map;
-          c.ws = out[q].cap ? out[q].ws : desc[q].ws;
-          c.u_dst = ch + off64[q];
-          c.v_dst = ch + off64[q] + far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD);
-          c.s_dst = nullptr;
-          c.m = mm[g];
-          c.n = nn[g];
-          c.rank = op->rank[b];
-          c.dense = op->dense[b];
-          c.cap = out[q].cap ? out[q].cap : desc[q].cap;
-          c.pad = 0;
-          c.kscale = desc[q].kscale;
-          c.u64_dst = c.v64_dst = nullptr;
-          op->uptr64[b] = c.u_dst;
-          op->vptr64[b] = c.v_dst;
-          cd64[size_t(kidx64[q])] = c;
-        }
-        for (size_t b0 = 0; b0 < cd64.size(); b0 += max_cd) {
-          const size_t k = std::min(max_cd, cd64.size() - b0);
-          CK(cudaMemcpyAsync(d_cd, cd64.data() + b0, k * sizeof(CompactDesc), cudaMemcpyHostToDevice, st));
-          CK(cudaEventRecord(ev_a0, st));
-          CK(launch_compact(ndim, P, K, ws, d_lmap, d_cd, int(k), Prec::kD, st));
-          CK(cudaEventRecord(ev_a1, st));
-          CK(cudaStreamSynchronize(st));
-          float ms = 0.f;
-          CK(cudaEventElapsedTime(&ms, ev_a0, ev_a1));
-          t_compact += 1e-3 * double(ms);
-        }
-      }
     }
   }
 }

@@ -1868,6 +1868,29 @@ static void compact_d(const PointsDev& P, const KernelDev& K, const double* ws, 
     compact_kernel<D, float><<<unsigned(nblocks), 256, 0, st>>>(P, K, ws, lmap, blocks, nblocks);
 }
 
+template <int D>
+static cudaError_t compact_preload_d() {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, compact_kernel<D, double>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, compact_kernel<D, float>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, compact_bf16_kernel<D>);
+  return e;
+}
+
+cudaError_t compact_preload(int ndim) {
+  switch (ndim) {
+    case 1: return compact_preload_d<1>();
+    case 2: return compact_preload_d<2>();
+    case 3: return compact_preload_d<3>();
+    case 4: return compact_preload_d<4>();
+    case 5: return compact_preload_d<5>();
+    case 6: return compact_preload_d<6>();
+    case 7: return compact_preload_d<7>();
+    case 8: return compact_preload_d<8>();
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,
                            const CompactDesc* blocks, int nblocks, Prec op, cudaStream_t st) {
   if (nblocks <= 0) return cudaSuccess;

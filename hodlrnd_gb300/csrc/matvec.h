@@ -278,5 +278,8 @@ struct CompactDesc {
 // U row i (reference order) lands on tree row lmap[t_map + i] - t_begin; V likewise.
 cudaError_t launch_compact(int ndim, const PointsDev& P, const KernelDev& K, const double* ws, const int32_t* lmap,
                            const CompactDesc* blocks, int nblocks, Prec op, cudaStream_t st);
+// Loads the compaction kernels (before launches that overlap running kernels:
+// with lazy module loading a first launch would wait for those).
+cudaError_t compact_preload(int ndim);
 
 }  // namespace hodlr
