@@ -1975,99 +1975,158 @@ namespace {
 void build_batch_plan(hodlr_batch& b, cudaStream_t st) {
   Plan::Host h;
   const bool f32 = b.vec == Prec::kF;
-  int64_t in_base = 0, y_base = 0, x_base = 0, zpart = 0;
-  int64_t near_parts = 0, far_parts = 0;
-  std::vector<BatchInst> inst;
+  const size_t nops = b.ops.size();
+  // where each instance's records go in the merged arrays (prefix sums over
+  // the instances), then the records themselves, instances in parallel
+  struct Base {
+    int64_t panels_near = 0, segs_near = 0, small_near = 0, big_near = 0, pfix_near = 0, near_parts = 0;
+    int64_t panels_far = 0, segs_far = 0, small_far = 0, big_far = 0, pfix_far = 0, far_parts = 0;
+    int64_t zb = 0, zitems = 0, zfix = 0, zpart = 0, in = 0, y = 0, x = 0;
+  };
+  std::vector<Base> base(nops + 1);
+  std::vector<BatchInst> inst(nops);
   b.offsets.assign(1, 0);
-  for (hodlr_op* op : b.ops) {
+  bool contig_near = true, contig_far = true;
+  for (size_t j = 0; j < nops; j++) {
+    const hodlr_op* op = b.ops[j];
     const Plan& pn = f32 ? op->plan32 : op->plan64;  // near field and scratch sizes
     const Plan::Host& hn = *pn.host;
     const Plan::Host& hf = *op->plan64.host;  // far field (shared by both vector types)
-    BatchInst I;
+    const Base& a = base[j];
+    Base& e = base[j + 1];
+    BatchInst& I = inst[j];
     I.n = op->n;
-    I.x_base = x_base;
-    I.in_base = in_base;
-    I.y_base = y_base;
+    I.x_base = a.x;
+    I.in_base = a.in;
+    I.y_base = a.y;
     I.perm = op->d_perm;
     I.nslots = op->nslots;
     I.pad = 0;
-    inst.push_back(I);
-    // near field
-    const int rows_near = rows_per_item(pn.a_near);
-    const int32_t pb = int32_t(h.panels_near.size()), sbase = int32_t(h.segs_near.size());
-    for (Panel p : hn.panels_near) {
-      p.seg_begin += sbase;
-      p.seg_end += sbase;
-      p.yoff += y_base;
-      h.panels_near.push_back(p);
-    }
-    for (Seg s : hn.segs_near) {
-      s.in_off += in_base;
-      h.segs_near.push_back(s);
-    }
-    auto shift_item = [&](Item it, int32_t panel_base, int32_t seg_base, int64_t part_base) {
-      it.panel += panel_base;
-      it.seg_b += seg_base;
-      it.seg_e += seg_base;
-      if (it.part >= 0) it.part += int32_t(part_base);
-      return it;
-    };
-    for (const Item& it : hn.small_near) h.small_near.push_back(shift_item(it, pb, sbase, near_parts));
-    for (const Item& it : hn.big_near) h.big_near.push_back(shift_item(it, pb, sbase, near_parts));
-    for (PanelFix f : hn.pfix_near) {
-      f.panel += pb;
-      f.part += int32_t(near_parts);
-      h.pfix_near.push_back(f);
-    }
-    near_parts += pn.nypart_near / rows_near;
-    // far field
-    const int rows_far = rows_per_item(op->plan64.a_far);
-    const int32_t fpb = int32_t(h.panels_far.size()), fsb = int32_t(h.segs_far.size());
-    for (Panel p : hf.panels_far) {
-      p.seg_begin += fsb;
-      p.seg_end += fsb;
-      p.yoff += y_base;
-      h.panels_far.push_back(p);
-    }
-    for (Seg s : hf.segs_far) {
-      s.in_off += in_base;
-      h.segs_far.push_back(s);
-    }
-    for (const Item& it : hf.small_far) h.small_far.push_back(shift_item(it, fpb, fsb, far_parts));
-    for (const Item& it : hf.big_far) h.big_far.push_back(shift_item(it, fpb, fsb, far_parts));
+    e.panels_near = a.panels_near + int64_t(hn.panels_near.size());
+    e.segs_near = a.segs_near + int64_t(hn.segs_near.size());
+    e.small_near = a.small_near + int64_t(hn.small_near.size());
+    e.big_near = a.big_near + int64_t(hn.big_near.size());
+    e.pfix_near = a.pfix_near + int64_t(hn.pfix_near.size());
+    e.near_parts = a.near_parts + pn.nypart_near / rows_per_item(pn.a_near);
+    e.panels_far = a.panels_far + int64_t(hf.panels_far.size());
+    e.segs_far = a.segs_far + int64_t(hf.segs_far.size());
+    e.small_far = a.small_far + int64_t(hf.small_far.size());
+    e.big_far = a.big_far + int64_t(hf.big_far.size());
+    e.pfix_far = a.pfix_far + int64_t(hf.pfix_far.size());
     int64_t op_far_parts = 0;
-    for (PanelFix f : hf.pfix_far) {
-      op_far_parts += f.count;
-      f.panel += fpb;
-      f.part += int32_t(far_parts);
-      h.pfix_far.push_back(f);
-    }
-    far_parts += op_far_parts;
-    // V^T x
-    const int32_t zbb = int32_t(h.zb.size());
-    for (ZBlock z : hf.zb) {
-      z.x_off += in_base;
-      z.z_off += in_base;
-      h.zb.push_back(z);
-    }
-    for (ZItem it : hf.zitems) {
-      it.zb += zbb;
-      if (it.part >= 0) it.part += int32_t(zpart);
-      h.zitems.push_back(it);
-    }
-    for (ZFix f : hf.zfix) {
-      f.zpos += in_base;
-      f.part += int32_t(zpart);
-      h.zfix.push_back(f);
-    }
-    zpart += op->plan64.nzpart;
-    (void)rows_far;
-    in_base += op->n + op->zlen;
-    y_base += int64_t(op->nslots) * op->n;
-    x_base += op->n;
-    b.offsets.push_back(x_base);
+    for (const PanelFix& f : hf.pfix_far) op_far_parts += f.count;
+    e.far_parts = a.far_parts + op_far_parts;
+    e.zb = a.zb + int64_t(hf.zb.size());
+    e.zitems = a.zitems + int64_t(hf.zitems.size());
+    e.zfix = a.zfix + int64_t(hf.zfix.size());
+    e.zpart = a.zpart + op->plan64.nzpart;
+    e.in = a.in + op->n + op->zlen;
+    e.y = a.y + int64_t(op->nslots) * op->n;
+    e.x = a.x + op->n;
+    b.offsets.push_back(e.x);
     b.max_n = std::max(b.max_n, op->n);
+    // the merged items reference the same factor bytes, so their layout
+    // test is each instance's own
+    contig_near = contig_near && pn.contig_near;
+    contig_far = contig_far && op->plan64.contig_far;
   }
+  const Base& tot = base[nops];
+  h.panels_near.resize(size_t(tot.panels_near));
+  h.segs_near.resize(size_t(tot.segs_near));
+  h.small_near.resize(size_t(tot.small_near));
+  h.big_near.resize(size_t(tot.big_near));
+  h.pfix_near.resize(size_t(tot.pfix_near));
+  h.panels_far.resize(size_t(tot.panels_far));
+  h.segs_far.resize(size_t(tot.segs_far));
+  h.small_far.resize(size_t(tot.small_far));
+  h.big_far.resize(size_t(tot.big_far));
+  h.pfix_far.resize(size_t(tot.pfix_far));
+  h.zb.resize(size_t(tot.zb));
+  h.zitems.resize(size_t(tot.zitems));
+  h.zfix.resize(size_t(tot.zfix));
+  auto shift_item = [](Item it, int64_t panel_base, int64_t seg_base, int64_t part_base) {
+    it.panel += int32_t(panel_base);
+    it.seg_b += int32_t(seg_base);
+    it.seg_e += int32_t(seg_base);
+    if (it.part >= 0) it.part += int32_t(part_base);
+    return it;
+  };
+#pragma omp parallel for schedule(dynamic, 1) num_threads(std::max(1, std::min<int>(int(nops), 16)))
+  for (int64_t jj = 0; jj < int64_t(nops); jj++) {
+    const size_t j = size_t(jj);
+    const hodlr_op* op = b.ops[j];
+    const Plan& pn = f32 ? op->plan32 : op->plan64;
+    const Plan::Host& hn = *pn.host;
+    const Plan::Host& hf = *op->plan64.host;
+    const Base& a = base[j];
+    // near field
+    for (size_t k = 0; k < hn.panels_near.size(); k++) {
+      Panel p = hn.panels_near[k];
+      p.seg_begin += a.segs_near;
+      p.seg_end += a.segs_near;
+      p.yoff += a.y;
+      h.panels_near[size_t(a.panels_near) + k] = p;
+    }
+    for (size_t k = 0; k < hn.segs_near.size(); k++) {
+      Seg sg = hn.segs_near[k];
+      sg.in_off += a.in;
+      h.segs_near[size_t(a.segs_near) + k] = sg;
+    }
+    for (size_t k = 0; k < hn.small_near.size(); k++)
+      h.small_near[size_t(a.small_near) + k] = shift_item(hn.small_near[k], a.panels_near, a.segs_near, a.near_parts);
+    for (size_t k = 0; k < hn.big_near.size(); k++)
+      h.big_near[size_t(a.big_near) + k] = shift_item(hn.big_near[k], a.panels_near, a.segs_near, a.near_parts);
+    for (size_t k = 0; k < hn.pfix_near.size(); k++) {
+      PanelFix f = hn.pfix_near[k];
+      f.panel += int32_t(a.panels_near);
+      f.part += int32_t(a.near_parts);
+      h.pfix_near[size_t(a.pfix_near) + k] = f;
+    }
+    // far field
+    for (size_t k = 0; k < hf.panels_far.size(); k++) {
+      Panel p = hf.panels_far[k];
+      p.seg_begin += a.segs_far;
+      p.seg_end += a.segs_far;
+      p.yoff += a.y;
+      h.panels_far[size_t(a.panels_far) + k] = p;
+    }
+    for (size_t k = 0; k < hf.segs_far.size(); k++) {
+      Seg sg = hf.segs_far[k];
+      sg.in_off += a.in;
+      h.segs_far[size_t(a.segs_far) + k] = sg;
+    }
+    for (size_t k = 0; k < hf.small_far.size(); k++)
+      h.small_far[size_t(a.small_far) + k] = shift_item(hf.small_far[k], a.panels_far, a.segs_far, a.far_parts);
+    for (size_t k = 0; k < hf.big_far.size(); k++)
+      h.big_far[size_t(a.big_far) + k] = shift_item(hf.big_far[k], a.panels_far, a.segs_far, a.far_parts);
+    for (size_t k = 0; k < hf.pfix_far.size(); k++) {
+      PanelFix f = hf.pfix_far[k];
+      f.panel += int32_t(a.panels_far);
+      f.part += int32_t(a.far_parts);
+      h.pfix_far[size_t(a.pfix_far) + k] = f;
+    }
+    // V^T x
+    for (size_t k = 0; k < hf.zb.size(); k++) {
+      ZBlock z = hf.zb[k];
+      z.x_off += a.in;
+      z.z_off += a.in;
+      h.zb[size_t(a.zb) + k] = z;
+    }
+    for (size_t k = 0; k < hf.zitems.size(); k++) {
+      ZItem it = hf.zitems[k];
+      it.zb += int32_t(a.zb);
+      if (it.part >= 0) it.part += int32_t(a.zpart);
+      h.zitems[size_t(a.zitems) + k] = it;
+    }
+    for (size_t k = 0; k < hf.zfix.size(); k++) {
+      ZFix f = hf.zfix[k];
+      f.zpos += a.in;
+      f.part += int32_t(a.zpart);
+      h.zfix[size_t(a.zfix) + k] = f;
+    }
+  }
+  const int64_t in_base = tot.in, y_base = tot.y, x_base = tot.x, zpart = tot.zpart;
+  const int64_t near_parts = tot.near_parts, far_parts = tot.far_parts;
   if (in_base > (int64_t(1) << 31) || zpart > (int64_t(1) << 31))
     throw Failure{HODLR_ERR_INVALID, "hodlr_build_batch: the batch is too large for one merged plan"};
   b.ld_in = in_base;
@@ -2086,8 +2145,8 @@ void build_batch_plan(hodlr_batch& b, cudaStream_t st) {
   p.pfix_near = upload(b.mem, h.pfix_near, st, "batch near fix-ups");
   p.npfix_near = int(h.pfix_near.size());
   p.panels_far = upload(b.mem, h.panels_far, st, "batch far panels");
-  p.contig_near = small_items_contiguous(h.panels_near, h.segs_near, h.small_near, prec_size(p.a_near));
-  p.contig_far = p.a_far != Prec::kD && small_items_contiguous(h.panels_far, h.segs_far, h.small_far, prec_size(p.a_far));
+  p.contig_near = contig_near;
+  p.contig_far = p.a_far != Prec::kD && contig_far;
   p.segs_far = upload(b.mem, h.segs_far, st, "batch far segments");
   p.small_far = upload(b.mem, h.small_far, st, "batch far items");
   p.big_far = upload(b.mem, h.big_far, st, "batch far items");
