@@ -818,10 +818,26 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   // bitmap words and pivot list entries
   auto bits_need = [&](size_t g) { return uint64_t((mm[g] + 31) / 32 + (nn[g] + 31) / 32); };
   auto list_need = [&](size_t g) { return uint64_t(2 * (std::min(mm[g], nn[g]) + 2)); };
+  // (the sizes gathered into that order once, so that these passes and the
+  // batches' read them in sequence)
+  std::vector<int32_t> om(nb), on(nb), ocap(nb);
+#pragma omp parallel for schedule(static) num_threads(par_threads(int64_t(nb)))
+  for (int64_t i = 0; i < int64_t(nb); i++) {
+    const size_t g = todo[size_t(i)];
+    om[size_t(i)] = mm[g];
+    on[size_t(i)] = nn[g];
+    ocap[size_t(i)] = cap[g];
+  }
   std::vector<uint64_t> pw(nb + 1), pbits(nb + 1), plist(nb + 1);
-  par_exclusive_scan(int64_t(nb), pw.data(), [&](int64_t i) { return ws_need(todo[size_t(i)]); });
-  par_exclusive_scan(int64_t(nb), pbits.data(), [&](int64_t i) { return bits_need(todo[size_t(i)]); });
-  par_exclusive_scan(int64_t(nb), plist.data(), [&](int64_t i) { return list_need(todo[size_t(i)]); });
+  par_exclusive_scan(int64_t(nb), pw.data(), [&](int64_t i) {
+    return uint64_t(ocap[size_t(i)]) * uint64_t(om[size_t(i)] + on[size_t(i)]);
+  });
+  par_exclusive_scan(int64_t(nb), pbits.data(), [&](int64_t i) {
+    return uint64_t((om[size_t(i)] + 31) / 32 + (on[size_t(i)] + 31) / 32);
+  });
+  par_exclusive_scan(int64_t(nb), plist.data(), [&](int64_t i) {
+    return uint64_t(2 * (std::min(om[size_t(i)], on[size_t(i)]) + 2));
+  });
 
   KernelDev K{op0->kd.kind, op0->kd.scale, op0->kd.diag};
   // every kernel of the launches below loaded now, while the GPU is idle
@@ -882,6 +898,8 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   while (pos < todo.size() || !retry.empty()) {
     // next batch
     std::vector<size_t> batch;
+    size_t pos0 = 0;      // a run of the size order: its first position there
+    bool in_order = false;  // (else a list of blocks to retry)
     uint64_t acc_w = 0, acc_b = 0, acc_l = 0;
     auto take = [&](size_t g) {
       const uint64_t w = ws_need(g), bw = bits_need(g), lw = list_need(g);
@@ -915,6 +933,8 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
           hi = mid - 1;
       }
       batch.assign(todo.begin() + int64_t(pos), todo.begin() + int64_t(lo));
+      pos0 = pos;
+      in_order = true;
       pos = lo;
     }
     // descriptors: per-block sizes and teams (parallel: the blocks are visited
@@ -925,14 +945,25 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     desc.resize(nq);
     out.resize(nq);
     std::vector<uint64_t> qw(nq + 1), qb(nq + 1), ql(nq + 1);
-    par_exclusive_scan(int64_t(nq), qw.data(), [&](int64_t q) { return ws_need(batch[size_t(q)]); });
-    par_exclusive_scan(int64_t(nq), qb.data(), [&](int64_t q) { return bits_need(batch[size_t(q)]); });
-    par_exclusive_scan(int64_t(nq), ql.data(), [&](int64_t q) { return list_need(batch[size_t(q)]); });
     std::vector<int8_t> qteam(nq);
+    if (in_order) {  // the size order's prefix sums, from the batch's start
 #pragma omp parallel for schedule(static) num_threads(tq)
-    for (int64_t q = 0; q < int64_t(nq); q++) {
-      const size_t g = batch[size_t(q)];
-      qteam[size_t(q)] = int8_t(aca_team(mm[g], nn[g]));
+      for (int64_t q = 0; q <= int64_t(nq); q++) {
+        const size_t i = pos0 + size_t(q);
+        qw[size_t(q)] = pw[i] - pw[pos0];
+        qb[size_t(q)] = pbits[i] - pbits[pos0];
+        ql[size_t(q)] = plist[i] - plist[pos0];
+        if (q < int64_t(nq)) qteam[size_t(q)] = int8_t(aca_team(om[i], on[i]));
+      }
+    } else {
+      par_exclusive_scan(int64_t(nq), qw.data(), [&](int64_t q) { return ws_need(batch[size_t(q)]); });
+      par_exclusive_scan(int64_t(nq), qb.data(), [&](int64_t q) { return bits_need(batch[size_t(q)]); });
+      par_exclusive_scan(int64_t(nq), ql.data(), [&](int64_t q) { return list_need(batch[size_t(q)]); });
+#pragma omp parallel for schedule(static) num_threads(tq)
+      for (int64_t q = 0; q < int64_t(nq); q++) {
+        const size_t g = batch[size_t(q)];
+        qteam[size_t(q)] = int8_t(aca_team(mm[g], nn[g]));
+      }
     }
     const uint64_t ow = qw[nq], ob = qb[nq], ol = ql[nq];
     s_ws.ensure((ow + arena_doubles) * 8, st, "ACA workspace");
@@ -1068,11 +1099,24 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       // into pageable memory: returns once the run's results are here
       CK(cudaMemcpyAsync(out.data() + q0, d_out + q0, nw * sizeof(AcaOut), cudaMemcpyDeviceToHost, cs));
       CK(cudaStreamSynchronize(cs));
-      // blocks that outgrew their columns go back with 4x the columns
+      // Per block of the run, in one pass: its results into its operator,
+      // its operator, its stored bytes (FP32/BF16 and FP64 copies) and
+      // whether it is compacted (dense or rank > 0).  Blocks that outgrew
+      // their columns go back with 4x the columns.
+      std::vector<int32_t> bjob(nw);
+      std::vector<uint64_t> bsz(nw), bsz64(ref64 ? nw : 0);
+      std::vector<uint8_t> bkeep(nw), bkeep64(ref64 ? nw : 0);
       int64_t novf = 0;
 #pragma omp parallel for schedule(static) reduction(+ : novf) num_threads(tw)
-      for (int64_t qi = int64_t(q0); qi < int64_t(q0 + nw); qi++) {
-        const size_t q = size_t(qi), g = batch[q];
+      for (int64_t ii = 0; ii < int64_t(nw); ii++) {
+        const size_t i = size_t(ii), q = q0 + i, g = batch[q];
+        bjob[i] = job[g];
+        bsz[i] = 0;
+        bkeep[i] = 0;
+        if (ref64) {
+          bsz64[i] = 0;
+          bkeep64[i] = 0;
+        }
         if (out[q].flags & kAcaOverflow) {
           cap[g] = std::min(std::min(mm[g], nn[g]), cap[g] * 4);
           novf++;
@@ -1080,36 +1124,26 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
         }
         hodlr_op* op = ops[size_t(job[g])];
         const size_t b = size_t(int64_t(g) - boff[size_t(job[g])]);
-        op->rank[b] = out[q].rank;
-        op->dense[b] = (out[q].flags & kAcaDense) ? 1 : 0;
+        const int32_t r = out[q].rank;
+        const int8_t dn = (out[q].flags & kAcaDense) ? 1 : 0;
+        op->rank[b] = r;
+        op->dense[b] = dn;
+        bsz[i] = far_u_bytes(mm[g], nn[g], r, dn, fp) + far_v_bytes(nn[g], r, dn, fp);
+        bkeep[i] = (dn || r > 0) ? 1 : 0;
+        if (ref64 && op->has_ref) {
+          bsz64[i] = far_u_bytes(mm[g], nn[g], r, dn, Prec::kD) + far_v_bytes(nn[g], r, dn, Prec::kD);
+          bkeep64[i] = bkeep[i];
+        }
       }
       if (novf > 0)
         for (size_t q = q0; q < q0 + nw; q++)
           if (out[q].flags & kAcaOverflow) retry.push_back(batch[q]);
-      // block i of the run: its op, its index there, and whether it is stored
-      auto blk = [&](int64_t i, hodlr_op*& op, size_t& b) -> bool {
-        const size_t q = q0 + size_t(i), g = batch[q];
-        op = ops[size_t(job[g])];
-        b = size_t(int64_t(g) - boff[size_t(job[g])]);
-        return !(out[q].flags & kAcaOverflow);
-      };
-      auto job_of = [&](int64_t i) { return int(job[batch[q0 + size_t(i)]]); };
+      auto job_of = [&](int64_t i) { return int(bjob[size_t(i)]); };
       // byte offsets within each operator's chunk of this run (batch order)
-      // and the position among the blocks compacted (dense or rank > 0)
+      // and the position among the blocks compacted
       std::vector<uint64_t> bytes, off(nw), kidx(nw + 1);
-      par_group_offsets(int64_t(nw), int(nops), off.data(), bytes, job_of, [&](int64_t i) -> uint64_t {
-        hodlr_op* op;
-        size_t b;
-        if (!blk(i, op, b)) return 0;
-        const size_t g = batch[q0 + size_t(i)];
-        return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], fp) +
-               far_v_bytes(nn[g], op->rank[b], op->dense[b], fp);
-      });
-      par_exclusive_scan(int64_t(nw), kidx.data(), [&](int64_t i) -> uint64_t {
-        hodlr_op* op;
-        size_t b;
-        return blk(i, op, b) && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
-      });
+      par_group_offsets(int64_t(nw), int(nops), off.data(), bytes, job_of, [&](int64_t i) { return bsz[size_t(i)]; });
+      par_exclusive_scan(int64_t(nw), kidx.data(), [&](int64_t i) { return uint64_t(bkeep[size_t(i)]); });
       cds.resize(size_t(kidx[nw]));
       // the FP64 copy of the same blocks, for operators that keep one: with
       // FP32 factors both copies come from one compaction pass (the entries of
@@ -1118,19 +1152,9 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       if (ref64) {
         off64.resize(nw);
         kidx64.resize(nw + 1);
-        par_group_offsets(int64_t(nw), int(nops), off64.data(), bytes64, job_of, [&](int64_t i) -> uint64_t {
-          hodlr_op* op;
-          size_t b;
-          if (!blk(i, op, b) || !op->has_ref) return 0;
-          const size_t g = batch[q0 + size_t(i)];
-          return far_u_bytes(mm[g], nn[g], op->rank[b], op->dense[b], Prec::kD) +
-                 far_v_bytes(nn[g], op->rank[b], op->dense[b], Prec::kD);
-        });
-        par_exclusive_scan(int64_t(nw), kidx64.data(), [&](int64_t i) -> uint64_t {
-          hodlr_op* op;
-          size_t b;
-          return blk(i, op, b) && op->has_ref && (op->dense[b] || op->rank[b] > 0) ? 1 : 0;
-        });
+        par_group_offsets(int64_t(nw), int(nops), off64.data(), bytes64, job_of,
+                          [&](int64_t i) { return bsz64[size_t(i)]; });
+        par_exclusive_scan(int64_t(nw), kidx64.data(), [&](int64_t i) { return uint64_t(bkeep64[size_t(i)]); });
       }
       std::vector<char*> chunk(nops, nullptr), chunk64(nops, nullptr);
       for (size_t j = 0; j < nops; j++) {
