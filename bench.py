@@ -324,9 +324,20 @@ def run_gb300(args):
             engines[prec]["rel_residual_fp64_operator"] = float(
                 np.linalg.norm(b0 - others["fp64"] * X2[0].cpu().numpy()) / np.linalg.norm(b0))
 
-    # ---- single-RHS matvec throughput of each engine's operator
-    matvec = {p: matvec_rate(Mm, B[0], X2[0], stream)
-              for p, Mm in [(args.precision, M)] + list(others.items())}
+    # ---- single-RHS matvec throughput of each engine's operator: compensated
+    # products, and for FP32 and BF16 factors also the relaxed (plain FP32)
+    # products the solver's inner iterations use
+    ops_by_prec = dict([(args.precision, M)] + list(others.items()))
+    matvec = {p: matvec_rate(Mm, B[0], X2[0], stream) for p, Mm in ops_by_prec.items()}
+    for p in ("fp32_factors", "bf16_factors"):
+        if p in ops_by_prec:
+            ops_by_prec[p].set_relax("always")
+            matvec[p]["relaxed"] = matvec_rate(ops_by_prec[p], B[0], X2[0], stream)
+            ops_by_prec[p].set_relax(True)
+    if "fp32_factors" in matvec and "bf16_factors" in matvec:
+        f, b = matvec["fp32_factors"], matvec["bf16_factors"]
+        matvec["bf16_over_fp32_ms"] = {"compensated": round(b["ms"] / f["ms"], 3),
+                                       "relaxed": round(b["relaxed"]["ms"] / f["relaxed"]["ms"], 3)}
 
     # ---- accuracy of the headline solution against the FP64 operator
     acc = {}
