@@ -641,15 +641,9 @@ Prec far_prec(const hodlr_params& p) {
   return p.precision == HODLR_PREC_FP64 ? Prec::kD : p.precision == HODLR_PREC_BF16_FACTORS ? Prec::kB : Prec::kF;
 }
 
-// ACA of every far block of the given operators (one, or the instances of a
-// batch: their blocks share every launch), in workspace-bounded batches;
-// compacted factors go to per-batch chunks of each operator's memory (FP64 or
-// FP32) and op->uptr / op->vptr record where.  With several operators their
-// points and reference-order maps are concatenated for the launches, and each
-// block carries its operator's kernel scale.
-// Batches of at least kAcaWaveMin blocks (run_aca) are compacted kind by
+// Batches of at least kAcaRunMin blocks (run_aca) are compacted kind by
 // kind while the other kinds are still being compressed.
-constexpr size_t kAcaWaveMin = size_t(1) << 18;
+constexpr size_t kAcaRunMin = size_t(1) << 18;
 constexpr size_t kAcaCtrBytes = 32;  // the arena counter, then the kinds' queue counters (from byte 16)
 
 // Events without timing, destroyed with the set.
@@ -664,6 +658,12 @@ struct EventSet {
   }
 };
 
+// ACA of every far block of the given operators (one, or the instances of a
+// batch: their blocks share every launch), in workspace-bounded batches;
+// compacted factors go to chunks of each operator's memory (FP64 or FP32;
+// one per batch and team kind) and op->uptr / op->vptr record where.  With
+// several operators their points and reference-order maps are concatenated
+// for the launches, and each block carries its operator's kernel scale.
 void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
   const size_t nops = ops.size();
   hodlr_op* op0 = ops[0];
@@ -1001,7 +1001,7 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
       int kind;  // -1: every kind
     };
     std::vector<Run> runs;
-    bool by_kind = nq >= kAcaWaveMin;
+    bool by_kind = nq >= kAcaRunMin;
     for (size_t q = 1; by_kind && q < nq; q++) by_kind = qteam[q] <= qteam[q - 1];
     if (by_kind) {
       size_t cnt[kAcaTeamKinds] = {};
