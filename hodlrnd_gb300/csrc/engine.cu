@@ -713,8 +713,8 @@ void run_aca(const std::vector<hodlr_op*>& ops, cudaStream_t st) {
     cap[g] = std::min({mm[g], nn[g], cap0});
   }
   auto ws_need = [&](size_t g) { return uint64_t(cap[g]) * uint64_t(mm[g] + nn[g]); };
-  // Scratch of one batch: the FP64 workspace is bounded (4 GiB by default);
-  // a single block that needs more grows it.  Not counted against the
+  // Scratch of one batch: the FP64 workspace is bounded (its size below); a
+  // single block that needs more grows it.  Not counted against the
   // operators' memory: it is freed when the build returns.
   const size_t max_batch = size_t(1) << 23;
   struct Scratch {
