@@ -893,13 +893,16 @@ __global__ void __launch_bounds__(kLWarps * 32, HODLR_TUNE_L_MINB)
       const int32_t wcols = min(total, kLCols - cols);
       for (int c0 = 0; c0 < wcols; c0 += 32) {  // every lane takes part in the shuffles
         const int c = c0 + lane;
-        // the lane k whose share holds column c: the last with pre_k <= c
-        int k = 0;
-#pragma unroll
-        for (int b = 16; b > 0; b >>= 1) {
-          const int32_t pk = __shfl_sync(0xffffffffu, pre, k + b);  // k + b <= 31
-          if (pk <= c) k += b;
-        }
+        // the lane k whose share holds column c: the shares with columns are
+        // those of lanes 0, 1, ... in column order, so k is the number of
+        // shares starting before column c0, plus the shares starting in
+        // c0 .. c, minus one (one warp vote and one OR-reduction of the
+        // share starts, no search)
+        const bool owns = take > 0;
+        const int k0 = __popc(__ballot_sync(0xffffffffu, owns && pre < c0));
+        const uint32_t starts =
+            __reduce_or_sync(0xffffffffu, owns && pre >= c0 && pre < c0 + 32 ? 1u << (pre - c0) : 0u);
+        const int k = k0 - 1 + __popc(starts & (0xffffffffu >> (31 - lane)));
         const int32_t pk = __shfl_sync(0xffffffffu, pre, k);
         const int32_t jk = __shfl_sync(0xffffffffu, j0, k) + (c - pk);
         const int32_t sok = __shfl_sync(0xffffffffu, so, k);
